@@ -1,0 +1,177 @@
+/*
+ * sesgb.h -- C ABI of the GB300 Solvent-Excluded Surface build.
+ *
+ * Drop-in engine for the SES build of PlathC/SESDF: the reference's C++ classes
+ * bcs::Sesdf (full surface, sesdf/include/bcs/sesdf/sesdf.hpp:15-88) and
+ * bcs::Ssesdf (exterior only, sesdf/include/bcs/ssesdf/ssesdf.hpp:14-77) map onto
+ * the entry points below; include/bcs/ provides those classes over this ABI.
+ * All pointers are plain host or device pointers, all sizes are element counts
+ * unless stated otherwise, streams are passed as an opaque cudaStream_t value
+ * (void*, NULL = the legacy default stream). Every entry point returns
+ * SESGB_OK (0) or a negative status; sesgb_error_string() names a status and
+ * sesgb_last_error() gives the message of the last failure of a context.
+ */
+#ifndef SESGB_H
+#define SESGB_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SESGB_OK 0
+#define SESGB_ERR_INVALID -1   /* bad argument */
+#define SESGB_ERR_CUDA -2      /* a CUDA call failed */
+#define SESGB_ERR_OVERFLOW -3  /* a capacity was still exceeded after regrowing */
+#define SESGB_ERR_NOT_BUILT -4 /* results requested before a build */
+#define SESGB_ERR_TIMEOUT -5   /* a bounded device wait gave up */
+#define SESGB_ERR_MODE -6      /* request does not match the context's mode */
+
+#define SESGB_MODE_FULL 0     /* bcs::Sesdf */
+#define SESGB_MODE_EXTERIOR 1 /* bcs::Ssesdf */
+
+typedef struct sesgb_ctx sesgb_ctx;
+
+/* Build options; zero-initialise and set what you need. */
+typedef struct sesgb_options
+{
+    uint32_t max_neighbor_per_atom; /* neighbour slots per atom, 0 = 128 (BCS_SESDF_MAXNEIGHBORPERATOM) */
+    uint32_t max_intersections_per_circle; /* probes per circle used by the segment stage, 0 = 32 */
+    int32_t  device;                /* CUDA device, -1 = current */
+    uint32_t flags;                 /* SESGB_FLAG_* */
+} sesgb_options;
+
+/* Capture the build in a CUDA graph after its first run and replay it. */
+#define SESGB_FLAG_GRAPH 1u
+
+/* Output buffers of the full-surface build: field for field the reference's
+ * bcs::sesdf::SesdfData (sesdf/include/bcs/sesdf/graphics.hpp:39-66). Device pointers,
+ * valid until the next build or sesgb_destroy. */
+typedef struct sesgb_full_data
+{
+    uint32_t atomNb;
+    void *   atoms; /* float4[atomNb], atoms in reference-grid order */
+
+    uint32_t convexPatchNb;
+    void *   convexPatches; /* uint2[atomNb]: [start, end) sector range per atom */
+
+    uint32_t sectorNb;
+    void *   sectors; /* float4[sectorNb]: (axis, half angle) */
+
+    uint32_t segmentPatchNb;
+    void *   segmentPatches; /* uint4[segmentPatchNb]: (i, j, probe a, probe b) */
+
+    uint32_t circlePatchNb;
+    void *   circlePatches; /* uint2[circlePatchNb]: complete circles (i, j), i < j */
+
+    uint32_t concavePatchNb;
+    void *   concavePatchesPosition;  /* float4[concavePatchNb]: (x, y, z, +-1 or +-2) */
+    void *   concavePatchesId;        /* int4[concavePatchNb]: (i, j, k, neighbour count) */
+    void *   concavePatchesNeighbors; /* float4[32 * singular probes] */
+
+    float    probeRadius;
+    uint16_t maxConcaveNeighbors;
+} sesgb_full_data;
+
+/* Output buffers of the exterior-only build: the reference's
+ * bcs::ssesdf::SsesdfData (sesdf/include/bcs/ssesdf/graphics.hpp:29-48). */
+typedef struct sesgb_exterior_data
+{
+    uint32_t atomNb;
+    void *   atoms;
+
+    uint32_t circlePatchNb;
+    void *   circlePosition; /* float4: (torus centre, R) */
+    void *   circleAxis;     /* float4: (axis, probe radius) */
+    void *   circleVs;       /* float4: visibility sphere (centre - torus centre, radius) */
+
+    uint32_t concavePatchNb;
+    void *   concavePatchesPosition;
+    void *   concavePatchesId;
+    void *   concavePatchesNeighbors;
+
+    float    probeRadius;
+    uint16_t maxConcaveNeighbors;
+} sesgb_exterior_data;
+
+/* Counts and diagnostics of the last build. */
+typedef struct sesgb_counts
+{
+    uint32_t atoms;
+    uint32_t pairs;          /* directed circles (neighbour entries) */
+    uint32_t sectors;        /* visible directed circles */
+    uint32_t full_circles;   /* complete circles, i < j */
+    uint32_t partial_circles;/* partial circles, i < j */
+    uint32_t candidates;     /* (i, j, k) solved */
+    uint32_t probes;         /* concave patches */
+    uint32_t singular_probes;
+    uint32_t segments;
+    uint32_t tori;           /* exterior mode */
+    uint32_t max_neighbors;  /* largest neighbour count seen */
+    uint32_t truncated_atoms;/* atoms with more neighbours than the per-atom capacity (kept: the first ones) */
+    uint32_t truncated_circles; /* circles with more probes than max_intersections_per_circle */
+    uint32_t truncated_probe_neighbors; /* singular probes with more than 32 neighbours */
+    uint32_t degenerate_tori; /* torus axes parallel to z (the reference produces NaN there) */
+    uint32_t outside_atoms;  /* atoms outside the grid box given at creation */
+    uint32_t fp64_decisions[ 4 ]; /* predicates settled in double precision: neighbour, visibility, occlusion, probe neighbour */
+    uint32_t rebuilds;       /* capacity regrowths of the last build */
+} sesgb_counts;
+
+/* Reference-layout analysis buffers (sesdf/include/bcs/sesdf/sesdf.hpp:37-42). */
+#define SESGB_BUF_ATOM_INDICES 0      /* uint32[atomNb]: sorted id -> input id */
+#define SESGB_BUF_NEIGHBOR_COUNT 1    /* uint32[atomNb] */
+#define SESGB_BUF_NEIGHBOR_IDS 2      /* uint32[atomNb * max_neighbor_per_atom] */
+#define SESGB_BUF_VISIBILITY_STATUS 3 /* uint8[atomNb * max_neighbor_per_atom] (+1) */
+#define SESGB_BUF_GLOBAL_TO_TRIMMED 4 /* uint32[atomNb * max_neighbor_per_atom + 1] (full mode) */
+
+/* bcs::Sesdf::Sesdf / bcs::Ssesdf::Ssesdf (sesdf/src/sesdf/sesdf.cu:20-75,
+ * sesdf/src/ssesdf/ssesdf.cu:19-66). `atoms` is a host array of n float4
+ * (x, y, z, vdW radius) that stays owned by the caller and is read by every
+ * sesgb_build (it may be NULL when only sesgb_build_device is used). `aabb` is
+ * {min x, y, z, max x, y, z} (NULL: computed from `atoms` like getAabb,
+ * sesdf/src/core/molecule.cpp:132-143). */
+int sesgb_create( const float * atoms, uint32_t n, const float * aabb, float probe_radius, int mode,
+                  const sesgb_options * options, sesgb_ctx ** out );
+
+/* bcs::Sesdf::build (sesdf/src/sesdf/sesdf.cu:172-264): uploads the host atoms and
+ * builds; returns when the counts are known. */
+int sesgb_build( sesgb_ctx * ctx, void * stream );
+
+/* Same build from atoms already in device memory (float4[n]). */
+int sesgb_build_device( sesgb_ctx * ctx, const void * device_atoms, void * stream );
+
+/* Replaces the borrowed host atom pointer (same atom count). */
+int sesgb_set_host_atoms( sesgb_ctx * ctx, const float * atoms );
+
+/* bcs::Sesdf::getData (sesdf/src/sesdf/sesdf.cu:302-344) */
+int sesgb_get_full( sesgb_ctx * ctx, sesgb_full_data * out );
+/* bcs::Ssesdf::getData (sesdf/src/ssesdf/ssesdf.cu:212-232) */
+int sesgb_get_exterior( sesgb_ctx * ctx, sesgb_exterior_data * out );
+
+int sesgb_get_counts( sesgb_ctx * ctx, sesgb_counts * out );
+
+/* bcs::Sesdf::getAtomIndices (sesdf/src/sesdf/sesdf.cu:350): host copy of the
+ * sorted-to-input permutation. */
+int sesgb_atom_indices( sesgb_ctx * ctx, uint32_t * host_out );
+
+/* bcs::Sesdf::getD* analysis buffers (sesdf/src/sesdf/sesdf.cu:352-356): device
+ * pointer and size in bytes, in the reference's N x MaxNeighborPerAtom layout. */
+int sesgb_analysis_buffer( sesgb_ctx * ctx, int which, void ** device_ptr, uint64_t * bytes );
+
+/* Copies `bytes` from a device pointer returned by this library to host memory. */
+int sesgb_copy_to_host( sesgb_ctx * ctx, const void * device_ptr, void * host, uint64_t bytes );
+
+uint16_t sesgb_max_neighbor_per_atom( const sesgb_ctx * ctx );
+uint16_t sesgb_max_intersections_per_circle( const sesgb_ctx * ctx );
+uint16_t sesgb_max_intersection_neighbors( const sesgb_ctx * ctx );
+
+const char * sesgb_error_string( int status );
+const char * sesgb_last_error( const sesgb_ctx * ctx );
+void         sesgb_destroy( sesgb_ctx * ctx );
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SESGB_H */

@@ -1,0 +1,237 @@
+"""Python mirror of the drop-in API, over the C ABI of include/sesgb.h (ctypes).
+
+`SesBuild` follows bcs::Sesdf / bcs::Ssesdf (sesdf/include/bcs/sesdf/sesdf.hpp:15-88,
+sesdf/include/bcs/ssesdf/ssesdf.hpp:14-77): construction from atoms (x, y, z, vdW
+radius) and a probe radius, build(), and the output buffers. Outputs stay in
+device memory; fetch() copies them to numpy. There is no CPU fallback: without the
+CUDA library or a GPU every call raises.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+import threading
+
+import numpy as np
+
+from . import _build
+
+MODE_FULL = 0
+MODE_EXTERIOR = 1
+FLAG_GRAPH = 1
+
+BUF_ATOM_INDICES, BUF_NEIGHBOR_COUNT, BUF_NEIGHBOR_IDS, BUF_VISIBILITY_STATUS, BUF_GLOBAL_TO_TRIMMED = range(5)
+
+# every entry point include/sesgb.h declares
+EXPORTS = [
+    "sesgb_create", "sesgb_build", "sesgb_build_device", "sesgb_set_host_atoms", "sesgb_get_full",
+    "sesgb_get_exterior", "sesgb_get_counts", "sesgb_atom_indices", "sesgb_analysis_buffer", "sesgb_copy_to_host",
+    "sesgb_max_neighbor_per_atom", "sesgb_max_intersections_per_circle", "sesgb_max_intersection_neighbors",
+    "sesgb_error_string", "sesgb_last_error", "sesgb_destroy",
+]
+
+
+class SesgbError(RuntimeError):
+    pass
+
+
+class Options(ctypes.Structure):
+    _fields_ = [("max_neighbor_per_atom", ctypes.c_uint32), ("max_intersections_per_circle", ctypes.c_uint32),
+                ("device", ctypes.c_int32), ("flags", ctypes.c_uint32)]
+
+
+class FullData(ctypes.Structure):
+    _fields_ = [("atomNb", ctypes.c_uint32), ("atoms", ctypes.c_void_p),
+                ("convexPatchNb", ctypes.c_uint32), ("convexPatches", ctypes.c_void_p),
+                ("sectorNb", ctypes.c_uint32), ("sectors", ctypes.c_void_p),
+                ("segmentPatchNb", ctypes.c_uint32), ("segmentPatches", ctypes.c_void_p),
+                ("circlePatchNb", ctypes.c_uint32), ("circlePatches", ctypes.c_void_p),
+                ("concavePatchNb", ctypes.c_uint32), ("concavePatchesPosition", ctypes.c_void_p),
+                ("concavePatchesId", ctypes.c_void_p), ("concavePatchesNeighbors", ctypes.c_void_p),
+                ("probeRadius", ctypes.c_float), ("maxConcaveNeighbors", ctypes.c_uint16)]
+
+
+class ExteriorData(ctypes.Structure):
+    _fields_ = [("atomNb", ctypes.c_uint32), ("atoms", ctypes.c_void_p),
+                ("circlePatchNb", ctypes.c_uint32), ("circlePosition", ctypes.c_void_p),
+                ("circleAxis", ctypes.c_void_p), ("circleVs", ctypes.c_void_p),
+                ("concavePatchNb", ctypes.c_uint32), ("concavePatchesPosition", ctypes.c_void_p),
+                ("concavePatchesId", ctypes.c_void_p), ("concavePatchesNeighbors", ctypes.c_void_p),
+                ("probeRadius", ctypes.c_float), ("maxConcaveNeighbors", ctypes.c_uint16)]
+
+
+COUNT_FIELDS = ["atoms", "pairs", "sectors", "full_circles", "partial_circles", "candidates", "probes",
+                "singular_probes", "segments", "tori", "max_neighbors", "truncated_atoms", "truncated_circles",
+                "truncated_probe_neighbors", "degenerate_tori", "outside_atoms"]
+
+
+class Counts(ctypes.Structure):
+    _fields_ = [(f, ctypes.c_uint32) for f in COUNT_FIELDS] + [("fp64_decisions", ctypes.c_uint32 * 4),
+                                                               ("rebuilds", ctypes.c_uint32)]
+
+
+_lib = None
+_lock = threading.Lock()
+
+
+def load_library(path: str | None = None) -> ctypes.CDLL:
+    """Loads libsesgb.so (built in-tree); raises if it is missing."""
+    global _lib
+    with _lock:
+        if _lib is not None:
+            return _lib
+        path = path or _build.LIB
+        if not os.path.exists(path):
+            raise SesgbError(f"CUDA library not built: {path} (run __graft_entry__.build())")
+        lib = ctypes.CDLL(path)
+        P, U32, I32, F32 = ctypes.c_void_p, ctypes.c_uint32, ctypes.c_int, ctypes.c_float
+        lib.sesgb_create.argtypes = [P, U32, P, F32, I32, ctypes.POINTER(Options), ctypes.POINTER(P)]
+        lib.sesgb_build.argtypes = [P, P]
+        lib.sesgb_build_device.argtypes = [P, P, P]
+        lib.sesgb_set_host_atoms.argtypes = [P, P]
+        lib.sesgb_get_full.argtypes = [P, ctypes.POINTER(FullData)]
+        lib.sesgb_get_exterior.argtypes = [P, ctypes.POINTER(ExteriorData)]
+        lib.sesgb_get_counts.argtypes = [P, ctypes.POINTER(Counts)]
+        lib.sesgb_atom_indices.argtypes = [P, P]
+        lib.sesgb_analysis_buffer.argtypes = [P, I32, ctypes.POINTER(P), ctypes.POINTER(ctypes.c_uint64)]
+        lib.sesgb_copy_to_host.argtypes = [P, P, P, ctypes.c_uint64]
+        for f in ("sesgb_max_neighbor_per_atom", "sesgb_max_intersections_per_circle", "sesgb_max_intersection_neighbors"):
+            getattr(lib, f).argtypes = [P]
+            getattr(lib, f).restype = ctypes.c_uint16
+        lib.sesgb_error_string.argtypes = [I32]
+        lib.sesgb_error_string.restype = ctypes.c_char_p
+        lib.sesgb_last_error.argtypes = [P]
+        lib.sesgb_last_error.restype = ctypes.c_char_p
+        lib.sesgb_destroy.argtypes = [P]
+        lib.sesgb_destroy.restype = None
+        _lib = lib
+    return _lib
+
+
+def aabb(atoms: np.ndarray) -> np.ndarray:
+    """getAabb (sesdf/src/core/molecule.cpp:132-143) in float32."""
+    a = np.asarray(atoms, np.float32).reshape(-1, 4)
+    if a.shape[0] == 0:
+        return np.zeros(6, np.float32)
+    lo = (a[:, :3] - a[:, 3:4]).min(0)
+    hi = (a[:, :3] + a[:, 3:4]).max(0)
+    return np.concatenate([lo, hi]).astype(np.float32)
+
+
+class SesBuild:
+    """One SES build context (bcs::Sesdf for mode "full", bcs::Ssesdf for "exterior")."""
+
+    def __init__(self, atoms: np.ndarray, probe_radius: float = 1.4, mode: str = "full", box=None,
+                 max_neighbor_per_atom: int = 0, max_intersections_per_circle: int = 0, graph: bool = False,
+                 device: int = -1):
+        self._lib = load_library()
+        self.atoms = np.ascontiguousarray(np.asarray(atoms, np.float32).reshape(-1, 4))
+        self.mode = mode
+        self.probe_radius = float(probe_radius)
+        bx = None if box is None else np.ascontiguousarray(box, np.float32)
+        self.box = aabb(self.atoms) if bx is None else bx
+        opt = Options(max_neighbor_per_atom, max_intersections_per_circle, device, FLAG_GRAPH if graph else 0)
+        h = ctypes.c_void_p()
+        st = self._lib.sesgb_create(self.atoms.ctypes.data if self.atoms.size else None, self.atoms.shape[0],
+                                    self.box.ctypes.data, ctypes.c_float(probe_radius),
+                                    MODE_FULL if mode == "full" else MODE_EXTERIOR, ctypes.byref(opt), ctypes.byref(h))
+        self._h = h
+        self._check(st, "create")
+
+    def _check(self, st: int, what: str):
+        if st != 0:
+            msg = self._lib.sesgb_error_string(st).decode()
+            detail = self._lib.sesgb_last_error(self._h).decode() if self._h else ""
+            raise SesgbError(f"{what}: {msg} ({detail})")
+
+    def set_atoms(self, atoms: np.ndarray):
+        a = np.ascontiguousarray(np.asarray(atoms, np.float32).reshape(-1, 4))
+        if a.shape != self.atoms.shape:
+            raise ValueError("atom count is fixed at construction")
+        self.atoms = a
+        self._check(self._lib.sesgb_set_host_atoms(self._h, a.ctypes.data), "set_atoms")
+
+    def build(self, stream: int | None = None):
+        self._check(self._lib.sesgb_build(self._h, stream), "build")
+
+    def build_device(self, device_ptr: int, stream: int | None = None):
+        self._check(self._lib.sesgb_build_device(self._h, device_ptr, stream), "build_device")
+
+    def counts(self) -> dict:
+        c = Counts()
+        self._check(self._lib.sesgb_get_counts(self._h, ctypes.byref(c)), "counts")
+        d = {f: int(getattr(c, f)) for f in COUNT_FIELDS}
+        d["fp64_decisions"] = [int(x) for x in c.fp64_decisions]
+        d["rebuilds"] = int(c.rebuilds)
+        return d
+
+    def data(self):
+        if self.mode == "full":
+            d = FullData()
+            self._check(self._lib.sesgb_get_full(self._h, ctypes.byref(d)), "getData")
+        else:
+            d = ExteriorData()
+            self._check(self._lib.sesgb_get_exterior(self._h, ctypes.byref(d)), "getData")
+        return d
+
+    def _copy(self, ptr, count: int, dtype, width: int = 1) -> np.ndarray:
+        out = np.empty((count, width) if width > 1 else count, dtype=dtype)
+        if count:
+            self._check(self._lib.sesgb_copy_to_host(self._h, ptr, out.ctypes.data, out.nbytes), "copy")
+        return out
+
+    def analysis(self, which: int, dtype, width: int = 1) -> np.ndarray:
+        p = ctypes.c_void_p()
+        nb = ctypes.c_uint64()
+        self._check(self._lib.sesgb_analysis_buffer(self._h, which, ctypes.byref(p), ctypes.byref(nb)), "analysis")
+        n = nb.value // np.dtype(dtype).itemsize
+        return self._copy(p, n, dtype)
+
+    @property
+    def max_neighbor_per_atom(self) -> int:
+        return int(self._lib.sesgb_max_neighbor_per_atom(self._h))
+
+    def fetch(self, analysis: bool = True) -> dict:
+        """Host copies of every output buffer (and the analysis buffers)."""
+        c = self.counts()
+        d = self.data()
+        out = {"counts": c, "atoms": self._copy(d.atoms, d.atomNb, np.float32, 4)}
+        Q = c["singular_probes"]
+        out["probe_pos"] = self._copy(d.concavePatchesPosition, d.concavePatchNb, np.float32, 4)
+        out["probe_ids"] = self._copy(d.concavePatchesId, d.concavePatchNb, np.int32, 4)
+        out["probe_nbrs"] = self._copy(d.concavePatchesNeighbors, 32 * Q, np.float32, 4)
+        if self.mode == "full":
+            out["convex"] = self._copy(d.convexPatches, d.convexPatchNb, np.uint32, 2)
+            out["sectors"] = self._copy(d.sectors, d.sectorNb, np.float32, 4)
+            out["segments"] = self._copy(d.segmentPatches, d.segmentPatchNb, np.uint32, 4)
+            out["full"] = self._copy(d.circlePatches, d.circlePatchNb, np.uint32, 2)
+        else:
+            out["tori_pos"] = self._copy(d.circlePosition, d.circlePatchNb, np.float32, 4)
+            out["tori_axis"] = self._copy(d.circleAxis, d.circlePatchNb, np.float32, 4)
+            out["tori_vs"] = self._copy(d.circleVs, d.circlePatchNb, np.float32, 4)
+        if analysis:
+            out["perm"] = self.analysis(BUF_ATOM_INDICES, np.uint32)
+            out["nbr_count"] = self.analysis(BUF_NEIGHBOR_COUNT, np.uint32)
+            out["nbr_ids"] = self.analysis(BUF_NEIGHBOR_IDS, np.uint32).reshape(d.atomNb, -1)
+            st = self.analysis(BUF_VISIBILITY_STATUS, np.uint8)
+            out["status"] = st[: d.atomNb * self.max_neighbor_per_atom].reshape(d.atomNb, -1)
+            if self.mode == "full":
+                out["global_to_trimmed"] = self.analysis(BUF_GLOBAL_TO_TRIMMED, np.uint32)
+        return out
+
+    def close(self):
+        if getattr(self, "_h", None) and self._h.value:
+            self._lib.sesgb_destroy(self._h)
+            self._h = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *exc):
+        self.close()

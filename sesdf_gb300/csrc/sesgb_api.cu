@@ -1,0 +1,638 @@
+// sesgb_api.cu -- host orchestration of the SES build and the C ABI of include/sesgb.h.
+//
+// One build is a fixed sequence of launches on one stream with no host
+// synchronisation until the final read of the counters (the reference reads
+// counts back seven times per build and allocates its outputs per build,
+// sesdf/src/sesdf/sesdf.cu:172-264). Count-dependent buffers are allocated
+// with a capacity; every kernel bounds its writes by it and raises an overflow
+// bit instead. After a build whose counters show an overflow, the affected
+// buffers are regrown to the exact counts (plus a margin) and the build is
+// run again, so the first build of a new molecule may run twice.
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/sesgb.h"
+#include "sesgb_stages.cuh"
+
+using namespace sesgb;
+
+struct sesgb_ctx
+{
+    int           device = -1;
+    int           mode   = 0;
+    uint32_t      n      = 0;
+    float         rp     = 1.4f;
+    uint32_t      flags  = 0;
+    const float * hostAtoms = nullptr;
+    float         aabb[ 6 ] {};
+    int           gridBits = 0;
+
+    Build          b {};
+    DeviceCounts * hCounts = nullptr;
+    void *         scanScratch = nullptr;
+    size_t         scanScratchBytes = 0;
+    void *         radixScratch = nullptr;
+    uint32_t *     g2t = nullptr;
+
+    std::vector<void *> fixedAllocs, dynAllocs;
+    bool                built = false;
+    uint32_t            rebuilds = 0;
+    std::string         err;
+
+    // graph replay
+    cudaGraph_t     graph = nullptr;
+    cudaGraphExec_t graphExec = nullptr;
+    cudaStream_t    graphStream = nullptr;
+    const void *    graphAtoms = nullptr;
+};
+
+namespace
+{
+    const char * kStatusNames[] = { "ok", "invalid argument", "CUDA error", "capacity overflow", "not built", "timeout",
+                                    "wrong mode" };
+
+    bool cuda_ok( sesgb_ctx * c, cudaError_t e, const char * what )
+    {
+        if ( e == cudaSuccess )
+            return true;
+        c->err = std::string( what ) + ": " + cudaGetErrorString( e );
+        return false;
+    }
+
+    template<class T> T * dalloc( sesgb_ctx * c, std::vector<void *> & list, size_t count, bool & ok )
+    {
+        void * p = nullptr;
+        if ( !ok )
+            return nullptr;
+        if ( !cuda_ok( c, cudaMalloc( &p, std::max<size_t>( count, 1 ) * sizeof( T ) ), "cudaMalloc" ) )
+        {
+            ok = false;
+            return nullptr;
+        }
+        list.push_back( p );
+        return static_cast<T *>( p );
+    }
+
+    void free_list( std::vector<void *> & list )
+    {
+        for ( void * p : list )
+            cudaFree( p );
+        list.clear();
+    }
+
+    uint32_t floor_log2( uint64_t v )
+    {
+        uint32_t e = 0;
+        while ( v >>= 1 )
+            e++;
+        return e;
+    }
+    uint32_t next_pow2( uint64_t v )
+    {
+        uint64_t i = 1;
+        while ( v > i )
+            i <<= 1;
+        return (uint32_t)i;
+    }
+
+    // getAabb (sesdf/src/core/molecule.cpp:132-143)
+    void host_aabb( const float * atoms, uint32_t n, float * out )
+    {
+        for ( int a = 0; a < 3; a++ )
+        {
+            out[ a ]     = 3.402823466e+38f;
+            out[ 3 + a ] = -3.402823466e+38f;
+        }
+        for ( uint32_t i = 0; i < n; i++ )
+            for ( int a = 0; a < 3; a++ )
+            {
+                out[ a ]     = std::min( out[ a ], atoms[ 4 * i + a ] - atoms[ 4 * i + 3 ] );
+                out[ 3 + a ] = std::max( out[ 3 + a ], atoms[ 4 * i + a ] + atoms[ 4 * i + 3 ] );
+            }
+    }
+
+    // reference grid of Sesdf::Sesdf (sesdf/src/sesdf/sesdf.cu:23-33)
+    void setup_grid( sesgb_ctx * c )
+    {
+        const float maxVdw = 3.48f;
+        const uint32_t gs  = next_pow2( floor_log2( c->n ) );
+        for ( int a = 0; a < 3; a++ )
+        {
+            const float origin = ( c->aabb[ a ] - maxVdw ) - c->rp;
+            const float size   = std::fabs( ( ( c->aabb[ 3 + a ] + maxVdw ) + c->rp ) - origin );
+            ( &c->b.grid.origin.x )[ a ] = origin;
+            ( &c->b.grid.cell.x )[ a ]   = size / (float)gs;
+        }
+        c->b.grid.size = (int)gs;
+        c->gridBits    = 3 * (int)floor_log2( gs );
+    }
+
+    uint32_t grow( uint64_t need ) { return (uint32_t)std::min<uint64_t>( need + need / 4 + 1024, 0xfffffff0ull ); }
+
+    bool allocate_fixed( sesgb_ctx * c )
+    {
+        Build &        b  = c->b;
+        const size_t   n  = c->n;
+        bool           ok = true;
+        auto &         L  = c->fixedAllocs;
+        b.atomsIn         = dalloc<float4>( c, L, n, ok );
+        b.atoms           = dalloc<float4>( c, L, n, ok );
+        b.perm            = dalloc<uint32_t>( c, L, n, ok );
+        b.keys            = dalloc<uint32_t>( c, L, n, ok );
+        b.fine            = dalloc<FineGrid>( c, L, 1, ok );
+        b.capCells        = (uint32_t)std::max<size_t>( 1u << 16, 4 * n );
+        b.cellCount       = dalloc<uint32_t>( c, L, b.capCells + 1ull, ok );
+        b.cellStart       = dalloc<uint32_t>( c, L, b.capCells + 1ull, ok );
+        b.cellCursor      = dalloc<uint32_t>( c, L, b.capCells + 1ull, ok );
+        b.nbr             = dalloc<uint32_t>( c, L, n * b.cap, ok );
+        b.nbrCount        = dalloc<uint32_t>( c, L, n + 1, ok );
+        b.status          = dalloc<uint8_t>( c, L, n * b.cap + 1, ok );
+        b.slotTrim        = dalloc<uint32_t>( c, L, n * b.cap, ok );
+        uint32_t ** per[] = { &b.visCnt, &b.partCnt, &b.fullCnt, &b.torCnt, &b.visOff, &b.partOff, &b.fullOff, &b.torOff };
+        for ( uint32_t ** p : per )
+            *p = dalloc<uint32_t>( c, L, n + 1, ok );
+        b.convex = dalloc<uint2>( c, L, n, ok );
+        b.counts = dalloc<DeviceCounts>( c, L, 1, ok );
+        if ( ok && !cuda_ok( c, cudaMallocHost( &c->hCounts, sizeof( DeviceCounts ) ), "cudaMallocHost" ) )
+            ok = false;
+        c->radixScratch = dalloc<char>( c, L, radix_scratch_bytes( c->n ), ok );
+        if ( ok )
+        {
+            cudaMemset( b.status, 0, n * b.cap + 1 );
+            cudaMemset( b.nbrCount, 0, sizeof( uint32_t ) * ( n + 1 ) );
+        }
+        return ok;
+    }
+
+    bool allocate_dynamic( sesgb_ctx * c )
+    {
+        free_list( c->dynAllocs );
+        Build &      b  = c->b;
+        bool         ok = true;
+        auto &       L  = c->dynAllocs;
+        const size_t C1 = b.capC1, CC = b.capCand, PR = b.capProbes;
+        b.sectors     = dalloc<float4>( c, L, b.capSectors, ok );
+        b.fullCircles = dalloc<uint2>( c, L, b.capFull, ok );
+        b.trimSlot    = dalloc<uint32_t>( c, L, C1, ok );
+        b.candCnt     = dalloc<uint32_t>( c, L, C1 + 1, ok );
+        b.candOff     = dalloc<uint32_t>( c, L, C1 + 1, ok );
+        b.cand        = dalloc<uint4>( c, L, CC, ok );
+        b.isSing      = dalloc<uint32_t>( c, L, 2 * CC + 1, ok );
+        b.isReg       = dalloc<uint32_t>( c, L, 2 * CC + 1, ok );
+        b.slotPos     = dalloc<float4>( c, L, 2 * CC, ok );
+        b.slotCid     = dalloc<int4>( c, L, 2 * CC, ok );
+        b.probeIds    = dalloc<int4>( c, L, PR, ok );
+        b.probePos    = dalloc<float4>( c, L, PR, ok );
+        b.probeCid    = dalloc<int4>( c, L, PR, ok );
+        b.probeNbrs   = dalloc<float4>( c, L, PR * kMaxProbeNbr, ok );
+        b.ccount      = dalloc<uint32_t>( c, L, C1 + 1, ok );
+        b.cstart      = dalloc<uint32_t>( c, L, C1 + 1, ok );
+        b.ccursor     = dalloc<uint32_t>( c, L, C1 + 1, ok );
+        b.clist       = dalloc<uint32_t>( c, L, 3 * PR, ok );
+        b.segCnt      = dalloc<uint32_t>( c, L, C1 + 1, ok );
+        b.segOff      = dalloc<uint32_t>( c, L, C1 + 1, ok );
+        b.segments    = dalloc<uint4>( c, L, b.capSeg, ok );
+        b.torPos      = dalloc<float4>( c, L, b.capTori, ok );
+        b.torAxis     = dalloc<float4>( c, L, b.capTori, ok );
+        b.torVs       = dalloc<float4>( c, L, b.capTori, ok );
+        const size_t items = std::max<size_t>( c->n, PR );
+        b.cellItems = dalloc<uint32_t>( c, L, items, ok );
+        b.cellPos   = dalloc<float4>( c, L, items, ok );
+        const uint64_t scanMax = std::max<uint64_t>( { (uint64_t)c->n + 1, C1 + 1, 2 * CC + 1, (uint64_t)b.capCells + 1 } );
+        c->scanScratchBytes    = scan_scratch_bytes( scanMax );
+        c->scanScratch         = dalloc<char>( c, L, c->scanScratchBytes, ok );
+        return ok;
+    }
+
+    void destroy_graph( sesgb_ctx * c )
+    {
+        if ( c->graphExec )
+            cudaGraphExecDestroy( c->graphExec );
+        if ( c->graph )
+            cudaGraphDestroy( c->graph );
+        c->graphExec = nullptr;
+        c->graph     = nullptr;
+    }
+
+    // all launches of one build; no host synchronisation inside
+    void enqueue( sesgb_ctx * c, cudaStream_t s )
+    {
+        Build &     b    = c->b;
+        const auto  n    = c->n;
+        void *      sc   = c->scanScratch;
+        DeviceCounts * d = b.counts;
+        cudaMemsetAsync( d, 0, sizeof( DeviceCounts ), s );
+        if ( n == 0 )
+            return;
+
+        // A: reference-grid order, neighbour grid, neighbour lists
+        launch_hash( b, s );
+        radix_sort( b.keys, b.perm, n, c->gridBits, c->radixScratch, s );
+        launch_fine_params( b, -1.f, n, s );
+        launch_gather( b, s );
+        launch_cells( b, b.atoms, n, nullptr, sc, s );
+        launch_neighbors( b, s );
+
+        // B, C: visibility, sectors, complete and partial circles
+        launch_visibility( b, s );
+        exclusive_scan( b.visCnt, b.visOff, n, nullptr, &d->V, sc, s );
+        exclusive_scan( b.partCnt, b.partOff, n, nullptr, &d->C1, sc, s );
+        exclusive_scan( b.fullCnt, b.fullOff, n, nullptr, &d->F, sc, s );
+        exclusive_scan( b.nbrCount, b.torOff, n, nullptr, &d->P, sc, s );
+        launch_emit( b, s );
+
+        // D, E: probes
+        launch_candidates( b, false, s );
+        exclusive_scan( b.candCnt, b.candOff, b.capC1, &d->C1, &d->cand, sc, s );
+        launch_candidates( b, true, s );
+        launch_triplets( b, s );
+        exclusive_scan( b.isSing, b.isSing, 2ull * b.capCand, &d->probeSlots, &d->Q, sc, s );
+        exclusive_scan( b.isReg, b.isReg, 2ull * b.capCand, &d->probeSlots, &d->regTotal, sc, s );
+        cudaMemsetAsync( b.ccount, 0, sizeof( uint32_t ) * ( b.capC1 + 1ull ), s );
+        launch_place( b, s );
+
+        // F: segments
+        if ( c->mode == SESGB_MODE_FULL )
+        {
+            exclusive_scan( b.ccount, b.cstart, b.capC1, &d->C1, nullptr, sc, s );
+            cudaMemsetAsync( b.ccursor, 0, sizeof( uint32_t ) * ( b.capC1 + 1ull ), s );
+            launch_lists( b, s );
+            launch_segment_counts( b, s );
+            exclusive_scan( b.segCnt, b.segOff, b.capC1, &d->C1, &d->S, sc, s );
+            launch_segments( b, s );
+        }
+
+        // G: neighbours of singular probes
+        launch_fine_params( b, 2.f * c->rp + 0.01f, 0, s );
+        launch_cells( b, b.probePos, b.capProbes, &d->Q, sc, s );
+        launch_probe_neighbors( b, s );
+
+        // H: exterior tori
+        if ( c->mode == SESGB_MODE_EXTERIOR )
+        {
+            launch_tori( b, s );
+            exclusive_scan( b.torCnt, b.torOff, n, nullptr, &d->T, sc, s );
+            launch_tori_emit( b, s );
+        }
+    }
+
+    // regrows the buffers whose counts exceeded their capacity; true if any
+    bool regrow( sesgb_ctx * c )
+    {
+        Build &              b = c->b;
+        const DeviceCounts & h = *c->hCounts;
+        bool                 g = false;
+        auto fix = [ & ]( uint32_t & cap, uint64_t need ) {
+            if ( need > cap )
+            {
+                cap = grow( need );
+                g   = true;
+            }
+        };
+        fix( b.capSectors, h.V );
+        fix( b.capFull, h.F );
+        fix( b.capC1, h.C1 );
+        fix( b.capCand, h.cand );
+        fix( b.capProbes, h.I );
+        fix( b.capSeg, h.S );
+        fix( b.capTori, h.T );
+        if ( h.overflow & ( kOverflowProbes | kOverflowList ) )
+        {
+            // sizes follow I; a list overflow means a circle with more probes than one
+            // thread can order, which regrowing does not cure
+            if ( h.overflow & kOverflowProbes )
+                fix( b.capProbes, (uint64_t)b.capProbes * 2 );
+        }
+        return g;
+    }
+
+    int run_build( sesgb_ctx * c, cudaStream_t s, bool upload, const void * deviceAtoms )
+    {
+        for ( int attempt = 0; attempt < 6; attempt++ )
+        {
+            if ( upload && c->n )
+            {
+                if ( !c->hostAtoms )
+                {
+                    c->err = "no host atoms";
+                    return SESGB_ERR_INVALID;
+                }
+                if ( !cuda_ok( c, cudaMemcpyAsync( c->b.atomsIn, c->hostAtoms, sizeof( float4 ) * c->n, cudaMemcpyHostToDevice, s ),
+                               "upload" ) )
+                    return SESGB_ERR_CUDA;
+            }
+            else if ( deviceAtoms && c->n )
+            {
+                if ( !cuda_ok( c, cudaMemcpyAsync( c->b.atomsIn, deviceAtoms, sizeof( float4 ) * c->n, cudaMemcpyDeviceToDevice, s ),
+                               "copy" ) )
+                    return SESGB_ERR_CUDA;
+            }
+            const bool useGraph = ( c->flags & SESGB_FLAG_GRAPH ) && c->built;
+            if ( useGraph )
+            {
+                if ( !c->graphExec )
+                {
+                    cudaStream_t cap;
+                    if ( !cuda_ok( c, cudaStreamCreateWithFlags( &cap, cudaStreamNonBlocking ), "stream" ) )
+                        return SESGB_ERR_CUDA;
+                    cudaStreamBeginCapture( cap, cudaStreamCaptureModeThreadLocal );
+                    enqueue( c, cap );
+                    cudaMemcpyAsync( c->hCounts, c->b.counts, sizeof( DeviceCounts ), cudaMemcpyDeviceToHost, cap );
+                    const cudaError_t e = cudaStreamEndCapture( cap, &c->graph );
+                    cudaStreamDestroy( cap );
+                    if ( !cuda_ok( c, e, "capture" ) )
+                        return SESGB_ERR_CUDA;
+                    if ( !cuda_ok( c, cudaGraphInstantiate( &c->graphExec, c->graph, 0 ), "instantiate" ) )
+                        return SESGB_ERR_CUDA;
+                }
+                if ( !cuda_ok( c, cudaGraphLaunch( c->graphExec, s ), "graph launch" ) )
+                    return SESGB_ERR_CUDA;
+            }
+            else
+            {
+                enqueue( c, s );
+                cudaMemcpyAsync( c->hCounts, c->b.counts, sizeof( DeviceCounts ), cudaMemcpyDeviceToHost, s );
+            }
+            if ( !cuda_ok( c, cudaStreamSynchronize( s ), "build" ) )
+                return SESGB_ERR_CUDA;
+            if ( !cuda_ok( c, cudaGetLastError(), "launch" ) )
+                return SESGB_ERR_CUDA;
+            const DeviceCounts & h = *c->hCounts;
+            if ( ( h.overflow & ~(uint32_t)kOverflowNbr ) == 0 && h.V <= c->b.capSectors && h.F <= c->b.capFull
+                 && h.C1 <= c->b.capC1 && h.cand <= c->b.capCand && h.I <= c->b.capProbes && h.S <= c->b.capSeg
+                 && h.T <= c->b.capTori )
+            {
+                if ( h.overflow & kOverflowNbr )
+                {
+                    c->err = "an atom has more than 512 neighbour candidates passing the test";
+                    return SESGB_ERR_OVERFLOW;
+                }
+                c->built = true;
+                return SESGB_OK;
+            }
+            if ( ( h.overflow & kOverflowList ) && !regrow( c ) )
+            {
+                c->err = "a circle carries more probes than the segment stage holds";
+                return SESGB_ERR_OVERFLOW;
+            }
+            regrow( c );
+            destroy_graph( c );
+            c->rebuilds++;
+            if ( !allocate_dynamic( c ) )
+                return SESGB_ERR_CUDA;
+        }
+        c->err = "capacities still exceeded after regrowing";
+        return SESGB_ERR_OVERFLOW;
+    }
+} // namespace
+
+extern "C"
+{
+    int sesgb_create( const float * atoms, uint32_t n, const float * aabb, float probe_radius, int mode,
+                      const sesgb_options * options, sesgb_ctx ** out )
+    {
+        if ( !out || ( mode != SESGB_MODE_FULL && mode != SESGB_MODE_EXTERIOR ) || !( probe_radius >= 0.f ) )
+            return SESGB_ERR_INVALID;
+        if ( !aabb && n && !atoms )
+            return SESGB_ERR_INVALID;
+        *out             = nullptr;
+        sesgb_ctx * c    = new sesgb_ctx();
+        c->mode          = mode;
+        c->n             = n;
+        c->rp            = probe_radius;
+        c->hostAtoms     = atoms;
+        sesgb_options o  = options ? *options : sesgb_options {};
+        c->b.cap         = o.max_neighbor_per_atom ? o.max_neighbor_per_atom : 128u;
+        c->b.segCap      = o.max_intersections_per_circle ? o.max_intersections_per_circle : 32u;
+        c->flags         = o.flags;
+        c->b.mode        = mode;
+        c->b.rp          = probe_radius;
+        c->b.n           = n;
+        if ( c->b.cap > 4096 || c->b.segCap > (uint32_t)kSegBuf )
+        {
+            delete c;
+            return SESGB_ERR_INVALID;
+        }
+        if ( o.device >= 0 && !cuda_ok( c, cudaSetDevice( o.device ), "cudaSetDevice" ) )
+        {
+            delete c;
+            return SESGB_ERR_CUDA;
+        }
+        cudaGetDevice( &c->device );
+        if ( aabb )
+            std::memcpy( c->aabb, aabb, sizeof( c->aabb ) );
+        else
+            host_aabb( atoms, n, c->aabb );
+        setup_grid( c );
+
+        // first capacities from protein-like ratios; regrown on demand
+        Build & b    = c->b;
+        b.capSectors = grow( 40ull * n );
+        b.capFull    = grow( 4ull * n );
+        b.capC1      = grow( 24ull * n );
+        b.capCand    = grow( 24ull * n );
+        b.capProbes  = grow( 8ull * n );
+        b.capSeg     = grow( 8ull * n );
+        b.capTori    = grow( 16ull * n );
+        if ( !allocate_fixed( c ) || !allocate_dynamic( c ) || !cuda_ok( c, configure_kernels( c->b ), "configure" ) )
+        {
+            const int st = SESGB_ERR_CUDA;
+            sesgb_destroy( c );
+            return st;
+        }
+        *out = c;
+        return SESGB_OK;
+    }
+
+    int sesgb_set_host_atoms( sesgb_ctx * c, const float * atoms )
+    {
+        if ( !c )
+            return SESGB_ERR_INVALID;
+        c->hostAtoms = atoms;
+        return SESGB_OK;
+    }
+
+    int sesgb_build( sesgb_ctx * c, void * stream )
+    {
+        if ( !c )
+            return SESGB_ERR_INVALID;
+        return run_build( c, static_cast<cudaStream_t>( stream ), true, nullptr );
+    }
+
+    int sesgb_build_device( sesgb_ctx * c, const void * device_atoms, void * stream )
+    {
+        if ( !c || ( c->n && !device_atoms ) )
+            return SESGB_ERR_INVALID;
+        return run_build( c, static_cast<cudaStream_t>( stream ), false, device_atoms );
+    }
+
+    int sesgb_get_full( sesgb_ctx * c, sesgb_full_data * o )
+    {
+        if ( !c || !o )
+            return SESGB_ERR_INVALID;
+        if ( c->mode != SESGB_MODE_FULL )
+            return SESGB_ERR_MODE;
+        if ( !c->built )
+            return SESGB_ERR_NOT_BUILT;
+        const DeviceCounts & h      = *c->hCounts;
+        o->atomNb                   = c->n;
+        o->atoms                    = c->b.atoms;
+        o->convexPatchNb            = c->n;
+        o->convexPatches            = c->b.convex;
+        o->sectorNb                 = h.V;
+        o->sectors                  = c->b.sectors;
+        o->segmentPatchNb           = h.S;
+        o->segmentPatches           = c->b.segments;
+        o->circlePatchNb            = h.F;
+        o->circlePatches            = c->b.fullCircles;
+        o->concavePatchNb           = h.I;
+        o->concavePatchesPosition   = c->b.probePos;
+        o->concavePatchesId         = c->b.probeIds;
+        o->concavePatchesNeighbors  = c->b.probeNbrs;
+        o->probeRadius              = c->rp;
+        o->maxConcaveNeighbors      = (uint16_t)kMaxProbeNbr;
+        return SESGB_OK;
+    }
+
+    int sesgb_get_exterior( sesgb_ctx * c, sesgb_exterior_data * o )
+    {
+        if ( !c || !o )
+            return SESGB_ERR_INVALID;
+        if ( c->mode != SESGB_MODE_EXTERIOR )
+            return SESGB_ERR_MODE;
+        if ( !c->built )
+            return SESGB_ERR_NOT_BUILT;
+        const DeviceCounts & h     = *c->hCounts;
+        o->atomNb                  = c->n;
+        o->atoms                   = c->b.atoms;
+        o->circlePatchNb           = h.T;
+        o->circlePosition          = c->b.torPos;
+        o->circleAxis              = c->b.torAxis;
+        o->circleVs                = c->b.torVs;
+        o->concavePatchNb          = h.I;
+        o->concavePatchesPosition  = c->b.probePos;
+        o->concavePatchesId        = c->b.probeIds;
+        o->concavePatchesNeighbors = c->b.probeNbrs;
+        o->probeRadius             = c->rp;
+        o->maxConcaveNeighbors     = (uint16_t)kMaxProbeNbr;
+        return SESGB_OK;
+    }
+
+    int sesgb_get_counts( sesgb_ctx * c, sesgb_counts * o )
+    {
+        if ( !c || !o )
+            return SESGB_ERR_INVALID;
+        if ( !c->built )
+            return SESGB_ERR_NOT_BUILT;
+        const DeviceCounts & h          = *c->hCounts;
+        *o                              = sesgb_counts {};
+        o->atoms                        = c->n;
+        o->pairs                        = h.P;
+        o->sectors                      = c->mode == SESGB_MODE_FULL ? h.V : 0;
+        o->full_circles                 = c->mode == SESGB_MODE_FULL ? h.F : 0;
+        o->partial_circles              = h.C1;
+        o->candidates                   = h.cand;
+        o->probes                       = h.I;
+        o->singular_probes              = h.Q;
+        o->segments                     = h.S;
+        o->tori                         = h.T;
+        o->max_neighbors                = h.maxNbr;
+        o->truncated_atoms              = h.nbrTruncated;
+        o->truncated_circles            = h.segTruncated;
+        o->truncated_probe_neighbors    = h.snbrTruncated;
+        o->degenerate_tori              = h.torusDegenerate;
+        o->outside_atoms                = h.outside;
+        for ( int k = 0; k < 4; k++ )
+            o->fp64_decisions[ k ] = h.fp64[ k ];
+        o->rebuilds = c->rebuilds;
+        return SESGB_OK;
+    }
+
+    int sesgb_atom_indices( sesgb_ctx * c, uint32_t * host )
+    {
+        if ( !c || ( c->n && !host ) )
+            return SESGB_ERR_INVALID;
+        if ( !c->built )
+            return SESGB_ERR_NOT_BUILT;
+        return cuda_ok( c, cudaMemcpy( host, c->b.perm, sizeof( uint32_t ) * c->n, cudaMemcpyDeviceToHost ), "copy" )
+                   ? SESGB_OK
+                   : SESGB_ERR_CUDA;
+    }
+
+    int sesgb_analysis_buffer( sesgb_ctx * c, int which, void ** ptr, uint64_t * bytes )
+    {
+        if ( !c || !ptr || !bytes )
+            return SESGB_ERR_INVALID;
+        if ( !c->built )
+            return SESGB_ERR_NOT_BUILT;
+        const uint64_t slots = (uint64_t)c->n * c->b.cap;
+        switch ( which )
+        {
+        case SESGB_BUF_ATOM_INDICES: *ptr = c->b.perm, *bytes = 4ull * c->n; return SESGB_OK;
+        case SESGB_BUF_NEIGHBOR_COUNT: *ptr = c->b.nbrCount, *bytes = 4ull * c->n; return SESGB_OK;
+        case SESGB_BUF_NEIGHBOR_IDS: *ptr = c->b.nbr, *bytes = 4ull * slots; return SESGB_OK;
+        case SESGB_BUF_VISIBILITY_STATUS:
+        case SESGB_BUF_GLOBAL_TO_TRIMMED:
+        {
+            if ( which == SESGB_BUF_GLOBAL_TO_TRIMMED )
+            {
+                if ( c->mode != SESGB_MODE_FULL )
+                    return SESGB_ERR_MODE;
+                if ( !c->g2t && !cuda_ok( c, cudaMalloc( &c->g2t, 4ull * ( slots + 1 ) ), "cudaMalloc" ) )
+                    return SESGB_ERR_CUDA;
+            }
+            launch_reference_fill( c->b, which == SESGB_BUF_GLOBAL_TO_TRIMMED ? c->g2t : nullptr, nullptr );
+            if ( !cuda_ok( c, cudaDeviceSynchronize(), "fill" ) )
+                return SESGB_ERR_CUDA;
+            if ( which == SESGB_BUF_VISIBILITY_STATUS )
+                *ptr = c->b.status, *bytes = slots + 1;
+            else
+                *ptr = c->g2t, *bytes = 4ull * ( slots + 1 );
+            return SESGB_OK;
+        }
+        default: return SESGB_ERR_INVALID;
+        }
+    }
+
+    int sesgb_copy_to_host( sesgb_ctx * c, const void * dptr, void * host, uint64_t bytes )
+    {
+        if ( !c || ( bytes && ( !dptr || !host ) ) )
+            return SESGB_ERR_INVALID;
+        if ( !bytes )
+            return SESGB_OK;
+        return cuda_ok( c, cudaMemcpy( host, dptr, bytes, cudaMemcpyDeviceToHost ), "copy" ) ? SESGB_OK : SESGB_ERR_CUDA;
+    }
+
+    uint16_t sesgb_max_neighbor_per_atom( const sesgb_ctx * c ) { return c ? (uint16_t)c->b.cap : 0; }
+    uint16_t sesgb_max_intersections_per_circle( const sesgb_ctx * c ) { return c ? (uint16_t)c->b.segCap : 0; }
+    uint16_t sesgb_max_intersection_neighbors( const sesgb_ctx * ) { return (uint16_t)kMaxProbeNbr; }
+
+    const char * sesgb_error_string( int status )
+    {
+        const int k = -status;
+        if ( k < 0 || k >= (int)( sizeof( kStatusNames ) / sizeof( kStatusNames[ 0 ] ) ) )
+            return "unknown status";
+        return kStatusNames[ k ];
+    }
+
+    const char * sesgb_last_error( const sesgb_ctx * c ) { return c ? c->err.c_str() : "no context"; }
+
+    void sesgb_destroy( sesgb_ctx * c )
+    {
+        if ( !c )
+            return;
+        cudaDeviceSynchronize();
+        destroy_graph( c );
+        free_list( c->dynAllocs );
+        free_list( c->fixedAllocs );
+        if ( c->g2t )
+            cudaFree( c->g2t );
+        if ( c->hCounts )
+            cudaFreeHost( c->hCounts );
+        delete c;
+    }
+}

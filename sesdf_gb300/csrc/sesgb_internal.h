@@ -1,0 +1,82 @@
+// sesgb_internal.h -- host-side declarations shared by the CUDA translation units.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+#include "sesgb_device.cuh"
+
+namespace sesgb
+{
+    // Counters written by the kernels and read back once at the end of a build.
+    struct DeviceCounts
+    {
+        uint32_t P;        // neighbour pairs (directed circles) kept
+        uint32_t V;        // visible directed circles (convex sectors)
+        uint32_t F;        // complete circles with i < j
+        uint32_t C1;       // partial circles with i < j
+        uint32_t cand;     // (i, j, k) candidates of the probe solve
+        uint32_t I;        // probes (concave patches)
+        uint32_t Q;        // singular probes
+        uint32_t S;        // segments
+        uint32_t T;        // exterior tori
+        uint32_t maxNbr;   // largest neighbour count seen (before truncation)
+        uint32_t overflow; // bitmask, see Overflow
+        uint32_t outside;  // atoms outside the reference grid
+        uint32_t fp64[ 8 ]; // predicate evaluations settled in double precision, see Fp64Stage
+        uint32_t nbrTruncated;
+        uint32_t segTruncated;
+        uint32_t snbrTruncated;
+        uint32_t torusDegenerate;
+        uint32_t fineCells;  // cells of the neighbour grid in use
+        float    fineCell;   // edge of a neighbour-grid cell (A)
+        float    rmax;       // largest vdW radius
+        uint32_t probeSlots; // 2 * candidates (probe slots scanned by the partition)
+        uint32_t regTotal;   // regular (non-singular) probes
+        uint32_t P2;         // scratch total
+        uint32_t pad[ 2 ];
+    };
+
+    enum Overflow : uint32_t
+    {
+        kOverflowNbr     = 1u << 0, // an atom has more neighbours than the per-atom capacity
+        kOverflowSectors = 1u << 1,
+        kOverflowFull    = 1u << 2,
+        kOverflowC1      = 1u << 3,
+        kOverflowCand    = 1u << 4,
+        kOverflowProbes  = 1u << 5,
+        kOverflowSeg     = 1u << 6,
+        kOverflowTori    = 1u << 7,
+        kOverflowCells   = 1u << 8,
+        kOverflowList    = 1u << 9,
+    };
+
+    enum Fp64Stage : uint32_t
+    {
+        kFp64Neighbor = 0,
+        kFp64Visibility,
+        kFp64Occlusion,
+        kFp64SingularNbr,
+        kFp64Count
+    };
+
+    // neighbour grid (a uniform grid whose cell is at least the largest pair cutoff)
+    struct FineGrid
+    {
+        float3   origin;
+        float    h;
+        int3     dims;
+        uint32_t cells;
+    };
+
+    // ---- primitives (sesgb_sort.cu) ------------------------------------------
+    // scratch bytes needed by exclusive_scan for n elements
+    size_t scan_scratch_bytes( uint64_t n );
+    // out[i] = sum_{k<i} in[k] for i < n (n read from *nDevice when given, else nHost);
+    // out[n] = total; *total (device) = total when non-null. in == out allowed.
+    void exclusive_scan( const uint32_t * in, uint32_t * out, uint64_t nHost, const uint32_t * nDevice, uint32_t * total,
+                         void * scratch, cudaStream_t stream );
+
+    size_t radix_scratch_bytes( uint32_t n );
+    // stable LSD radix sort of (keys, vals) on the low `bits` bits; result in keys/vals
+    void radix_sort( uint32_t * keys, uint32_t * vals, uint32_t n, int bits, void * scratch, cudaStream_t stream );
+} // namespace sesgb

@@ -1,0 +1,1124 @@
+// sesgb_stages.cu -- the kernels of the SES build (full surface and exterior only).
+//
+// Stage map (reference functions restated, file:line of PlathC/SESDF):
+//   k_hash / k_gather        AccelerationGrid::build, computeHashes, buildAccelerationGrid
+//                            (sesdf/src/cuda/grid.cu:15-132) -- same cell hash and stable order
+//   k_neighbors              findCirclesBetweenAtoms (sesdf/src/sesdf/operations.cu:34-124)
+//   k_visibility             computeCirclesVisibilityStatus (operations.cu:126-204; ssesdf :169-244)
+//   k_emit                   scans of findCircles + buildConvexPatchesSectors
+//                            (sesdf/include/bcs/sesdf/operations.inl:46-93,175-228)
+//   k_candidates/k_triplets  findIntersectionsBetweenCircles (operations.inl:230-486; ssesdf operation.inl:100-351)
+//   k_place/k_lists          thrust::sort by |w| + fillIntersections (operations.inl:128-141; operations.cu:206-269;
+//                            ssesdf/operations.cu:287-329)
+//   k_segments               buildConicPatches + buildSegments (operations.inl:488-668)
+//   k_probe_neighbors        handleIntersectionSingularities + findIntersectionsNeighbors (operations.cu:14-32,271-338)
+//   k_tori                   fillCircles (ssesdf/operations.cu:246-285)
+//
+// Every predicate is first evaluated in float32 in coordinates relative to the
+// owning atom; when its margin is inside a conservative band (kRel times the
+// magnitudes involved, about 30x the float32 error bound) it is decided by the
+// double-precision twin in sesgb_device.cuh, which evaluates the reference's
+// formula exactly as the FP64 oracle does.
+#include <cfloat>
+
+#include "sesgb_stages.cuh"
+
+namespace sesgb
+{
+    namespace
+    {
+        constexpr float kRel = 1.0f / 65536.0f;
+
+        __device__ __forceinline__ int3 fine_cell( const FineGrid & g, float x, float y, float z )
+        {
+            int cx = (int)floorf( ( x - g.origin.x ) / g.h );
+            int cy = (int)floorf( ( y - g.origin.y ) / g.h );
+            int cz = (int)floorf( ( z - g.origin.z ) / g.h );
+            cx     = cx < 0 ? 0 : ( cx >= g.dims.x ? g.dims.x - 1 : cx );
+            cy     = cy < 0 ? 0 : ( cy >= g.dims.y ? g.dims.y - 1 : cy );
+            cz     = cz < 0 ? 0 : ( cz >= g.dims.z ? g.dims.z - 1 : cz );
+            return make_int3( cx, cy, cz );
+        }
+        __device__ __forceinline__ uint32_t fine_key( const FineGrid & g, int3 c )
+        {
+            return ( (uint32_t)c.z * (uint32_t)g.dims.y + (uint32_t)c.y ) * (uint32_t)g.dims.x + (uint32_t)c.x;
+        }
+
+        // The 27 cells around c as 9 rows of up to three x-adjacent cells, each a
+        // contiguous range of the cell-ordered item array. Lane r < 9 computes row r;
+        // every lane receives all nine (start, exclusive prefix) pairs.
+        struct Rows
+        {
+            uint32_t start[ 9 ];
+            uint32_t pre[ 9 ];
+            uint32_t total;
+        };
+        __device__ __forceinline__ void stencil_rows( const FineGrid & g, const uint32_t * cellStart, int3 c, Rows & rows )
+        {
+            const uint32_t lane = lane_id();
+            uint32_t       st = 0, len = 0;
+            if ( lane < 9 )
+            {
+                const int y = c.y + (int)( lane % 3 ) - 1;
+                const int z = c.z + (int)( lane / 3 ) - 1;
+                if ( y >= 0 && z >= 0 && y < g.dims.y && z < g.dims.z )
+                {
+                    const int      x0 = c.x > 0 ? c.x - 1 : 0;
+                    const int      x1 = c.x + 1 < g.dims.x ? c.x + 1 : g.dims.x - 1;
+                    const uint32_t c0 = fine_key( g, make_int3( x0, y, z ) );
+                    const uint32_t c1 = fine_key( g, make_int3( x1, y, z ) );
+                    st                = cellStart[ c0 ];
+                    len               = cellStart[ c1 + 1 ] - st;
+                }
+            }
+            uint32_t       total;
+            const uint32_t pre = warp_exclusive_sum( len, total );
+#pragma unroll
+            for ( int r = 0; r < 9; r++ )
+            {
+                rows.start[ r ] = __shfl_sync( 0xffffffffu, st, r );
+                rows.pre[ r ]   = __shfl_sync( 0xffffffffu, pre, r );
+            }
+            rows.total = total;
+        }
+        __device__ __forceinline__ uint32_t row_item( const Rows & rows, uint32_t f )
+        {
+            int r = 0;
+#pragma unroll
+            for ( int q = 1; q < 9; q++ )
+                r = rows.pre[ q ] <= f ? q : r;
+            return rows.start[ r ] + ( f - rows.pre[ r ] );
+        }
+
+        template<class T> __device__ void warp_bitonic_sort( T * a, uint32_t count, uint32_t capacity, T pad )
+        {
+            const uint32_t lane = lane_id();
+            uint32_t       n2   = 32;
+            while ( n2 < count )
+                n2 <<= 1;
+            if ( n2 > capacity )
+                n2 = capacity;
+            for ( uint32_t idx = count + lane; idx < n2; idx += 32 )
+                a[ idx ] = pad;
+            __syncwarp();
+            for ( uint32_t k = 2; k <= n2; k <<= 1 )
+                for ( uint32_t j = k >> 1; j > 0; j >>= 1 )
+                {
+                    for ( uint32_t idx = lane; idx < n2; idx += 32 )
+                    {
+                        const uint32_t ixj = idx ^ j;
+                        if ( ixj > idx )
+                        {
+                            const bool asc = ( idx & k ) == 0;
+                            const T    x   = a[ idx ];
+                            const T    y   = a[ ixj ];
+                            if ( ( x > y ) == asc )
+                            {
+                                a[ idx ] = y;
+                                a[ ixj ] = x;
+                            }
+                        }
+                    }
+                    __syncwarp();
+                }
+        }
+
+        // ------------------------------------------------------------------
+        __global__ void k_hash( Build b )
+        {
+            const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+            if ( i >= b.n )
+                return;
+            const float4 a = b.atomsIn[ i ];
+            const int3   p = ref_grid_position( b.grid, a.x, a.y, a.z );
+            if ( p.x < 0 || p.y < 0 || p.z < 0 || p.x >= b.grid.size || p.y >= b.grid.size || p.z >= b.grid.size )
+                atomicAdd( &b.counts->outside, 1u );
+            b.keys[ i ] = ref_grid_hash( b.grid, p );
+            b.perm[ i ] = i;
+            atomicMax( reinterpret_cast<int *>( &b.counts->rmax ), __float_as_int( fmaxf( a.w, 0.f ) ) );
+        }
+
+        // one thread: neighbour-grid geometry from the reference grid box
+        __global__ void k_fine_params( Build b, float cutoff )
+        {
+            if ( cutoff < 0.f )
+                cutoff = 2.f * ( b.counts->rmax + b.rp ) + 0.01f;
+            const float ex = b.grid.cell.x * b.grid.size, ey = b.grid.cell.y * b.grid.size, ez = b.grid.cell.z * b.grid.size;
+            float       h  = cutoff;
+            int3        d;
+            for ( int it = 0; it < 200; it++ )
+            {
+                d = make_int3( max( 1, (int)ceilf( ex / h ) ), max( 1, (int)ceilf( ey / h ) ), max( 1, (int)ceilf( ez / h ) ) );
+                if ( (uint64_t)d.x * d.y * d.z <= b.capCells )
+                    break;
+                h *= 1.1f;
+            }
+            FineGrid g;
+            g.origin = b.grid.origin;
+            g.h      = h;
+            g.dims   = d;
+            g.cells  = (uint32_t)( (uint64_t)d.x * d.y * d.z );
+            *b.fine  = g;
+            b.counts->fineCells = g.cells;
+            b.counts->fineCell  = h;
+        }
+
+        __global__ void k_gather( Build b )
+        {
+            const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+            if ( s >= b.n )
+                return;
+            b.atoms[ s ] = b.atomsIn[ b.perm[ s ] ];
+        }
+
+        __global__ void k_cell_count( Build b, const float4 * pos, uint32_t nHost, const uint32_t * nDevice )
+        {
+            const uint32_t n = nDevice ? min( *nDevice, nHost ) : nHost;
+            const FineGrid g = *b.fine;
+            for ( uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x )
+            {
+                const float4 p = pos[ q ];
+                atomicAdd( &b.cellCount[ fine_key( g, fine_cell( g, p.x, p.y, p.z ) ) ], 1u );
+            }
+        }
+
+        __global__ void k_cell_scatter( Build b, const float4 * pos, uint32_t nHost, const uint32_t * nDevice )
+        {
+            const uint32_t n = nDevice ? min( *nDevice, nHost ) : nHost;
+            const FineGrid g = *b.fine;
+            for ( uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x )
+            {
+                const float4   p   = pos[ q ];
+                const uint32_t key = fine_key( g, fine_cell( g, p.x, p.y, p.z ) );
+                const uint32_t idx = b.cellStart[ key ] + atomicAdd( &b.cellCursor[ key ], 1u );
+                b.cellItems[ idx ] = q;
+                b.cellPos[ idx ]   = p;
+            }
+        }
+
+        // ---- neighbour lists ---------------------------------------------
+        __global__ void __launch_bounds__( 32 * kWarpsPerBlock ) k_neighbors( Build b )
+        {
+            __shared__ uint32_t buf[ kWarpsPerBlock ][ kNbrBuf ];
+            const uint32_t      warp = threadIdx.x >> 5, lane = lane_id();
+            const uint32_t      i    = blockIdx.x * kWarpsPerBlock + warp;
+            if ( i >= b.n )
+                return;
+            const FineGrid g  = *b.fine;
+            const float4   ai = b.atoms[ i ];
+            Rows           rows;
+            stencil_rows( g, b.cellStart, fine_cell( g, ai.x, ai.y, ai.z ), rows );
+            const float Ri    = ai.w + b.rp;
+            uint32_t    count = 0, fp64 = 0;
+            for ( uint32_t base = 0; base < rows.total; base += 32 )
+            {
+                const uint32_t f    = base + lane;
+                bool           pass = false;
+                uint32_t       j    = 0;
+                if ( f < rows.total )
+                {
+                    const uint32_t idx = row_item( rows, f );
+                    j                  = b.cellItems[ idx ];
+                    if ( j != i )
+                    {
+                        const float4 aj = b.cellPos[ idx ];
+                        const f3     dj = F3( aj.x - ai.x, aj.y - ai.y, aj.z - ai.z );
+                        const float  d  = dot( dj, dj );
+                        const float  R  = Ri + ( aj.w + b.rp );
+                        const float  m  = d - R * R - 1e-4f;
+                        const float  e  = kRel * ( d + R * R + 1.f );
+                        if ( m < -e )
+                            pass = true;
+                        else if ( m <= e )
+                        {
+                            pass = dneighbor( D3( ai ), ai.w, D3( aj ), aj.w, (double)b.rp );
+                            fp64++;
+                        }
+                    }
+                }
+                const uint32_t mask = __ballot_sync( 0xffffffffu, pass );
+                const uint32_t pos  = count + __popc( mask & lanemask_lt() );
+                if ( pass && pos < kNbrBuf )
+                    buf[ warp ][ pos ] = j;
+                count += __popc( mask );
+            }
+            __syncwarp();
+            const uint32_t held = count < kNbrBuf ? count : kNbrBuf;
+            warp_bitonic_sort<uint32_t>( buf[ warp ], held, kNbrBuf, 0xffffffffu );
+            const uint32_t kept = held < b.cap ? held : b.cap;
+            for ( uint32_t s = lane; s < kept; s += 32 )
+                b.nbr[ (size_t)i * b.cap + s ] = buf[ warp ][ s ];
+            for ( int o = 16; o > 0; o >>= 1 )
+                fp64 += __shfl_xor_sync( 0xffffffffu, fp64, o );
+            if ( lane == 0 )
+            {
+                b.nbrCount[ i ] = kept;
+                atomicMax( &b.counts->maxNbr, count );
+                if ( count > b.cap )
+                    atomicAdd( &b.counts->nbrTruncated, 1u );
+                if ( count > kNbrBuf )
+                    atomicOr( &b.counts->overflow, (uint32_t)kOverflowNbr );
+                if ( fp64 )
+                    atomicAdd( &b.counts->fp64[ kFp64Neighbor ], fp64 );
+            }
+        }
+
+        // ---- circle visibility ----------------------------------------------
+        // Status of the directed circle (i, slot s): float32 filter per k, double
+        // precision for the k whose margin is inside the band.
+        __device__ uint8_t circle_status( const Build & b, uint32_t i, const float4 & ai, const float4 * rel, uint32_t ni,
+                                          uint32_t s, uint32_t & fp64 )
+        {
+            const float  Ri = ai.w + b.rp;
+            const float4 q  = rel[ s ];
+            const f3     dj = F3( q.x, q.y, q.z );
+            const float  Rj = q.w;
+            const float  d  = dot( dj, dj );
+            const float  t  = ( Ri * Ri - Rj * Rj + d ) / ( 2.f * d );
+            const f3     c  = dj * t;
+            const float  r2 = fmaxf( Ri * Ri - dot( c, c ), 0.f );
+            const f3     nr = dj * rsqrtf( d );
+
+            bool    buried = false, touched = false, haveD = false;
+            dcircle dc;
+            for ( uint32_t k = 0; k < ni; k++ )
+            {
+                if ( k == s )
+                    continue;
+                const float4 qk  = rel[ k ];
+                const f3     v   = c - F3( qk.x, qk.y, qk.z );
+                const float  vv  = dot( v, v );
+                const float  sv  = dot( v, nr );
+                const float  p2  = fmaxf( vv - sv * sv, 0.f );
+                const float  Rk2 = qk.w * qk.w;
+                const float  A   = vv + r2 - Rk2 - 1e-4f;
+                const float  M   = vv + r2 + Rk2 + 1.f;
+                const float  eA  = kRel * M;
+                const float  G   = A * A - 4.f * p2 * r2;
+                const float  eG  = kRel * ( A * A + 4.f * p2 * r2 + 2.f * fabsf( A ) * M + 4.f * M * ( r2 + p2 ) );
+                bool         bk = false, tk = false, decided = true;
+                // k on (or next to) the axis of the circle: the reference formula
+                // divides by |v| and takes sqrt(1 - cos^2), which yields NaN (k
+                // ignored) exactly when |v| = 0 or |cos| > 1 in its arithmetic;
+                // only the double-precision twin reproduces that
+                if ( vv <= eA || p2 <= kRel * ( vv + 1.f ) )
+                    decided = false;
+                else if ( A < -eA )
+                {
+                    tk = true;
+                    if ( G > eG )
+                        bk = true;
+                    else if ( !( G < -eG ) )
+                        decided = false;
+                }
+                else if ( A > eA )
+                {
+                    if ( G < -eG )
+                        tk = true;
+                    else if ( !( G > eG ) )
+                        decided = false;
+                }
+                else
+                    decided = false;
+                if ( !decided )
+                {
+                    if ( !haveD )
+                    {
+                        const uint32_t j  = b.nbr[ (size_t)i * b.cap + s ];
+                        const float4   aj = b.atoms[ j ];
+                        dc                = dcircle_geometry( D3( ai ), ai.w, D3( aj ), aj.w, (double)b.rp );
+                        haveD             = true;
+                    }
+                    const uint32_t kid = b.nbr[ (size_t)i * b.cap + k ];
+                    const float4   ak  = b.atoms[ kid ];
+                    const int      r   = dcircle_vs_atom( dc, D3( ak ), __dadd_rn( (double)ak.w, (double)b.rp ) );
+                    bk                 = r & 1;
+                    tk                 = r & 2;
+                    fp64++;
+                }
+                touched = touched || tk;
+                if ( bk )
+                {
+                    buried = true;
+                    break;
+                }
+            }
+            return buried ? 0 : ( touched ? 1 : 2 );
+        }
+
+        __global__ void __launch_bounds__( 32 * kWarpsPerBlock ) k_visibility( Build b )
+        {
+            extern __shared__ float4 smem[];
+            const uint32_t           warp = threadIdx.x >> 5, lane = lane_id();
+            const uint32_t           i    = blockIdx.x * kWarpsPerBlock + warp;
+            if ( i >= b.n )
+                return;
+            float4 *       rel = smem + (size_t)warp * b.cap;
+            const uint32_t ni  = b.nbrCount[ i ];
+            const float4   ai  = b.atoms[ i ];
+            for ( uint32_t s = lane; s < ni; s += 32 )
+            {
+                const float4 aj = b.atoms[ b.nbr[ (size_t)i * b.cap + s ] ];
+                rel[ s ]        = make_float4( aj.x - ai.x, aj.y - ai.y, aj.z - ai.z, aj.w + b.rp );
+            }
+            __syncwarp();
+            uint32_t vis = 0, part = 0, full = 0, fp64 = 0;
+            for ( uint32_t s = lane; s < ni; s += 32 )
+            {
+                const uint32_t j  = b.nbr[ (size_t)i * b.cap + s ];
+                uint8_t        st = 0;
+                if ( b.mode == 0 || i < j )
+                    st = circle_status( b, i, ai, rel, ni, s, fp64 );
+                b.status[ (size_t)i * b.cap + s ] = st;
+                vis += st != 0;
+                part += ( st == 1 && i < j );
+                full += ( st == 2 && i < j );
+            }
+            for ( int o = 16; o > 0; o >>= 1 )
+            {
+                vis += __shfl_xor_sync( 0xffffffffu, vis, o );
+                part += __shfl_xor_sync( 0xffffffffu, part, o );
+                full += __shfl_xor_sync( 0xffffffffu, full, o );
+                fp64 += __shfl_xor_sync( 0xffffffffu, fp64, o );
+            }
+            if ( lane == 0 )
+            {
+                b.visCnt[ i ]  = vis;
+                b.partCnt[ i ] = part;
+                b.fullCnt[ i ] = full;
+                if ( fp64 )
+                    atomicAdd( &b.counts->fp64[ kFp64Visibility ], fp64 );
+            }
+        }
+
+        // ---- sectors, complete circles, partial-circle numbering -----------
+        // sector of buildConvexPatchesSectors (operations.inl:186-213) in
+        // coordinates relative to atom i
+        __device__ float4 sector_of( const Build & b, const float4 & ai, const float4 & aj )
+        {
+            const float rirp   = ai.w + b.rp;
+            const float sqrirp = rirp * rirp;
+            const f3    dj     = F3( aj.x - ai.x, aj.y - ai.y, aj.z - ai.z );
+            const float Rj     = aj.w + b.rp;
+            const float d      = dot( dj, dj );
+            const float t      = ( rirp * rirp - Rj * Rj + d ) / ( 2.f * d );
+            const f3    cij    = dj * t;
+            const float radius = sqrtf( fmaxf( sqrirp - dot( cij, cij ), 0.f ) );
+            const f3    cicj   = normalize( dj );
+            f3          ref    = F3( 1.f, 0.f, 0.f );
+            if ( fabsf( dot( cicj, ref ) ) > 1.f - 1e-4f )
+                ref = F3( 0.f, 1.f, 0.f );
+            const f3    nn = normalize( cross( cicj, ref ) );
+            const f3    x  = cij + nn * radius;
+            const float c  = fminf( fmaxf( dot( cicj, x * ( 1.f / rirp ) ), -1.f ), 1.f );
+            return make_float4( cicj.x, cicj.y, cicj.z, acosf( c ) );
+        }
+
+        __global__ void __launch_bounds__( 32 * kWarpsPerBlock ) k_emit( Build b )
+        {
+            const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
+            const uint32_t i    = blockIdx.x * kWarpsPerBlock + warp;
+            if ( i >= b.n )
+                return;
+            const uint32_t ni       = b.nbrCount[ i ];
+            const float4   ai       = b.atoms[ i ];
+            uint32_t       visBase  = b.visOff[ i ];
+            uint32_t       partBase = b.partOff[ i ];
+            uint32_t       fullBase = b.fullOff[ i ];
+            uint32_t       ovf      = 0;
+            for ( uint32_t base = 0; base < ni; base += 32 )
+            {
+                const uint32_t s     = base + lane;
+                const bool     valid = s < ni;
+                const size_t   slot  = (size_t)i * b.cap + s;
+                uint32_t       j     = 0;
+                uint8_t        st    = 0;
+                if ( valid )
+                {
+                    j  = b.nbr[ slot ];
+                    st = b.status[ slot ];
+                }
+                const bool     vis  = valid && st != 0;
+                const bool     part = valid && st == 1 && i < j;
+                const bool     full = valid && st == 2 && i < j;
+                const uint32_t mv   = __ballot_sync( 0xffffffffu, vis );
+                const uint32_t mp   = __ballot_sync( 0xffffffffu, part );
+                const uint32_t mf   = __ballot_sync( 0xffffffffu, full );
+                const uint32_t lt   = lanemask_lt();
+                if ( valid )
+                    b.slotTrim[ slot ] = partBase + __popc( mp & lt );
+                if ( vis && b.mode == 0 )
+                {
+                    const uint32_t idx = visBase + __popc( mv & lt );
+                    if ( idx < b.capSectors )
+                        b.sectors[ idx ] = sector_of( b, ai, b.atoms[ j ] );
+                    else
+                        ovf |= kOverflowSectors;
+                }
+                if ( part )
+                {
+                    const uint32_t t = partBase + __popc( mp & lt );
+                    if ( t < b.capC1 )
+                        b.trimSlot[ t ] = (uint32_t)slot;
+                    else
+                        ovf |= kOverflowC1;
+                }
+                if ( full && b.mode == 0 )
+                {
+                    const uint32_t f = fullBase + __popc( mf & lt );
+                    if ( f < b.capFull )
+                        b.fullCircles[ f ] = make_uint2( i, j );
+                    else
+                        ovf |= kOverflowFull;
+                }
+                visBase += __popc( mv );
+                partBase += __popc( mp );
+                fullBase += __popc( mf );
+            }
+            if ( lane == 0 && b.mode == 0 )
+                b.convex[ i ] = make_uint2( b.visOff[ i ], b.visOff[ i ] + b.visCnt[ i ] );
+            if ( ovf )
+                atomicOr( &b.counts->overflow, ovf );
+        }
+
+        // ---- probe candidates ------------------------------------------------
+        __device__ __forceinline__ int find_in_row( const uint32_t * row, uint32_t len, uint32_t target )
+        {
+            uint32_t lo = 0, hi = len;
+            while ( lo < hi )
+            {
+                const uint32_t mid = ( lo + hi ) >> 1;
+                if ( row[ mid ] < target )
+                    lo = mid + 1;
+                else
+                    hi = mid;
+            }
+            return ( lo < len && row[ lo ] == target ) ? (int)lo : -1;
+        }
+
+        __global__ void k_candidates( Build b, bool write )
+        {
+            const uint32_t C1 = min( b.counts->C1, b.capC1 );
+            uint32_t       ovf = 0;
+            for ( uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < C1; t += gridDim.x * blockDim.x )
+            {
+                const uint32_t   slot = b.trimSlot[ t ];
+                const uint32_t   i    = slot / b.cap;
+                const uint32_t   sj   = slot - i * b.cap;
+                const uint32_t   j    = b.nbr[ slot ];
+                const uint32_t   ni   = b.nbrCount[ i ];
+                const uint32_t   nj   = b.nbrCount[ j ];
+                const uint32_t * rowI = b.nbr + (size_t)i * b.cap;
+                const uint32_t * rowJ = b.nbr + (size_t)j * b.cap;
+                const uint8_t *  stI  = b.status + (size_t)i * b.cap;
+                uint32_t         cnt  = 0;
+                const uint32_t   off  = write ? b.candOff[ t ] : 0;
+                // k > j  <=>  slot of k after slot of j (rows are ascending)
+                for ( uint32_t sk = sj + 1; sk < ni; sk++ )
+                {
+                    if ( stI[ sk ] != 1 )
+                        continue;
+                    const int sjk = find_in_row( rowJ, nj, rowI[ sk ] );
+                    if ( sjk < 0 )
+                        continue;
+                    if ( write )
+                    {
+                        const uint32_t c = off + cnt;
+                        if ( c < b.capCand )
+                            b.cand[ c ] = make_uint4( t, i * b.cap + sk, j * b.cap + (uint32_t)sjk, 0u );
+                        else
+                            ovf |= kOverflowCand;
+                    }
+                    cnt++;
+                }
+                if ( !write )
+                    b.candCnt[ t ] = cnt;
+            }
+            if ( ovf )
+                atomicOr( &b.counts->overflow, ovf );
+        }
+
+        // ---- probe solve -----------------------------------------------------
+        __global__ void __launch_bounds__( 128 ) k_triplets( Build b )
+        {
+            const uint32_t nc   = min( b.counts->cand, b.capCand );
+            if ( blockIdx.x == 0 && threadIdx.x == 0 )
+                b.counts->probeSlots = 2u * nc;
+            const double   rp   = (double)b.rp;
+            const double   tol  = (double)1e-4f;
+            uint32_t       fp64 = 0;
+            for ( uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x )
+            {
+                const uint4    cd     = b.cand[ c ];
+                const uint32_t t      = cd.x;
+                const uint32_t slotIK = cd.y, slotJK = cd.z;
+                const uint32_t slotIJ = b.trimSlot[ t ];
+                const uint32_t i      = slotIJ / b.cap;
+                const uint32_t sj     = slotIJ - i * b.cap;
+                const uint32_t sk     = slotIK - i * b.cap;
+                const uint32_t j      = b.nbr[ slotIJ ];
+                const uint32_t k      = b.nbr[ slotIK ];
+                const float4   ai = b.atoms[ i ], aj = b.atoms[ j ], ak = b.atoms[ k ];
+                const d3       ci = D3( ai ), cj = D3( aj ), ck = D3( ak );
+                const double   ri = ai.w;
+
+                const dcircle cij = dcircle_geometry( ci, ri, cj, (double)aj.w, rp );
+                const dcircle cik = dcircle_geometry( ci, ri, ck, (double)ak.w, rp );
+                const d3      u   = dsub( cik.normal, dmul( cij.normal, ddot( cik.normal, cij.normal ) ) );
+                const double  den = ddot( u, cik.normal );
+                const d3 xc = dadd( cij.center, dmul( u, __ddiv_rn( ddot( dsub( cik.center, cij.center ), cik.normal ), den ) ) );
+                const d3     xci = dsub( xc, ci );
+                const double Ri  = __dadd_rn( ri, rp );
+                const double tt  = __dadd_rn( -ddot( xci, xci ), __dmul_rn( Ri, Ri ) );
+
+                int  w[ 2 ] = { 0, 0 };
+                d3   x[ 2 ];
+                if ( tt >= 0.0 )
+                {
+                    const d3     nn   = dnrm( dcross( cij.normal, cik.normal ) );
+                    const double root = __dsqrt_rn( tt );
+                    x[ 0 ]            = dadd( xc, dmul( nn, root ) );
+                    x[ 1 ]            = dsub( xc, dmul( nn, root ) );
+                    bool vis[ 2 ]     = { true, true };
+                    f3   xr[ 2 ];
+                    for ( int e = 0; e < 2; e++ )
+                        xr[ e ] = F3( __double2float_rn( __dsub_rn( x[ e ].x, ci.x ) ),
+                                      __double2float_rn( __dsub_rn( x[ e ].y, ci.y ) ),
+                                      __double2float_rn( __dsub_rn( x[ e ].z, ci.z ) ) );
+                    const uint32_t ni = b.nbrCount[ i ];
+                    for ( uint32_t sl = 0; sl < ni && ( vis[ 0 ] || vis[ 1 ] ); sl++ )
+                    {
+                        if ( sl == sj || sl == sk )
+                            continue;
+                        const float4 al  = b.atoms[ b.nbr[ (size_t)i * b.cap + sl ] ];
+                        const f3     dl  = F3( al.x - ai.x, al.y - ai.y, al.z - ai.z );
+                        const float  Rl  = al.w + b.rp;
+                        const float  Rl2 = Rl * Rl;
+                        for ( int e = 0; e < 2; e++ )
+                        {
+                            if ( !vis[ e ] )
+                                continue;
+                            const f3    ev = dl - xr[ e ];
+                            const float ee = dot( ev, ev );
+                            const float m  = ee - Rl2;
+                            const float em = kRel * ( ee + Rl2 + 1.f );
+                            if ( m < -em )
+                                vis[ e ] = false;
+                            else if ( !( m > em ) )
+                            {
+                                const double Rld = __dadd_rn( (double)al.w, rp );
+                                const d3     dv  = dsub( D3( al ), x[ e ] );
+                                vis[ e ]         = __dsub_rn( ddot( dv, dv ), __dmul_rn( Rld, Rld ) ) > 0.0;
+                                fp64++;
+                            }
+                        }
+                    }
+                    if ( vis[ 0 ] || vis[ 1 ] )
+                    {
+                        const d3 p2p3 = dnrm( dsub( cj, ci ) );
+                        const d3 p4p3 = dnrm( dsub( cj, ck ) );
+                        const d3 pn   = dnrm( dcross( p2p3, p4p3 ) );
+                        for ( int e = 0; e < 2; e++ )
+                        {
+                            if ( !vis[ e ] )
+                                continue;
+                            const double dd       = ddot( dsub( ci, x[ e ] ), pn );
+                            const bool   singular = __dsub_rn( __dmul_rn( dd, dd ), __dmul_rn( rp, rp ) ) < -tol;
+                            w[ e ]                = ( e == 0 ? 1 : -1 ) * ( 1 + ( singular ? 1 : 0 ) );
+                        }
+                    }
+                }
+                for ( int e = 0; e < 2; e++ )
+                {
+                    const size_t q = 2ull * c + e;
+                    const int    s = w[ e ] == 2 || w[ e ] == -2;
+                    b.isSing[ q ]  = w[ e ] != 0 && s;
+                    b.isReg[ q ]   = w[ e ] != 0 && !s;
+                    if ( w[ e ] == 0 )
+                    {
+                        b.slotCid[ q ] = make_int4( 0, 0, 0, 0 );
+                        continue;
+                    }
+                    b.slotPos[ q ] = make_float4( __double2float_rn( x[ e ].x ), __double2float_rn( x[ e ].y ),
+                                                  __double2float_rn( x[ e ].z ), (float)w[ e ] );
+                    if ( b.mode == 0 )
+                        b.slotCid[ q ] = make_int4( (int)t, (int)b.slotTrim[ slotJK ], (int)b.slotTrim[ slotIK ], w[ e ] );
+                    else
+                        b.slotCid[ q ] = make_int4( (int)slotIJ, (int)slotIK, (int)slotJK, w[ e ] );
+                }
+            }
+            for ( int o = 16; o > 0; o >>= 1 )
+                fp64 += __shfl_xor_sync( 0xffffffffu, fp64, o );
+            if ( lane_id() == 0 && fp64 )
+                atomicAdd( &b.counts->fp64[ kFp64Occlusion ], fp64 );
+        }
+
+        // ---- stable partition (singular first) and fill ----------------------
+        __global__ void k_place( Build b )
+        {
+            const uint32_t ns  = 2u * min( b.counts->cand, b.capCand );
+            const uint32_t Q   = b.counts->Q;
+            uint32_t       ovf = 0;
+            if ( blockIdx.x == 0 && threadIdx.x == 0 )
+                b.counts->I = Q + b.counts->regTotal;
+            for ( uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < ns; q += gridDim.x * blockDim.x )
+            {
+                const int4 cid = b.slotCid[ q ];
+                if ( cid.w == 0 )
+                    continue;
+                const bool     sing = cid.w == 2 || cid.w == -2;
+                const uint32_t idx  = sing ? b.isSing[ q ] : Q + b.isReg[ q ];
+                if ( idx >= b.capProbes )
+                {
+                    ovf |= kOverflowProbes;
+                    continue;
+                }
+                b.probePos[ idx ] = b.slotPos[ q ];
+                b.probeCid[ idx ] = cid;
+                uint32_t i, j, k;
+                if ( b.mode == 0 )
+                {
+                    const uint32_t sIJ = b.trimSlot[ cid.x ];
+                    i                  = sIJ / b.cap;
+                    j                  = b.nbr[ sIJ ];
+                    k                  = b.nbr[ b.trimSlot[ cid.z ] ];
+                    atomicAdd( &b.ccount[ cid.x ], 1u );
+                    atomicAdd( &b.ccount[ cid.y ], 1u );
+                    atomicAdd( &b.ccount[ cid.z ], 1u );
+                }
+                else
+                {
+                    i = (uint32_t)cid.x / b.cap;
+                    j = b.nbr[ cid.x ];
+                    k = b.nbr[ cid.y ];
+                    // exterior: the probe's three circles become tori (status 1 -> 2)
+                    if ( b.status[ cid.x ] == 1 )
+                        b.status[ cid.x ] = 2;
+                    if ( b.status[ cid.y ] == 1 )
+                        b.status[ cid.y ] = 2;
+                    if ( b.status[ cid.z ] == 1 )
+                        b.status[ cid.z ] = 2;
+                }
+                b.probeIds[ idx ] = make_int4( (int)i, (int)j, (int)k, 0 );
+            }
+            if ( ovf )
+                atomicOr( &b.counts->overflow, ovf );
+        }
+
+        __global__ void k_lists( Build b )
+        {
+            const uint32_t I = min( b.counts->I, b.capProbes );
+            for ( uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < I; q += gridDim.x * blockDim.x )
+            {
+                const int4     cid = b.probeCid[ q ];
+                const uint32_t t3[ 3 ] = { (uint32_t)cid.x, (uint32_t)cid.y, (uint32_t)cid.z };
+                for ( int e = 0; e < 3; e++ )
+                {
+                    const uint32_t t   = t3[ e ];
+                    const uint32_t pos = b.cstart[ t ] + atomicAdd( &b.ccursor[ t ], 1u );
+                    b.clist[ pos ]     = q;
+                }
+            }
+        }
+
+        __global__ void k_segment_counts( Build b )
+        {
+            const uint32_t C1 = min( b.counts->C1, b.capC1 );
+            for ( uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < C1; t += gridDim.x * blockDim.x )
+            {
+                const uint32_t c = min( b.ccount[ t ], b.segCap );
+                b.segCnt[ t ]    = c / 2u;
+                if ( b.ccount[ t ] > b.segCap )
+                    atomicAdd( &b.counts->segTruncated, 1u );
+            }
+        }
+
+        // ---- segments (buildSegments, operations.inl:552-668) ---------------
+        __global__ void __launch_bounds__( 128 ) k_segments( Build b )
+        {
+            const uint32_t C1  = min( b.counts->C1, b.capC1 );
+            uint32_t       ovf = 0;
+            for ( uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < C1; t += gridDim.x * blockDim.x )
+            {
+                const uint32_t cnt = b.ccount[ t ];
+                if ( cnt < 2 )
+                    continue;
+                if ( cnt > (uint32_t)kSegBuf )
+                {
+                    ovf |= kOverflowList;
+                    continue;
+                }
+                uint32_t         lst[ kSegBuf ];
+                const uint32_t * src = b.clist + b.cstart[ t ];
+                for ( uint32_t m = 0; m < cnt; m++ )
+                {
+                    // insertion into ascending order
+                    const uint32_t v = src[ m ];
+                    uint32_t       p = m;
+                    while ( p > 0 && lst[ p - 1 ] > v )
+                    {
+                        lst[ p ] = lst[ p - 1 ];
+                        p--;
+                    }
+                    lst[ p ] = v;
+                }
+                const uint32_t nb  = min( cnt, b.segCap );
+                const uint32_t sIJ = b.trimSlot[ t ];
+                const uint32_t i   = sIJ / b.cap;
+                const uint32_t j   = b.nbr[ sIJ ];
+                const float4   ai = b.atoms[ i ], aj = b.atoms[ j ];
+                const dcircle  geo = dcircle_geometry( D3( ai ), (double)ai.w, D3( aj ), (double)aj.w, (double)b.rp );
+
+                const uint32_t st          = lst[ 0 ];
+                const int4     sids        = b.probeIds[ st ];
+                const float4   spos        = b.probePos[ st ];
+                const bool     isSecondary = (int)i == sids.x && (int)j == sids.z;
+                const double   direction   = copysign( 1.0, (double)spos.w ) * ( isSecondary ? -1.0 : 1.0 );
+                const d3       ref         = dsub( D3( spos ), geo.center );
+
+                double  key[ kSegBuf ];
+                uint8_t ord[ kSegBuf ];
+                key[ 0 ] = 0.0;
+                ord[ 0 ] = 0;
+                for ( uint32_t m = 1; m < nb; m++ )
+                {
+                    d3 v1 = ref;
+                    d3 v2 = dnrm( dsub( D3( b.probePos[ lst[ m ] ] ), geo.center ) );
+                    if ( direction < 0.0 )
+                    {
+                        const d3 tmp = v1;
+                        v1           = v2;
+                        v2           = tmp;
+                    }
+                    const double kv = dpseudo_angle( v1, v2, geo.normal );
+                    // stable insertion by (key, m)
+                    uint32_t p = m;
+                    while ( p > 0 && key[ p - 1 ] > kv )
+                    {
+                        key[ p ] = key[ p - 1 ];
+                        ord[ p ] = ord[ p - 1 ];
+                        p--;
+                    }
+                    key[ p ] = kv;
+                    ord[ p ] = (uint8_t)m;
+                }
+                uint32_t out = b.segOff[ t ];
+                for ( uint32_t m = 0; m + 1 < nb; m += 2, out++ )
+                {
+                    uint32_t a1 = lst[ ord[ m ] ], a2 = lst[ ord[ m + 1 ] ];
+                    if ( direction < 0.0 )
+                    {
+                        const uint32_t tmp = a1;
+                        a1                 = a2;
+                        a2                 = tmp;
+                    }
+                    if ( out < b.capSeg )
+                        b.segments[ out ] = make_uint4( i, j, a1, a2 );
+                    else
+                        ovf |= kOverflowSeg;
+                }
+            }
+            if ( ovf )
+                atomicOr( &b.counts->overflow, ovf );
+        }
+
+        // ---- neighbours of singular probes -------------------------------------
+        __global__ void __launch_bounds__( 32 * kWarpsPerBlock ) k_probe_neighbors( Build b )
+        {
+            __shared__ unsigned long long buf[ kWarpsPerBlock ][ kSnbrBuf ];
+            const uint32_t                warp = threadIdx.x >> 5, lane = lane_id();
+            const uint32_t                Q    = min( b.counts->Q, b.capProbes );
+            const FineGrid                g    = *b.fine;
+            const float                   t2   = 2.f * b.rp;
+            const double                  t2d  = 2.0 * (double)b.rp;
+            uint32_t                      fp64 = 0, trunc = 0;
+            for ( uint32_t q = blockIdx.x * kWarpsPerBlock + warp; q < Q; q += gridDim.x * kWarpsPerBlock )
+            {
+                const float4 pq = b.probePos[ q ];
+                Rows         rows;
+                stencil_rows( g, b.cellStart, fine_cell( g, pq.x, pq.y, pq.z ), rows );
+                uint32_t count = 0;
+                for ( uint32_t base = 0; base < rows.total; base += 32 )
+                {
+                    const uint32_t     f    = base + lane;
+                    bool               pass = false;
+                    unsigned long long key  = 0;
+                    if ( f < rows.total )
+                    {
+                        const uint32_t idx = row_item( rows, f );
+                        const uint32_t p   = b.cellItems[ idx ];
+                        if ( p != q )
+                        {
+                            const float4 pp = b.cellPos[ idx ];
+                            const f3     dv = F3( pq.x - pp.x, pq.y - pp.y, pq.z - pp.z );
+                            const float  d2 = dot( dv, dv );
+                            const float  m  = d2 - t2 * t2;
+                            const float  e  = kRel * ( d2 + t2 * t2 + 1.f );
+                            if ( m < -e )
+                                pass = true;
+                            else if ( !( m > e ) )
+                            {
+                                const d3 dd = dsub( D3( pq ), D3( pp ) );
+                                pass        = __dsqrt_rn( ddot( dd, dd ) ) < t2d;
+                                fp64++;
+                            }
+                            if ( pass )
+                                key = ( (unsigned long long)ref_grid_hash( b.grid, ref_grid_position( b.grid, pp.x, pp.y, pp.z ) ) << 32 )
+                                      | p;
+                        }
+                    }
+                    const uint32_t mask = __ballot_sync( 0xffffffffu, pass );
+                    const uint32_t pos  = count + __popc( mask & lanemask_lt() );
+                    if ( pass && pos < kSnbrBuf )
+                        buf[ warp ][ pos ] = key;
+                    count += __popc( mask );
+                }
+                __syncwarp();
+                const uint32_t held = count < kSnbrBuf ? count : kSnbrBuf;
+                warp_bitonic_sort<unsigned long long>( buf[ warp ], held, kSnbrBuf, ~0ull );
+                const uint32_t kept = held < kMaxProbeNbr ? held : kMaxProbeNbr;
+                if ( lane < kept )
+                {
+                    const uint32_t p  = (uint32_t)( buf[ warp ][ lane ] & 0xffffffffull );
+                    const float4   pp = b.probePos[ p ];
+                    const float    wv = b.mode == 0 ? __fmul_rn( __fmul_rn( pq.x, pq.y ), pq.z ) : 0.f;
+                    b.probeNbrs[ (size_t)q * kMaxProbeNbr + lane ] = make_float4( pp.x, pp.y, pp.z, wv );
+                }
+                if ( lane == 0 )
+                {
+                    b.probeIds[ q ].w = (int)kept;
+                    if ( count > kMaxProbeNbr )
+                        trunc++;
+                }
+                __syncwarp();
+            }
+            for ( int o = 16; o > 0; o >>= 1 )
+                fp64 += __shfl_xor_sync( 0xffffffffu, fp64, o );
+            if ( lane == 0 )
+            {
+                if ( fp64 )
+                    atomicAdd( &b.counts->fp64[ kFp64SingularNbr ], fp64 );
+                if ( trunc )
+                    atomicAdd( &b.counts->snbrTruncated, trunc );
+            }
+        }
+
+        // exterior: probe position w becomes the index of its neighbour block
+        // (ssesdf/operations.cu:397); done after every neighbour search read xyz
+        __global__ void k_probe_w( Build b )
+        {
+            const uint32_t Q = min( b.counts->Q, b.capProbes );
+            for ( uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < Q; q += gridDim.x * blockDim.x )
+                b.probePos[ q ].w = (float)(int)( q * kMaxProbeNbr );
+        }
+
+        // ---- exterior tori ---------------------------------------------------
+        __global__ void __launch_bounds__( 32 * kWarpsPerBlock ) k_tori_count( Build b )
+        {
+            const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
+            const uint32_t i    = blockIdx.x * kWarpsPerBlock + warp;
+            if ( i >= b.n )
+                return;
+            const uint32_t ni = b.nbrCount[ i ];
+            uint32_t       c  = 0;
+            for ( uint32_t s = lane; s < ni; s += 32 )
+                c += b.status[ (size_t)i * b.cap + s ] == 2;
+            for ( int o = 16; o > 0; o >>= 1 )
+                c += __shfl_xor_sync( 0xffffffffu, c, o );
+            if ( lane == 0 )
+                b.torCnt[ i ] = c;
+        }
+
+        __global__ void __launch_bounds__( 32 * kWarpsPerBlock ) k_tori( Build b )
+        {
+            const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
+            const uint32_t i    = blockIdx.x * kWarpsPerBlock + warp;
+            if ( i >= b.n )
+                return;
+            const uint32_t ni   = b.nbrCount[ i ];
+            const float4   ai   = b.atoms[ i ];
+            uint32_t       base = b.torOff[ i ], ovf = 0, degenerate = 0;
+            for ( uint32_t s0 = 0; s0 < ni; s0 += 32 )
+            {
+                const uint32_t s     = s0 + lane;
+                const bool     valid = s < ni && b.status[ (size_t)i * b.cap + s ] == 2;
+                const uint32_t m     = __ballot_sync( 0xffffffffu, valid );
+                if ( valid )
+                {
+                    const uint32_t idx = base + __popc( m & lanemask_lt() );
+                    const float4   aj  = b.atoms[ b.nbr[ (size_t)i * b.cap + s ] ];
+                    const float    Ri  = ai.w + b.rp;
+                    const float    Rj  = aj.w + b.rp;
+                    const f3       dj  = F3( aj.x - ai.x, aj.y - ai.y, aj.z - ai.z );
+                    const float    d   = dot( dj, dj );
+                    const float    t   = ( Ri * Ri - Rj * Rj + d ) / ( 2.f * d );
+                    const f3       c   = dj * t; // circle centre relative to atom i
+                    const float    r   = sqrtf( fmaxf( Ri * Ri - dot( c, c ), 0.f ) );
+                    const f3       ta  = normalize( c );
+                    f3             cz  = cross( ta, F3( 0.f, 0.f, 1.f ) );
+                    if ( dot( cz, cz ) < 1e-12f )
+                    {
+                        // the reference normalises a zero vector here (NaN); use the x axis instead
+                        cz = cross( ta, F3( 1.f, 0.f, 0.f ) );
+                        degenerate++;
+                    }
+                    const f3    ortho = normalize( cz );
+                    const f3    P     = c + ortho * r;
+                    const f3    X     = normalize( P ) * ai.w;
+                    const float lpi   = sqrtf( dot( P, P ) );
+                    const f3    Pj    = P - dj;
+                    const float lpj   = sqrtf( dot( Pj, Pj ) );
+                    const f3    C     = dj * ( lpi / ( lpj + lpi ) );
+                    const f3    XC    = X - C;
+                    const float dist  = sqrtf( dot( XC, XC ) );
+                    const f3    Cout  = C - c;
+                    if ( idx < b.capTori )
+                    {
+                        b.torPos[ idx ]  = make_float4( ai.x + c.x, ai.y + c.y, ai.z + c.z, r );
+                        b.torAxis[ idx ] = make_float4( ta.x, ta.y, ta.z, b.rp );
+                        b.torVs[ idx ]   = make_float4( Cout.x, Cout.y, Cout.z, dist );
+                    }
+                    else
+                        ovf |= kOverflowTori;
+                }
+                base += __popc( m );
+            }
+            for ( int o = 16; o > 0; o >>= 1 )
+                degenerate += __shfl_xor_sync( 0xffffffffu, degenerate, o );
+            if ( lane == 0 && degenerate )
+                atomicAdd( &b.counts->torusDegenerate, degenerate );
+            if ( ovf )
+                atomicOr( &b.counts->overflow, ovf );
+        }
+
+        // ---- reference-layout analysis buffers --------------------------------
+        // globalToTrimmedId (operations.inl:46-47): exclusive count of partial
+        // slots over the whole N x cap slot array, plus one trailing total
+        __global__ void k_reference_fill( Build b, uint32_t * g2t )
+        {
+            const uint64_t total = (uint64_t)b.n * b.cap;
+            for ( uint64_t q = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x; q <= total; q += (uint64_t)gridDim.x * blockDim.x )
+            {
+                if ( q == total )
+                {
+                    if ( g2t )
+                        g2t[ q ] = b.counts->C1;
+                    continue;
+                }
+                const uint32_t i = (uint32_t)( q / b.cap ), s = (uint32_t)( q % b.cap );
+                const uint32_t ni = b.nbrCount[ i ];
+                if ( s >= ni )
+                {
+                    b.status[ q ] = 0;
+                    if ( g2t )
+                        g2t[ q ] = b.partOff[ i ] + b.partCnt[ i ];
+                }
+                else if ( g2t )
+                    g2t[ q ] = b.slotTrim[ q ];
+            }
+        }
+
+        inline uint32_t blocks_for( uint64_t n, uint32_t threads )
+        {
+            return (uint32_t)( ( n + threads - 1 ) / threads );
+        }
+        inline uint32_t persistent_blocks( uint32_t threads )
+        {
+            // a few waves over 152 SMs for grid-stride kernels whose length is on the device
+            return 152u * ( 2048u / threads );
+        }
+    } // namespace
+
+    void launch_hash( const Build & b, cudaStream_t s )
+    {
+        if ( b.n )
+            k_hash<<<blocks_for( b.n, 256 ), 256, 0, s>>>( b );
+    }
+    void launch_fine_params( const Build & b, float cutoff, uint32_t, cudaStream_t s ) { k_fine_params<<<1, 1, 0, s>>>( b, cutoff ); }
+    void launch_gather( const Build & b, cudaStream_t s )
+    {
+        if ( b.n )
+            k_gather<<<blocks_for( b.n, 256 ), 256, 0, s>>>( b );
+    }
+    void launch_cells( const Build & b, const float4 * pos, uint32_t nHost, const uint32_t * nDevice, void * scanScratch,
+                       cudaStream_t s )
+    {
+        cudaMemsetAsync( b.cellCount, 0, sizeof( uint32_t ) * ( (size_t)b.capCells + 1 ), s );
+        cudaMemsetAsync( b.cellCursor, 0, sizeof( uint32_t ) * ( (size_t)b.capCells + 1 ), s );
+        if ( nHost == 0 )
+            return;
+        const uint32_t blocks = nDevice ? min( persistent_blocks( 256 ), blocks_for( nHost, 256 ) ) : blocks_for( nHost, 256 );
+        k_cell_count<<<blocks, 256, 0, s>>>( b, pos, nHost, nDevice );
+        const uint32_t * cells = reinterpret_cast<const uint32_t *>( reinterpret_cast<const char *>( b.fine ) + offsetof( FineGrid, cells ) );
+        exclusive_scan( b.cellCount, b.cellStart, b.capCells, cells, nullptr, scanScratch, s );
+        k_cell_scatter<<<blocks, 256, 0, s>>>( b, pos, nHost, nDevice );
+    }
+    void launch_neighbors( const Build & b, cudaStream_t s )
+    {
+        if ( b.n )
+            k_neighbors<<<blocks_for( b.n, kWarpsPerBlock ), 32 * kWarpsPerBlock, 0, s>>>( b );
+    }
+    void launch_visibility( const Build & b, cudaStream_t s )
+    {
+        if ( !b.n )
+            return;
+        const size_t smem = sizeof( float4 ) * (size_t)b.cap * kWarpsPerBlock;
+        k_visibility<<<blocks_for( b.n, kWarpsPerBlock ), 32 * kWarpsPerBlock, smem, s>>>( b );
+    }
+    void launch_emit( const Build & b, cudaStream_t s )
+    {
+        if ( b.n )
+            k_emit<<<blocks_for( b.n, kWarpsPerBlock ), 32 * kWarpsPerBlock, 0, s>>>( b );
+    }
+    void launch_candidates( const Build & b, bool write, cudaStream_t s )
+    {
+        k_candidates<<<min( persistent_blocks( 256 ), blocks_for( b.capC1, 256 ) + 1 ), 256, 0, s>>>( b, write );
+    }
+    void launch_triplets( const Build & b, cudaStream_t s )
+    {
+        k_triplets<<<min( persistent_blocks( 128 ), blocks_for( b.capCand, 128 ) + 1 ), 128, 0, s>>>( b );
+    }
+    void launch_place( const Build & b, cudaStream_t s )
+    {
+        k_place<<<min( persistent_blocks( 256 ), blocks_for( 2ull * b.capCand, 256 ) + 1 ), 256, 0, s>>>( b );
+    }
+    void launch_lists( const Build & b, cudaStream_t s )
+    {
+        k_lists<<<min( persistent_blocks( 256 ), blocks_for( b.capProbes, 256 ) + 1 ), 256, 0, s>>>( b );
+    }
+    void launch_segment_counts( const Build & b, cudaStream_t s )
+    {
+        k_segment_counts<<<min( persistent_blocks( 256 ), blocks_for( b.capC1, 256 ) + 1 ), 256, 0, s>>>( b );
+    }
+    void launch_segments( const Build & b, cudaStream_t s )
+    {
+        k_segments<<<min( persistent_blocks( 128 ), blocks_for( b.capC1, 128 ) + 1 ), 128, 0, s>>>( b );
+    }
+    void launch_probe_neighbors( const Build & b, cudaStream_t s )
+    {
+        k_probe_neighbors<<<min( persistent_blocks( 256 ), blocks_for( b.capProbes, kWarpsPerBlock ) + 1 ), 32 * kWarpsPerBlock, 0, s>>>( b );
+        if ( b.mode == 1 )
+            k_probe_w<<<min( persistent_blocks( 256 ), blocks_for( b.capProbes, 256 ) + 1 ), 256, 0, s>>>( b );
+    }
+    void launch_tori( const Build & b, cudaStream_t s )
+    {
+        if ( !b.n )
+            return;
+        k_tori_count<<<blocks_for( b.n, kWarpsPerBlock ), 32 * kWarpsPerBlock, 0, s>>>( b );
+    }
+    void launch_tori_emit( const Build & b, cudaStream_t s )
+    {
+        if ( b.n )
+            k_tori<<<blocks_for( b.n, kWarpsPerBlock ), 32 * kWarpsPerBlock, 0, s>>>( b );
+    }
+    cudaError_t configure_kernels( const Build & b )
+    {
+        const size_t smem = sizeof( float4 ) * (size_t)b.cap * kWarpsPerBlock;
+        return cudaFuncSetAttribute( k_visibility, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem );
+    }
+    void launch_reference_fill( const Build & b, uint32_t * globalToTrimmed, cudaStream_t s )
+    {
+        const uint64_t total = (uint64_t)b.n * b.cap + 1;
+        k_reference_fill<<<min( persistent_blocks( 256 ), blocks_for( total, 256 ) ), 256, 0, s>>>( b, globalToTrimmed );
+    }
+} // namespace sesgb

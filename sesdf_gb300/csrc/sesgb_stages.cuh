@@ -1,0 +1,107 @@
+// sesgb_stages.cuh -- parameter block of the SES build kernels and their launchers.
+#pragma once
+#include "sesgb_internal.h"
+
+namespace sesgb
+{
+    constexpr int kWarpsPerBlock = 8;               // warp-per-item kernels: 256 threads
+    constexpr int kNbrBuf        = 512;             // per-warp candidate buffer of the neighbour search
+    constexpr int kSegBuf        = 64;              // probes per circle the segment stage can hold
+    constexpr int kSnbrBuf       = 256;             // per-warp candidate buffer of the singular-probe search
+    constexpr uint32_t kMaxProbeNbr = 32;           // MaxIntersectionNeighbors (sesdf.cu:18)
+
+    // Everything a kernel of the build needs, passed by value.
+    struct Build
+    {
+        // configuration
+        uint32_t n;      // atoms
+        uint32_t cap;    // neighbour slots per atom (MaxNeighborPerAtom)
+        uint32_t segCap; // probes per circle used for segments
+        int      mode;   // 0 full surface, 1 exterior only
+        float    rp;
+        GridRef  grid;
+
+        // capacities of the count-dependent buffers
+        uint32_t capSectors, capFull, capC1, capCand, capProbes, capSeg, capTori, capCells;
+
+        // atoms
+        float4 *       atomsIn; // input order (device copy)
+        float4 *       atoms;   // reference-grid order (the output "atoms")
+        uint32_t *     perm;    // sorted id -> input id
+        uint32_t *     keys;    // sort keys scratch (n)
+
+        // neighbour grid
+        FineGrid * fine;
+        uint32_t * cellCount; // capCells + 1
+        uint32_t * cellStart; // capCells + 1
+        uint32_t * cellCursor;
+        uint32_t * cellItems; // n (or Q) item ids in cell order
+        float4 *   cellPos;   // positions in cell order
+
+        // neighbour lists and circles, slot = i * cap + s (the reference layout)
+        uint32_t * nbr;
+        uint32_t * nbrCount;
+        uint8_t *  status;
+        uint32_t * slotTrim; // partial-circle number of each slot (exclusive count)
+
+        // per-atom counts and offsets
+        uint32_t *visCnt, *partCnt, *fullCnt, *torCnt;
+        uint32_t *visOff, *partOff, *fullOff, *torOff;
+
+        // convex patches
+        float4 * sectors;
+        uint2 *  convex;
+        uint2 *  fullCircles;
+
+        // partial circles
+        uint32_t * trimSlot; // C1
+        uint32_t * candCnt;  // C1 + 1
+        uint32_t * candOff;  // C1 + 1
+        uint4 *    cand;     // capCand: (t, slotIK, slotJK, -)
+
+        // probe slots (two per candidate)
+        uint32_t * isSing;  // 2 capCand + 1
+        uint32_t * isReg;   // 2 capCand + 1
+        float4 *   slotPos; // 2 capCand
+        int4 *     slotCid; // 2 capCand
+
+        // probes, final order (singular first)
+        int4 *     probeIds;  // capProbes: output ids
+        float4 *   probePos;  // capProbes: output positions
+        int4 *     probeCid;  // capProbes: circle ids (full: partial-circle numbers; exterior: slots)
+        float4 *   probeNbrs; // capProbes * 32
+        uint32_t * ccount;    // C1 + 1
+        uint32_t * cstart;    // C1 + 1
+        uint32_t * ccursor;   // C1
+        uint32_t * clist;     // 3 capProbes
+        uint32_t * segCnt;    // C1 + 1
+        uint32_t * segOff;    // C1 + 1
+        uint4 *    segments;  // capSeg
+
+        // exterior tori
+        float4 *torPos, *torAxis, *torVs;
+
+        DeviceCounts * counts;
+    };
+
+    // ---- launchers (sesgb_stages.cu) ---------------------------------------
+    void launch_hash( const Build & b, cudaStream_t s );
+    void launch_fine_params( const Build & b, float cutoff, uint32_t items, cudaStream_t s );
+    void launch_gather( const Build & b, cudaStream_t s );
+    void launch_cells( const Build & b, const float4 * pos, uint32_t nHost, const uint32_t * nDevice, void * scanScratch,
+                       cudaStream_t s );
+    void launch_neighbors( const Build & b, cudaStream_t s );
+    void launch_visibility( const Build & b, cudaStream_t s );
+    void launch_emit( const Build & b, cudaStream_t s );
+    void launch_candidates( const Build & b, bool write, cudaStream_t s );
+    void launch_triplets( const Build & b, cudaStream_t s );
+    void launch_place( const Build & b, cudaStream_t s );
+    void launch_lists( const Build & b, cudaStream_t s );
+    void launch_segment_counts( const Build & b, cudaStream_t s );
+    void launch_segments( const Build & b, cudaStream_t s );
+    void launch_probe_neighbors( const Build & b, cudaStream_t s );
+    void launch_tori( const Build & b, cudaStream_t s );
+    void launch_tori_emit( const Build & b, cudaStream_t s );
+    cudaError_t configure_kernels( const Build & b );
+    void launch_reference_fill( const Build & b, uint32_t * globalToTrimmed, cudaStream_t s );
+} // namespace sesgb

@@ -1,0 +1,86 @@
+"""Generates the golden fixtures: outputs of the reference's own CUDA kernels.
+
+Runs on a machine with a GPU and the reference harness built (oracle/_ref/, see
+oracle/Makefile): for each input it builds the reference's full-surface and
+exterior-only surfaces through oracle/refharness.py and stores the outputs in
+compact form (neighbour lists as CSR) in <outdir>/<case>_<mode>.npz, together
+with the input atoms, box and probe radius.
+
+    python tests/golden/make_golden.py <outdir> [case ...]
+"""
+import os
+import sys
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.dirname(HERE))
+
+from cases import hand_cases  # noqa: E402
+from oracle import refharness  # noqa: E402
+from sesdf_gb300 import synth  # noqa: E402
+
+RP = 1.4
+
+
+def golden_inputs():
+    cases = {k: v for k, v in hand_cases().items() if v.shape[0] > 0}
+    cases["globule2k"] = synth.globule(2000, 1000)
+    return cases
+
+
+def compact_neighbors(nbrs, ids, Q):
+    blocks = np.asarray(nbrs, np.float32).reshape(-1, 32, 4)
+    rows = [blocks[q, :max(0, min(32, int(ids[q, 3])))] for q in range(int(Q))]
+    return np.concatenate(rows) if rows else np.zeros((0, 4), np.float32)
+
+
+def compact(ref: dict, mode: str) -> dict:
+    c = ref["counts"]
+    cnt = ref["nbr_count"].astype(np.uint32)
+    rows = [ref["nbr_ids"][i, :cnt[i]] for i in range(len(cnt))]
+    srows = [ref["status"][i, :cnt[i]] for i in range(len(cnt))]
+    out = {
+        "perm": ref["perm"], "atoms_sorted": ref["atoms"], "nbr_count": cnt,
+        "nbr": np.concatenate(rows) if rows else np.zeros(0, np.uint32),
+        "status": np.concatenate(srows) if srows else np.zeros(0, np.uint8),
+        "probe_ids": ref["probe_ids"], "probe_pos": ref["probe_pos"],
+        # only the filled part of each probe's 32-entry neighbour block (the rest is unwritten memory)
+        "probe_nbrs": compact_neighbors(ref["probe_nbrs"], ref["probe_ids"], c["Q"]),
+        "counts": np.array([c[k] for k in refharness.COUNT_NAMES], np.uint64),
+    }
+    if mode == "full":
+        for k in ("convex", "full", "sectors", "segments"):
+            out[k] = ref[k]
+        g2t = ref["global_to_trimmed"]
+        cap = refharness.MAX_NBR
+        out["slot_trim"] = np.concatenate([g2t[i * cap:i * cap + cnt[i]] for i in range(len(cnt))]) if len(cnt) else np.zeros(0, np.uint32)
+    else:
+        for k in ("tori_pos", "tori_axis", "tori_vs"):
+            out[k] = ref[k]
+    return out
+
+
+def main():
+    outdir = sys.argv[1]
+    only = set(sys.argv[2:])
+    os.makedirs(outdir, exist_ok=True)
+    for name, atoms in golden_inputs().items():
+        if only and name not in only:
+            continue
+        for mode in ("full", "exterior"):
+            r = refharness.RefBuild(atoms, RP, mode)
+            r.build()
+            ref = r.fetch()
+            r.close()
+            data = compact(ref, mode)
+            box = r.box
+            np.savez_compressed(os.path.join(outdir, f"{name}_{mode}.npz"), atoms=atoms, box=box,
+                                probe_radius=np.float32(RP), **data)
+            print(name, mode, {k: int(v) for k, v in zip(refharness.COUNT_NAMES, data["counts"])}, flush=True)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,276 @@
+"""Comparison of the reference's own kernels with the FP64 oracle, band-aware.
+
+The reference evaluates its predicates in float32 with --use_fast_math
+(sesdf/CMakeLists.txt:117-125); the oracle evaluates the same expressions in
+double precision. They may disagree only where a predicate's margin is within
+the float32 error of the reference's arithmetic (the degeneracy band). Every
+difference found is checked against that band and reported as "explained" when
+its FP64 margin lies inside it, together with the cases that depend on it
+(probes on a circle whose status differs, segments of such circles).
+
+Band widths (|FP64 margin| below which a disagreement is explained):
+  neighbour   |d^2 - R^2 - 1e-4|            < 64 eps32 (d^2 + R^2)
+  visibility  |complete - R_k^2 - 1e-4|      < 2^-10 (complete + R_k^2)     (float32 sqrt(1-cos^2) amplifies)
+  occlusion   ||c_l - x|^2 - R_l^2|          < 2^-10 (|c_l - x|^2 + R_l^2)  (float32 triplet solve)
+  singular    |d^2 - rp^2 + 1e-4|            < 2^-10 (d^2 + rp^2)
+  probe pair  |t| (x1 = x2)                  < 2^-10 R_i^2
+"""
+from __future__ import annotations
+
+import numpy as np
+
+import canon
+
+EPS32 = 2.0 ** -23
+WIDE = 2.0 ** -10
+
+
+def _f(x):
+    return np.float64(np.float32(x))
+
+
+def circle_geometry(ci, ri, cj, rj, rp):
+    R1, R2 = ri + rp, rj + rp
+    d = np.dot(ci - cj, ci - cj)
+    t = (R1 * R1 - R2 * R2 + d) / (2 * d)
+    c = ci + (cj - ci) * t
+    r = np.sqrt(max(R1 * R1 - np.dot(ci - c, ci - c), 0.0))
+    n = (cj - ci) / np.sqrt(np.dot(cj - ci, cj - ci))
+    return c, n, r
+
+
+def status_margin(pos, rad, i, j, nbrs, rp):
+    """Smallest |margin| over k of the two visibility predicates of circle (i, j)."""
+    c, n, r = circle_geometry(pos[i], rad[i], pos[j], rad[j], rp)
+    best = np.inf
+    for k in nbrs:
+        if k == j:
+            continue
+        v = c - pos[k]
+        dist = np.sqrt(np.dot(v, v))
+        s = np.dot(v, n)
+        p = np.sqrt(max(dist * dist - s * s, 0.0))
+        if dist == 0.0 or p < 1e-2 * dist:
+            # k on the circle's axis: the reference's sqrt(1 - cos^2) is NaN or
+            # loses half its digits in float32 (operations.cu:172-179)
+            return 0.0
+        Rk2 = (rad[k] + rp) ** 2
+        for sign in (1.0, -1.0):
+            comp = (sign * p + r) ** 2 + s * s
+            m = abs(comp - Rk2 - _f(1e-4))
+            best = min(best, m / (comp + Rk2))
+    return best
+
+
+def probe_solutions(pos, rad, i, j, k, rp):
+    ci, cj, ck = pos[i], pos[j], pos[k]
+    cij, nij, _ = circle_geometry(ci, rad[i], cj, rad[j], rp)
+    cik, nik, _ = circle_geometry(ci, rad[i], ck, rad[k], rp)
+    u = nik - nij * np.dot(nik, nij)
+    den = np.dot(u, nik)
+    xc = cij + u * (np.dot(cik - cij, nik) / den)
+    Ri2 = (rad[i] + rp) ** 2
+    t = Ri2 - np.dot(xc - ci, xc - ci)
+    if not t >= 0:
+        return None, t / Ri2
+    nn = np.cross(nij, nik)
+    nn = nn / np.linalg.norm(nn)
+    return (xc + nn * np.sqrt(t), xc - nn * np.sqrt(t)), t / Ri2
+
+
+def occlusion_margin(pos, rad, x, i, exclude, nbrs, rp):
+    best = np.inf
+    for l in nbrs:
+        if l in exclude:
+            continue
+        e = pos[l] - x
+        ee = np.dot(e, e)
+        Rl2 = (rad[l] + rp) ** 2
+        best = min(best, abs(ee - Rl2) / (ee + Rl2))
+    return best
+
+
+def compare(atoms_in: np.ndarray, rp: float, mode: str, ref: dict, o: dict) -> dict:
+    """ref: reference outputs (compact golden form); o: oracle.run output. Returns a report."""
+    rpd = _f(rp)
+    n = atoms_in.shape[0]
+    pos = atoms_in[:, :3].astype(np.float64)
+    rad = atoms_in[:, 3].astype(np.float64)
+    rep = {"perm_mismatch": int(np.count_nonzero(ref["perm"] != o["perm"]))}
+
+    # neighbours (input ids)
+    roff = np.concatenate([[0], np.cumsum(ref["nbr_count"].astype(np.int64))])
+    rrows = [ref["nbr"][roff[s]:roff[s + 1]] for s in range(n)]
+    ocnt, orows = canon.csr_rows(o["noff"], o["nbr"])
+    rn = canon.neighbor_sets(ref["perm"], ref["nbr_count"], rrows)
+    on = canon.neighbor_sets(o["perm"], ocnt, orows)
+    bad_pairs = set()
+    unexplained = 0
+    for a in range(n):
+        for b in rn[a] ^ on[a]:
+            d2 = np.dot(pos[a] - pos[b], pos[a] - pos[b])
+            R = (rad[a] + rpd) + (rad[b] + rpd)
+            m = abs(d2 - R * R - _f(1e-4))
+            bad_pairs.add(frozenset((a, b)))
+            if m >= 64 * EPS32 * (d2 + R * R):
+                unexplained += 1
+    rep["nbr_mismatch"] = len(bad_pairs)
+    rep["nbr_unexplained"] = unexplained
+
+    # statuses of directed circles (input ids)
+    srows_r = [ref["status"][roff[s]:roff[s + 1]] for s in range(n)]
+    srows_o = [o["status"][o["noff"][s]:o["noff"][s + 1]] for s in range(n)]
+    ext = mode == "exterior"
+    sr = canon.status_map(ref["perm"], ref["nbr_count"], rrows, srows_r, ext)
+    so = canon.status_map(o["perm"], ocnt, orows, srows_o, ext)
+    tainted = set()
+    st_bad = st_unexp = 0
+    for key in set(sr) | set(so):
+        if sr.get(key) == so.get(key):
+            continue
+        a, b = key
+        if frozenset(key) in bad_pairs:
+            tainted.add(frozenset(key))
+            st_bad += 1
+            continue
+        if ext and ( key not in sr or key not in so ):
+            # sorted order decides which direction is evaluated
+            continue
+        st_bad += 1
+        tainted.add(frozenset(key))
+        if status_margin(pos, rad, a, b, sorted(on[a]), rpd) >= WIDE:
+            st_unexp += 1
+    rep["status_mismatch"] = st_bad
+    rep["status_unexplained"] = st_unexp
+
+    # probes
+    rk = canon.probe_keys(atoms_in, ref["perm"], ref["probe_ids"], ref["probe_pos"])
+    ok = canon.probe_keys(atoms_in, o["perm"], o["ids"], o["posf"])
+    rmap = {k: q for q, k in enumerate(rk)}
+    omap = {k: q for q, k in enumerate(ok)}
+    pr_bad = pr_unexp = 0
+    bad_probes = set()
+    for key in set(rmap) ^ set(omap):
+        pr_bad += 1
+        bad_probes.add(key)
+        trip = key[0]
+        circles = [frozenset((trip[0], trip[1])), frozenset((trip[0], trip[2])), frozenset((trip[1], trip[2]))]
+        if any(c in tainted or c in bad_pairs for c in circles):
+            continue
+        # margins of the triplet solve and of the occlusion test
+        explained = False
+        for owner in trip:
+            others = [t for t in trip if t != owner]
+            sol, tnorm = probe_solutions(pos, rad, owner, others[0], others[1], rpd)
+            if sol is None or abs(tnorm) < WIDE:
+                explained = True
+                break
+            for x in sol:
+                if canon.side(atoms_in, trip, x) != key[1]:
+                    continue
+                if occlusion_margin(pos, rad, x, owner, set(trip), on[owner], rpd) < WIDE:
+                    explained = True
+        if not explained:
+            pr_unexp += 1
+    rep["probe_mismatch"] = pr_bad
+    rep["probe_unexplained"] = pr_unexp
+    if ext and st_unexp:
+        # exterior statuses are read after probes promoted their circles to tori;
+        # a probe present on one side only changes its three circles
+        probe_circles = set()
+        for key in bad_probes:
+            t = key[0]
+            probe_circles |= {frozenset((t[0], t[1])), frozenset((t[0], t[2])), frozenset((t[1], t[2]))}
+        st_unexp = 0
+        for key in set(sr) | set(so):
+            if sr.get(key) == so.get(key) or key not in sr or key not in so:
+                continue
+            fk = frozenset(key)
+            if fk in bad_pairs or fk in probe_circles:
+                continue
+            if status_margin(pos, rad, key[0], key[1], sorted(on[key[0]]), rpd) >= WIDE:
+                st_unexp += 1
+        rep["status_unexplained"] = st_unexp
+    common = sorted(set(rmap) & set(omap))
+    if common:
+        rq = np.array([rmap[k] for k in common])
+        oq = np.array([omap[k] for k in common])
+        err = np.abs(ref["probe_pos"][rq, :3].astype(np.float64) - o["posd"][oq, :3])
+        rep["probe_pos_max_err"] = float(err.max())
+        rep["probe_pos_over_1e-4"] = int(np.count_nonzero(err.max(axis=1) > 1e-4))
+        rsing = np.abs(ref["probe_pos"][rq, 3]) == 2 if not ext else None
+        osing = np.abs(o["cids"][oq, 3]) == 2
+        if rsing is None:
+            # exterior: w of a singular probe holds its neighbour-block index; singular
+            # probes are the first Q
+            rsing = rq < ref["counts"][5]
+        rep["singular_mismatch"] = int(np.count_nonzero(rsing != osing))
+    else:
+        rep["probe_pos_max_err"] = 0.0
+        rep["probe_pos_over_1e-4"] = 0
+        rep["singular_mismatch"] = 0
+    rep["probes_common"] = len(common)
+
+    if mode == "full":
+        # sectors per directed circle (input ids), in each side's slot order
+        def sector_map(perm, cnt, rows, st_rows, sectors):
+            out, q = {}, 0
+            for s in range(n):
+                for e in range(cnt[s]):
+                    if st_rows[s][e] != 0:
+                        out[(int(perm[s]), int(perm[rows[s][e]]))] = sectors[q]
+                        q += 1
+            return out
+        sm_r = sector_map(ref["perm"], ref["nbr_count"], rrows, srows_r, ref["sectors"])
+        sm_o = sector_map(o["perm"], ocnt, orows, srows_o, o["sectors"])
+        common_s = set(sm_r) & set(sm_o)
+        # axis error, and half-angle error compared through its cosine (the angle
+        # itself is ill-conditioned next to 0 and pi, e.g. for tangent spheres)
+        rep["sector_axis_max_err"] = float(max((np.max(np.abs(np.asarray(sm_r[k][:3], np.float64) - sm_o[k][:3]))
+                                                for k in common_s), default=0.0))
+        rep["sector_cos_max_err"] = float(max((abs(np.cos(np.float64(sm_r[k][3])) - np.cos(sm_o[k][3])) for k in common_s),
+                                              default=0.0))
+        rep["sector_max_err"] = max(rep["sector_axis_max_err"], rep["sector_cos_max_err"])
+        # complete circles
+        fr = canon.pair_set(ref["perm"], ref["full"])
+        fo = canon.pair_set(o["perm"], o["full"])
+        rep["full_mismatch"] = len(fr ^ fo)
+        rep["full_unexplained"] = len([c for c in fr ^ fo if c not in tainted])
+        # segments: per circle, the set of probe pairs
+        sg_r = canon.segment_set(ref["perm"], ref["segments"], rk)
+        sg_o = canon.segment_set(o["perm"], o["segments"], ok)
+        seg_bad = sg_r ^ sg_o
+        unexp = 0
+        for circle, pair in seg_bad:
+            if circle in tainted or any(p in bad_probes for p in pair):
+                continue
+            unexp += 1
+        rep["segment_mismatch"] = len(seg_bad)
+        rep["segment_unexplained"] = unexp
+        rep["segments_ref"] = len(ref["segments"])
+    else:
+        # tori per circle: compare where both sides have one
+        def tori_map(perm, cnt, rows, st_rows, tp, ta, tv):
+            out, q = {}, 0
+            for s in range(n):
+                for e in range(cnt[s]):
+                    if st_rows[s][e] == 2:
+                        out[frozenset((int(perm[s]), int(perm[rows[s][e]])))] = np.concatenate([tp[q], ta[q], tv[q]])
+                        q += 1
+            return out
+        srows_r2 = srows_r
+        srows_o2 = [o["status"][o["noff"][s]:o["noff"][s + 1]] for s in range(n)]
+        tm_r = tori_map(ref["perm"], ref["nbr_count"], rrows, srows_r2, ref["tori_pos"], ref["tori_axis"], ref["tori_vs"])
+        T = o["tori"]
+        tm_o = tori_map(o["perm"], ocnt, orows, srows_o2, T[:, 0:4], T[:, 4:8], T[:, 8:12])
+        rep["tori_mismatch"] = len(set(tm_r) ^ set(tm_o))
+        pc = set()
+        for key in bad_probes:
+            t = key[0]
+            pc |= {frozenset((t[0], t[1])), frozenset((t[0], t[2])), frozenset((t[1], t[2]))}
+        rep["tori_unexplained"] = len([c for c in set(tm_r) ^ set(tm_o) if c not in tainted and c not in pc
+                                       and c not in bad_pairs])
+        errs = [np.max(np.abs(np.asarray(tm_r[k], np.float64) - tm_o[k])) for k in set(tm_r) & set(tm_o)
+                if np.all(np.isfinite(tm_o[k])) and np.all(np.isfinite(tm_r[k]))]
+        rep["tori_max_err"] = float(max(errs, default=0.0))
+    return rep

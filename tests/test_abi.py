@@ -1,0 +1,53 @@
+"""The C-ABI library loads and exports every entry point include/sesgb.h declares (no GPU needed)."""
+import ctypes
+import os
+import re
+
+import pytest
+
+from sesdf_gb300 import _build, api
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    text = open(os.path.join(ROOT, "include", "sesgb.h")).read()
+    return sorted(set(re.findall(r"\b(sesgb_[a-z_0-9]+)\s*\(", text)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    _build.build_cuda()
+    return api.load_library()
+
+
+def test_header_lists_the_binding(lib):
+    assert set(declared_functions()) == set(api.EXPORTS)
+
+
+def test_every_declared_symbol_is_exported(lib):
+    missing = [f for f in declared_functions() if not hasattr(lib, f)]
+    assert not missing, missing
+
+
+def test_error_strings(lib):
+    assert lib.sesgb_error_string(0) == b"ok"
+    assert lib.sesgb_error_string(-3) == b"capacity overflow"
+    assert lib.sesgb_error_string(-99) == b"unknown status"
+    assert lib.sesgb_last_error(None) == b"no context"
+
+
+def test_invalid_arguments_are_rejected_without_a_gpu(lib):
+    h = ctypes.c_void_p()
+    # bad mode / missing output pointer: rejected before any CUDA call
+    assert lib.sesgb_create(None, 0, None, ctypes.c_float(1.4), 7, None, ctypes.byref(h)) == -1
+    assert lib.sesgb_create(None, 0, None, ctypes.c_float(1.4), 0, None, None) == -1
+    assert lib.sesgb_build(None, None) == -1
+    assert lib.sesgb_get_counts(None, None) == -1
+
+
+def test_cpp_dropin_symbols(lib):
+    # bcs::Sesdf / bcs::Ssesdf are compiled into the same library
+    for sym in ("_ZN3bcs5Sesdf5buildEv", "_ZN3bcs6Ssesdf5buildEv", "_ZN3bcs5Sesdf7getDataEv",
+                "_ZN3bcs6Ssesdf7getDataEv", "_ZN3bcs5Sesdf14getAtomIndicesEv"):
+        assert hasattr(lib, sym), sym

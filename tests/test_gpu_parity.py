@@ -1,0 +1,158 @@
+"""Parity of the GPU build (through the C ABI) with the FP64 oracle.
+
+Topology (neighbour lists, statuses, circles, probes, segments, singular
+neighbours) must be identical; probe positions are compared bit for bit (both
+sides solve in double precision with the same operations and round to float32);
+sectors and tori, which the GPU computes in float32, within 1e-4 A (rad).
+"""
+import numpy as np
+import pytest
+
+import canon
+from cases import hand_cases
+from oracle import oracle
+from sesdf_gb300 import SesBuild, synth
+
+pytestmark = pytest.mark.gpu
+RP = 1.4
+GEOM_TOL = 1e-4  # A (and rad for sector angles)
+
+
+def run_both(atoms, mode, rp=RP):
+    with SesBuild(atoms, rp, mode) as g:
+        g.build()
+        out = g.fetch()
+    o = oracle.run(atoms, rp, mode)
+    return out, o
+
+
+def compare(atoms, out, o, mode):
+    n = atoms.shape[0]
+    c = out["counts"]
+    assert c["atoms"] == n
+    assert c["truncated_atoms"] == 0
+    assert c["outside_atoms"] == 0
+    # stable reference-grid order: same permutation
+    assert np.array_equal(out["perm"], o["perm"]), "sorted order differs"
+    assert np.array_equal(out["atoms"], o["atoms"])
+    # neighbour lists and statuses, slot for slot
+    cnt = np.diff(o["noff"])
+    assert np.array_equal(out["nbr_count"], cnt)
+    for i in range(n):
+        row = o["nbr"][o["noff"][i]:o["noff"][i + 1]]
+        assert np.array_equal(out["nbr_ids"][i, :cnt[i]], row), f"neighbours of {i}"
+        assert np.array_equal(out["status"][i, :cnt[i]], o["status"][o["noff"][i]:o["noff"][i + 1]]), f"status of {i}"
+    assert c["pairs"] == len(o["nbr"])
+    assert c["partial_circles"] == len(o["trim_slot"])
+    # probes: ids, positions (bit for bit), singular partition
+    assert c["probes"] == len(o["ids"]) and c["singular_probes"] == o["Q"]
+    assert np.array_equal(out["probe_ids"][:, :3], o["ids"][:, :3])
+    assert np.array_equal(out["probe_ids"][:, 3], o["ids"][:, 3]), "singular neighbour counts"
+    assert np.array_equal(out["probe_pos"], o["posf"])
+    # singular neighbours: same sets (list order follows the reference-grid hash)
+    Q = o["Q"]
+    gn = out["probe_nbrs"].reshape(Q, 32, 4)
+    on = o["snbr"].reshape(Q, 32, 4)
+    for q in range(Q):
+        k = o["ids"][q, 3]
+        a = sorted(map(tuple, gn[q, :k].tolist()))
+        b = sorted(map(tuple, on[q, :k].tolist()))
+        assert a == b, f"neighbours of singular probe {q}"
+    if mode == "full":
+        assert np.array_equal(out["full"], o["full"])
+        assert np.array_equal(out["convex"], o["convex"])
+        assert out["sectors"].shape == o["sectors"].shape
+        if len(o["sectors"]):
+            sg = out["sectors"].astype(np.float64)
+            assert np.max(np.abs(sg[:, :3] - o["sectors"][:, :3])) < GEOM_TOL
+            # the half angle through its cosine (ill-conditioned next to 0 and pi)
+            assert np.max(np.abs(np.cos(sg[:, 3]) - np.cos(o["sectors"][:, 3]))) < GEOM_TOL
+        assert np.array_equal(out["segments"], o["segments"])
+        g2t = out["global_to_trimmed"]
+        cap = out["nbr_ids"].shape[1]
+        for i in range(n):
+            assert np.array_equal(g2t[i * cap:i * cap + cnt[i]], o["slot_trim"][o["noff"][i]:o["noff"][i + 1]])
+    else:
+        T = o["tori"].shape[0]
+        assert c["tori"] == T
+        if T:
+            tor = np.concatenate([out["tori_pos"], out["tori_axis"], out["tori_vs"]], axis=1).astype(np.float64)
+            ok = np.isfinite(o["tori"]).all(axis=1)  # the reference's NaN for axes parallel to z
+            assert np.max(np.abs(tor[ok] - o["tori"][ok])) < GEOM_TOL
+
+
+@pytest.mark.parametrize("name", sorted(hand_cases().keys()))
+@pytest.mark.parametrize("mode", ["full", "exterior"])
+def test_hand_cases(name, mode):
+    atoms = hand_cases()[name]
+    out, o = run_both(atoms, mode)
+    compare(atoms, out, o, mode)
+
+
+@pytest.mark.parametrize("mode", ["full", "exterior"])
+def test_globule_2k(mode):
+    atoms = synth.globule(2000, 1000)
+    out, o = run_both(atoms, mode)
+    compare(atoms, out, o, mode)
+
+
+@pytest.mark.parametrize("mode", ["full", "exterior"])
+def test_globule_20k(mode):
+    atoms = synth.globule(20000, 1500)
+    out, o = run_both(atoms, mode)
+    compare(atoms, out, o, mode)
+
+
+def test_probe_radius_24():
+    # the reference's second benchmark configuration (probe 2.4 A, 288 slots,
+    # sesdf/CMakeLists.txt:96-117)
+    atoms = synth.globule(2000, 1001)
+    with SesBuild(atoms, 2.4, "full", max_neighbor_per_atom=288) as g:
+        g.build()
+        out = g.fetch()
+    o = oracle.run(atoms, 2.4, "full", max_nbr=288)
+    compare(atoms, out, o, "full")
+
+
+@pytest.mark.slow
+@pytest.mark.parametrize("mode", ["full", "exterior"])
+def test_assembly_100k(mode):
+    atoms = synth.assembly()
+    out, o = run_both(atoms, mode)
+    compare(atoms, out, o, mode)
+
+
+def test_repeated_builds_are_identical():
+    atoms = synth.globule(3000, 77)
+    with SesBuild(atoms, RP, "full") as g:
+        g.build()
+        a = g.fetch()
+        g.build()
+        b = g.fetch()
+    for k in ("perm", "nbr_count", "probe_pos", "probe_ids", "segments", "sectors", "full"):
+        assert np.array_equal(a[k], b[k]), k
+
+
+def test_graph_replay_matches():
+    atoms = synth.globule(3000, 78)
+    with SesBuild(atoms, RP, "full") as g:
+        g.build()
+        a = g.fetch()
+    with SesBuild(atoms, RP, "full", graph=True) as g:
+        for _ in range(3):
+            g.build()
+        b = g.fetch()
+    for k in ("perm", "probe_pos", "probe_ids", "segments", "sectors"):
+        assert np.array_equal(a[k], b[k]), k
+
+
+def test_set_atoms_moves_surface():
+    base = synth.globule(2000, 1000)
+    moved = synth.jitter(base, 0.3, 5)
+    with SesBuild(base, RP, "full") as g:
+        g.build()
+        g.set_atoms(moved)
+        g.build()
+        out = g.fetch()
+    o = oracle.run(moved, RP, "full", box=g.box)
+    compare(moved, out, o, "full")
