@@ -44,6 +44,8 @@ typedef struct sesgb_options
 
 /* Capture the build in a CUDA graph after its first run and replay it. */
 #define SESGB_FLAG_GRAPH 1u
+/* Record CUDA events between the stages of each build (see sesgb_stage_times). */
+#define SESGB_FLAG_PROFILE 2u
 
 /* Output buffers of the full-surface build: field for field the reference's
  * bcs::sesdf::SesdfData (sesdf/include/bcs/sesdf/graphics.hpp:39-66). Device pointers,
@@ -114,7 +116,8 @@ typedef struct sesgb_counts
     uint32_t truncated_probe_neighbors; /* singular probes with more than 32 neighbours */
     uint32_t degenerate_tori; /* torus axes parallel to z (the reference produces NaN there) */
     uint32_t outside_atoms;  /* atoms outside the grid box given at creation */
-    uint32_t fp64_decisions[ 4 ]; /* predicates settled in double precision: neighbour, visibility, occlusion, probe neighbour */
+    uint32_t fp64_decisions[ 5 ]; /* settled in double precision: neighbour, visibility and occlusion predicates,
+                                     probe-neighbour distances, probe candidates re-solved after a float32 band hit */
     uint32_t rebuilds;       /* capacity regrowths of the last build */
 } sesgb_counts;
 
@@ -141,6 +144,14 @@ int sesgb_build( sesgb_ctx * ctx, void * stream );
 /* Same build from atoms already in device memory (float4[n]). */
 int sesgb_build_device( sesgb_ctx * ctx, const void * device_atoms, void * stream );
 
+/* Asynchronous form of sesgb_build / sesgb_build_device: enqueues the whole
+ * build on `stream` (device_atoms NULL = upload the borrowed host atoms) and
+ * returns; sesgb_finish waits for it, and if a count exceeded a buffer's
+ * capacity, regrows the buffer and builds again before returning. Results are
+ * valid after sesgb_finish. */
+int sesgb_build_async( sesgb_ctx * ctx, const void * device_atoms, void * stream );
+int sesgb_finish( sesgb_ctx * ctx );
+
 /* Replaces the borrowed host atom pointer (same atom count). */
 int sesgb_set_host_atoms( sesgb_ctx * ctx, const float * atoms );
 
@@ -165,6 +176,15 @@ int sesgb_copy_to_host( sesgb_ctx * ctx, const void * device_ptr, void * host, u
 uint16_t sesgb_max_neighbor_per_atom( const sesgb_ctx * ctx );
 uint16_t sesgb_max_intersections_per_circle( const sesgb_ctx * ctx );
 uint16_t sesgb_max_intersection_neighbors( const sesgb_ctx * ctx );
+
+/* Per-stage milliseconds of the last build (SESGB_FLAG_PROFILE): writes up to
+ * `capacity` values and the number of stages; stage names by sesgb_stage_name.
+ * The per-stage timers mirror app/detailed/sesdf_benchmark.inl of the reference. */
+int          sesgb_stage_times( sesgb_ctx * ctx, float * ms, uint32_t capacity, uint32_t * count );
+const char * sesgb_stage_name( uint32_t stage );
+
+/* Number of kernels this library has launched in this process (host-side count). */
+uint64_t sesgb_launch_count( void );
 
 const char * sesgb_error_string( int status );
 const char * sesgb_last_error( const sesgb_ctx * ctx );

@@ -77,7 +77,8 @@ static inline double dot( v3 a, v3 b ) { return a.x * b.x + a.y * b.y + a.z * b.
 static inline v3 cross( v3 a, v3 b ) { return mk( a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x ); }
 /* helper_math.h normalize: v * rsqrt(dot(v, v)); restated as v * (1 / sqrt(dot)) */
 static inline v3 nrm( v3 v ) { return mul( v, 1.0 / sqrt( dot( v, v ) ) ); }
-static inline double clampd( double x, double lo, double hi ) { return x < lo ? lo : ( x > hi ? hi : x ); }
+/* helper_math.h clamp: fmaxf(a, fminf(f, b)) (a NaN argument yields b) */
+static inline double clampd( double x, double lo, double hi ) { return fmax( lo, fmin( x, hi ) ); }
 
 typedef struct
 {

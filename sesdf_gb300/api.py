@@ -19,6 +19,7 @@ from . import _build
 MODE_FULL = 0
 MODE_EXTERIOR = 1
 FLAG_GRAPH = 1
+FLAG_PROFILE = 2
 
 BUF_ATOM_INDICES, BUF_NEIGHBOR_COUNT, BUF_NEIGHBOR_IDS, BUF_VISIBILITY_STATUS, BUF_GLOBAL_TO_TRIMMED = range(5)
 
@@ -27,7 +28,8 @@ EXPORTS = [
     "sesgb_create", "sesgb_build", "sesgb_build_device", "sesgb_set_host_atoms", "sesgb_get_full",
     "sesgb_get_exterior", "sesgb_get_counts", "sesgb_atom_indices", "sesgb_analysis_buffer", "sesgb_copy_to_host",
     "sesgb_max_neighbor_per_atom", "sesgb_max_intersections_per_circle", "sesgb_max_intersection_neighbors",
-    "sesgb_error_string", "sesgb_last_error", "sesgb_destroy",
+    "sesgb_error_string", "sesgb_last_error", "sesgb_destroy", "sesgb_stage_times", "sesgb_stage_name",
+    "sesgb_launch_count", "sesgb_build_async", "sesgb_finish",
 ]
 
 
@@ -66,7 +68,7 @@ COUNT_FIELDS = ["atoms", "pairs", "sectors", "full_circles", "partial_circles", 
 
 
 class Counts(ctypes.Structure):
-    _fields_ = [(f, ctypes.c_uint32) for f in COUNT_FIELDS] + [("fp64_decisions", ctypes.c_uint32 * 4),
+    _fields_ = [(f, ctypes.c_uint32) for f in COUNT_FIELDS] + [("fp64_decisions", ctypes.c_uint32 * 5),
                                                                ("rebuilds", ctypes.c_uint32)]
 
 
@@ -104,8 +106,20 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         lib.sesgb_last_error.restype = ctypes.c_char_p
         lib.sesgb_destroy.argtypes = [P]
         lib.sesgb_destroy.restype = None
+        lib.sesgb_stage_times.argtypes = [P, P, U32, ctypes.POINTER(U32)]
+        lib.sesgb_stage_name.argtypes = [U32]
+        lib.sesgb_stage_name.restype = ctypes.c_char_p
+        lib.sesgb_build_async.argtypes = [P, P, P]
+        lib.sesgb_finish.argtypes = [P]
+        lib.sesgb_launch_count.argtypes = []
+        lib.sesgb_launch_count.restype = ctypes.c_uint64
         _lib = lib
     return _lib
+
+
+def launch_count() -> int:
+    """Kernels launched by the library in this process."""
+    return int(load_library().sesgb_launch_count())
 
 
 def aabb(atoms: np.ndarray) -> np.ndarray:
@@ -123,14 +137,15 @@ class SesBuild:
 
     def __init__(self, atoms: np.ndarray, probe_radius: float = 1.4, mode: str = "full", box=None,
                  max_neighbor_per_atom: int = 0, max_intersections_per_circle: int = 0, graph: bool = False,
-                 device: int = -1):
+                 device: int = -1, profile: bool = False):
         self._lib = load_library()
         self.atoms = np.ascontiguousarray(np.asarray(atoms, np.float32).reshape(-1, 4))
         self.mode = mode
         self.probe_radius = float(probe_radius)
         bx = None if box is None else np.ascontiguousarray(box, np.float32)
         self.box = aabb(self.atoms) if bx is None else bx
-        opt = Options(max_neighbor_per_atom, max_intersections_per_circle, device, FLAG_GRAPH if graph else 0)
+        flags = (FLAG_GRAPH if graph else 0) | (FLAG_PROFILE if profile else 0)
+        opt = Options(max_neighbor_per_atom, max_intersections_per_circle, device, flags)
         h = ctypes.c_void_p()
         st = self._lib.sesgb_create(self.atoms.ctypes.data if self.atoms.size else None, self.atoms.shape[0],
                                     self.box.ctypes.data, ctypes.c_float(probe_radius),
@@ -156,6 +171,17 @@ class SesBuild:
 
     def build_device(self, device_ptr: int, stream: int | None = None):
         self._check(self._lib.sesgb_build_device(self._h, device_ptr, stream), "build_device")
+
+    def build_async(self, device_ptr: int | None = None, stream: int | None = None):
+        """Enqueues a build (device atoms, or the host atoms when None); finish() waits."""
+        self._check(self._lib.sesgb_build_async(self._h, device_ptr, stream), "build_async")
+
+    def finish(self):
+        self._check(self._lib.sesgb_finish(self._h), "finish")
+
+    def set_host_pointer(self, ptr: int):
+        """Reads atoms from raw host memory (e.g. pinned) from now on; caller keeps it alive."""
+        self._check(self._lib.sesgb_set_host_atoms(self._h, ptr), "set_host_pointer")
 
     def counts(self) -> dict:
         c = Counts()
@@ -187,6 +213,13 @@ class SesBuild:
         n = nb.value // np.dtype(dtype).itemsize
         return self._copy(p, n, dtype)
 
+    def stage_times(self) -> dict:
+        """Milliseconds per stage of the last build (needs profile=True)."""
+        ms = (ctypes.c_float * 16)()
+        n = ctypes.c_uint32()
+        self._check(self._lib.sesgb_stage_times(self._h, ms, 16, ctypes.byref(n)), "stage_times")
+        return {self._lib.sesgb_stage_name(k).decode(): float(ms[k]) for k in range(n.value)}
+
     @property
     def max_neighbor_per_atom(self) -> int:
         return int(self._lib.sesgb_max_neighbor_per_atom(self._h))
@@ -212,9 +245,10 @@ class SesBuild:
         if analysis:
             out["perm"] = self.analysis(BUF_ATOM_INDICES, np.uint32)
             out["nbr_count"] = self.analysis(BUF_NEIGHBOR_COUNT, np.uint32)
-            out["nbr_ids"] = self.analysis(BUF_NEIGHBOR_IDS, np.uint32).reshape(d.atomNb, -1)
+            cap = self.max_neighbor_per_atom
+            out["nbr_ids"] = self.analysis(BUF_NEIGHBOR_IDS, np.uint32)[: d.atomNb * cap].reshape(d.atomNb, cap)
             st = self.analysis(BUF_VISIBILITY_STATUS, np.uint8)
-            out["status"] = st[: d.atomNb * self.max_neighbor_per_atom].reshape(d.atomNb, -1)
+            out["status"] = st[: d.atomNb * cap].reshape(d.atomNb, cap)
             if self.mode == "full":
                 out["global_to_trimmed"] = self.analysis(BUF_GLOBAL_TO_TRIMMED, np.uint32)
         return out

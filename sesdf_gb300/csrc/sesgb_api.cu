@@ -43,11 +43,21 @@ struct sesgb_ctx
     uint32_t            rebuilds = 0;
     std::string         err;
 
+    // per-stage events (SESGB_FLAG_PROFILE)
+    static constexpr int kStages = 10;
+    cudaEvent_t          ev[ kStages + 1 ] {};
+    float                stageMs[ kStages ] {};
+    bool                 profiled = false;
+
     // graph replay
     cudaGraph_t     graph = nullptr;
     cudaGraphExec_t graphExec = nullptr;
-    cudaStream_t    graphStream = nullptr;
-    const void *    graphAtoms = nullptr;
+    bool            lastUsedGraph = false;
+
+    // build in flight (sesgb_build_async .. sesgb_finish)
+    cudaStream_t pendingStream = nullptr;
+    bool         pendingUpload = false;
+    const void * pendingAtoms  = nullptr;
 };
 
 namespace
@@ -152,7 +162,9 @@ namespace
         b.nbrCount        = dalloc<uint32_t>( c, L, n + 1, ok );
         b.status          = dalloc<uint8_t>( c, L, n * b.cap + 1, ok );
         b.slotTrim        = dalloc<uint32_t>( c, L, n * b.cap, ok );
-        uint32_t ** per[] = { &b.visCnt, &b.partCnt, &b.fullCnt, &b.torCnt, &b.visOff, &b.partOff, &b.fullOff, &b.torOff };
+        uint32_t ** per[] = { &b.visCnt,  &b.partCnt, &b.fullCnt, &b.torCnt,  &b.visOff,    &b.partOff, &b.fullOff,
+                              &b.torOff,  &b.singCnt, &b.regCnt,  &b.singOff, &b.regOff,    &b.chunkStart,
+                              &b.chunkLen };
         for ( uint32_t ** p : per )
             *p = dalloc<uint32_t>( c, L, n + 1, ok );
         b.convex = dalloc<uint2>( c, L, n, ok );
@@ -174,17 +186,14 @@ namespace
         Build &      b  = c->b;
         bool         ok = true;
         auto &       L  = c->dynAllocs;
-        const size_t C1 = b.capC1, CC = b.capCand, PR = b.capProbes;
+        const size_t C1 = b.capC1, PR = b.capProbes;
         b.sectors     = dalloc<float4>( c, L, b.capSectors, ok );
         b.fullCircles = dalloc<uint2>( c, L, b.capFull, ok );
         b.trimSlot    = dalloc<uint32_t>( c, L, C1, ok );
-        b.candCnt     = dalloc<uint32_t>( c, L, C1 + 1, ok );
-        b.candOff     = dalloc<uint32_t>( c, L, C1 + 1, ok );
-        b.cand        = dalloc<uint4>( c, L, CC, ok );
-        b.isSing      = dalloc<uint32_t>( c, L, 2 * CC + 1, ok );
-        b.isReg       = dalloc<uint32_t>( c, L, 2 * CC + 1, ok );
-        b.slotPos     = dalloc<float4>( c, L, 2 * CC, ok );
-        b.slotCid     = dalloc<int4>( c, L, 2 * CC, ok );
+        b.stagePos    = dalloc<float4>( c, L, PR, ok );
+        b.stageCid    = dalloc<int4>( c, L, PR, ok );
+        b.stageIds    = dalloc<int4>( c, L, PR, ok );
+        b.jobs        = dalloc<uint4>( c, L, PR, ok );
         b.probeIds    = dalloc<int4>( c, L, PR, ok );
         b.probePos    = dalloc<float4>( c, L, PR, ok );
         b.probeCid    = dalloc<int4>( c, L, PR, ok );
@@ -202,7 +211,7 @@ namespace
         const size_t items = std::max<size_t>( c->n, PR );
         b.cellItems = dalloc<uint32_t>( c, L, items, ok );
         b.cellPos   = dalloc<float4>( c, L, items, ok );
-        const uint64_t scanMax = std::max<uint64_t>( { (uint64_t)c->n + 1, C1 + 1, 2 * CC + 1, (uint64_t)b.capCells + 1 } );
+        const uint64_t scanMax = std::max<uint64_t>( { (uint64_t)c->n + 1, C1 + 1, (uint64_t)b.capCells + 1 } );
         c->scanScratchBytes    = scan_scratch_bytes( scanMax );
         c->scanScratch         = dalloc<char>( c, L, c->scanScratchBytes, ok );
         return ok;
@@ -218,27 +227,38 @@ namespace
         c->graph     = nullptr;
     }
 
+    const char * kStageNames[] = { "grid", "neighbors", "visibility", "circles", "probes",
+                                   "place", "", "segments", "probe_neighbors", "tori" };
+
     // all launches of one build; no host synchronisation inside
-    void enqueue( sesgb_ctx * c, cudaStream_t s )
+    void enqueue( sesgb_ctx * c, cudaStream_t s, bool profile )
     {
         Build &     b    = c->b;
         const auto  n    = c->n;
         void *      sc   = c->scanScratch;
         DeviceCounts * d = b.counts;
+        auto mark = [ & ]( int k ) {
+            if ( profile )
+                cudaEventRecord( c->ev[ k ], s );
+        };
         cudaMemsetAsync( d, 0, sizeof( DeviceCounts ), s );
         if ( n == 0 )
             return;
 
         // A: reference-grid order, neighbour grid, neighbour lists
+        mark( 0 );
         launch_hash( b, s );
         radix_sort( b.keys, b.perm, n, c->gridBits, c->radixScratch, s );
         launch_fine_params( b, -1.f, n, s );
         launch_gather( b, s );
         launch_cells( b, b.atoms, n, nullptr, sc, s );
+        mark( 1 );
         launch_neighbors( b, s );
 
         // B, C: visibility, sectors, complete and partial circles
+        mark( 2 );
         launch_visibility( b, s );
+        mark( 3 );
         exclusive_scan( b.visCnt, b.visOff, n, nullptr, &d->V, sc, s );
         exclusive_scan( b.partCnt, b.partOff, n, nullptr, &d->C1, sc, s );
         exclusive_scan( b.fullCnt, b.fullOff, n, nullptr, &d->F, sc, s );
@@ -246,14 +266,16 @@ namespace
         launch_emit( b, s );
 
         // D, E: probes
-        launch_candidates( b, false, s );
-        exclusive_scan( b.candCnt, b.candOff, b.capC1, &d->C1, &d->cand, sc, s );
-        launch_candidates( b, true, s );
-        launch_triplets( b, s );
-        exclusive_scan( b.isSing, b.isSing, 2ull * b.capCand, &d->probeSlots, &d->Q, sc, s );
-        exclusive_scan( b.isReg, b.isReg, 2ull * b.capCand, &d->probeSlots, &d->regTotal, sc, s );
+        mark( 4 );
+        launch_probes( b, s );
+        launch_probe_jobs( b, s );
+        mark( 5 );
+        exclusive_scan( b.singCnt, b.singOff, n, nullptr, &d->Q, sc, s );
+        exclusive_scan( b.regCnt, b.regOff, n, nullptr, &d->regTotal, sc, s );
         cudaMemsetAsync( b.ccount, 0, sizeof( uint32_t ) * ( b.capC1 + 1ull ), s );
         launch_place( b, s );
+        mark( 6 );
+        mark( 7 );
 
         // F: segments
         if ( c->mode == SESGB_MODE_FULL )
@@ -267,17 +289,20 @@ namespace
         }
 
         // G: neighbours of singular probes
+        mark( 8 );
         launch_fine_params( b, 2.f * c->rp + 0.01f, 0, s );
         launch_cells( b, b.probePos, b.capProbes, &d->Q, sc, s );
         launch_probe_neighbors( b, s );
 
         // H: exterior tori
+        mark( 9 );
         if ( c->mode == SESGB_MODE_EXTERIOR )
         {
             launch_tori( b, s );
             exclusive_scan( b.torCnt, b.torOff, n, nullptr, &d->T, sc, s );
             launch_tori_emit( b, s );
         }
+        mark( 10 );
     }
 
     // regrows the buffers whose counts exceeded their capacity; true if any
@@ -296,7 +321,7 @@ namespace
         fix( b.capSectors, h.V );
         fix( b.capFull, h.F );
         fix( b.capC1, h.C1 );
-        fix( b.capCand, h.cand );
+        fix( b.capProbes, h.staged );
         fix( b.capProbes, h.I );
         fix( b.capSeg, h.S );
         fix( b.capTori, h.T );
@@ -310,61 +335,86 @@ namespace
         return g;
     }
 
-    int run_build( sesgb_ctx * c, cudaStream_t s, bool upload, const void * deviceAtoms )
+    // enqueues one build (upload, kernels, counter read-back) without waiting
+    int enqueue_build( sesgb_ctx * c, cudaStream_t s, bool upload, const void * deviceAtoms )
     {
+        if ( upload && c->n )
+        {
+            if ( !c->hostAtoms )
+            {
+                c->err = "no host atoms";
+                return SESGB_ERR_INVALID;
+            }
+            if ( !cuda_ok( c, cudaMemcpyAsync( c->b.atomsIn, c->hostAtoms, sizeof( float4 ) * c->n, cudaMemcpyHostToDevice, s ),
+                           "upload" ) )
+                return SESGB_ERR_CUDA;
+        }
+        else if ( deviceAtoms && c->n )
+        {
+            if ( !cuda_ok( c, cudaMemcpyAsync( c->b.atomsIn, deviceAtoms, sizeof( float4 ) * c->n, cudaMemcpyDeviceToDevice, s ),
+                           "copy" ) )
+                return SESGB_ERR_CUDA;
+        }
+        c->pendingStream = s;
+        c->pendingUpload = upload;
+        c->pendingAtoms  = deviceAtoms;
+        const bool useGraph = ( c->flags & SESGB_FLAG_GRAPH ) && c->built;
+        c->lastUsedGraph    = useGraph;
+        if ( useGraph )
+        {
+            if ( !c->graphExec )
+            {
+                cudaStream_t cap;
+                if ( !cuda_ok( c, cudaStreamCreateWithFlags( &cap, cudaStreamNonBlocking ), "stream" ) )
+                    return SESGB_ERR_CUDA;
+                cudaStreamBeginCapture( cap, cudaStreamCaptureModeThreadLocal );
+                enqueue( c, cap, false );
+                cudaMemcpyAsync( c->hCounts, c->b.counts, sizeof( DeviceCounts ), cudaMemcpyDeviceToHost, cap );
+                const cudaError_t e = cudaStreamEndCapture( cap, &c->graph );
+                cudaStreamDestroy( cap );
+                if ( !cuda_ok( c, e, "capture" ) )
+                    return SESGB_ERR_CUDA;
+                if ( !cuda_ok( c, cudaGraphInstantiate( &c->graphExec, c->graph, 0 ), "instantiate" ) )
+                    return SESGB_ERR_CUDA;
+            }
+            if ( !cuda_ok( c, cudaGraphLaunch( c->graphExec, s ), "graph launch" ) )
+                return SESGB_ERR_CUDA;
+            c->profiled = false;
+        }
+        else
+        {
+            const bool profile = ( c->flags & SESGB_FLAG_PROFILE ) && c->n;
+            if ( profile && !c->ev[ 0 ] )
+                for ( auto & e : c->ev )
+                    cudaEventCreate( &e );
+            enqueue( c, s, profile );
+            cudaMemcpyAsync( c->hCounts, c->b.counts, sizeof( DeviceCounts ), cudaMemcpyDeviceToHost, s );
+            c->profiled = profile;
+        }
+        return cuda_ok( c, cudaGetLastError(), "launch" ) ? SESGB_OK : SESGB_ERR_CUDA;
+    }
+
+    bool counts_fit( const sesgb_ctx * c )
+    {
+        const DeviceCounts & h = *c->hCounts;
+        const Build &        b = c->b;
+        return ( h.overflow & ~(uint32_t)kOverflowNbr ) == 0 && h.V <= b.capSectors && h.F <= b.capFull && h.C1 <= b.capC1
+               && h.staged <= b.capProbes && h.I <= b.capProbes && h.S <= b.capSeg && h.T <= b.capTori;
+    }
+
+    // waits for the enqueued build; on a capacity overflow regrows and builds again
+    int finish_build( sesgb_ctx * c )
+    {
+        cudaStream_t s = c->pendingStream;
         for ( int attempt = 0; attempt < 6; attempt++ )
         {
-            if ( upload && c->n )
-            {
-                if ( !c->hostAtoms )
-                {
-                    c->err = "no host atoms";
-                    return SESGB_ERR_INVALID;
-                }
-                if ( !cuda_ok( c, cudaMemcpyAsync( c->b.atomsIn, c->hostAtoms, sizeof( float4 ) * c->n, cudaMemcpyHostToDevice, s ),
-                               "upload" ) )
-                    return SESGB_ERR_CUDA;
-            }
-            else if ( deviceAtoms && c->n )
-            {
-                if ( !cuda_ok( c, cudaMemcpyAsync( c->b.atomsIn, deviceAtoms, sizeof( float4 ) * c->n, cudaMemcpyDeviceToDevice, s ),
-                               "copy" ) )
-                    return SESGB_ERR_CUDA;
-            }
-            const bool useGraph = ( c->flags & SESGB_FLAG_GRAPH ) && c->built;
-            if ( useGraph )
-            {
-                if ( !c->graphExec )
-                {
-                    cudaStream_t cap;
-                    if ( !cuda_ok( c, cudaStreamCreateWithFlags( &cap, cudaStreamNonBlocking ), "stream" ) )
-                        return SESGB_ERR_CUDA;
-                    cudaStreamBeginCapture( cap, cudaStreamCaptureModeThreadLocal );
-                    enqueue( c, cap );
-                    cudaMemcpyAsync( c->hCounts, c->b.counts, sizeof( DeviceCounts ), cudaMemcpyDeviceToHost, cap );
-                    const cudaError_t e = cudaStreamEndCapture( cap, &c->graph );
-                    cudaStreamDestroy( cap );
-                    if ( !cuda_ok( c, e, "capture" ) )
-                        return SESGB_ERR_CUDA;
-                    if ( !cuda_ok( c, cudaGraphInstantiate( &c->graphExec, c->graph, 0 ), "instantiate" ) )
-                        return SESGB_ERR_CUDA;
-                }
-                if ( !cuda_ok( c, cudaGraphLaunch( c->graphExec, s ), "graph launch" ) )
-                    return SESGB_ERR_CUDA;
-            }
-            else
-            {
-                enqueue( c, s );
-                cudaMemcpyAsync( c->hCounts, c->b.counts, sizeof( DeviceCounts ), cudaMemcpyDeviceToHost, s );
-            }
             if ( !cuda_ok( c, cudaStreamSynchronize( s ), "build" ) )
                 return SESGB_ERR_CUDA;
-            if ( !cuda_ok( c, cudaGetLastError(), "launch" ) )
-                return SESGB_ERR_CUDA;
+            if ( c->profiled )
+                for ( int k = 0; k < sesgb_ctx::kStages; k++ )
+                    cudaEventElapsedTime( &c->stageMs[ k ], c->ev[ k ], c->ev[ k + 1 ] );
             const DeviceCounts & h = *c->hCounts;
-            if ( ( h.overflow & ~(uint32_t)kOverflowNbr ) == 0 && h.V <= c->b.capSectors && h.F <= c->b.capFull
-                 && h.C1 <= c->b.capC1 && h.cand <= c->b.capCand && h.I <= c->b.capProbes && h.S <= c->b.capSeg
-                 && h.T <= c->b.capTori )
+            if ( counts_fit( c ) )
             {
                 if ( h.overflow & kOverflowNbr )
                 {
@@ -374,9 +424,14 @@ namespace
                 c->built = true;
                 return SESGB_OK;
             }
-            if ( ( h.overflow & kOverflowList ) && !regrow( c ) )
+            if ( ( h.overflow & kOverflowList ) )
             {
                 c->err = "a circle carries more probes than the segment stage holds";
+                return SESGB_ERR_OVERFLOW;
+            }
+            if ( ( h.overflow & kOverflowAtomProbes ) )
+            {
+                c->err = "an atom owns more than 128 probes (the reference's per-atom limit as well)";
                 return SESGB_ERR_OVERFLOW;
             }
             regrow( c );
@@ -384,9 +439,18 @@ namespace
             c->rebuilds++;
             if ( !allocate_dynamic( c ) )
                 return SESGB_ERR_CUDA;
+            const int st = enqueue_build( c, s, c->pendingUpload, c->pendingAtoms );
+            if ( st != SESGB_OK )
+                return st;
         }
         c->err = "capacities still exceeded after regrowing";
         return SESGB_ERR_OVERFLOW;
+    }
+
+    int run_build( sesgb_ctx * c, cudaStream_t s, bool upload, const void * deviceAtoms )
+    {
+        const int st = enqueue_build( c, s, upload, deviceAtoms );
+        return st != SESGB_OK ? st : finish_build( c );
     }
 } // namespace
 
@@ -434,7 +498,6 @@ extern "C"
         b.capSectors = grow( 40ull * n );
         b.capFull    = grow( 4ull * n );
         b.capC1      = grow( 24ull * n );
-        b.capCand    = grow( 24ull * n );
         b.capProbes  = grow( 8ull * n );
         b.capSeg     = grow( 8ull * n );
         b.capTori    = grow( 16ull * n );
@@ -468,6 +531,20 @@ extern "C"
         if ( !c || ( c->n && !device_atoms ) )
             return SESGB_ERR_INVALID;
         return run_build( c, static_cast<cudaStream_t>( stream ), false, device_atoms );
+    }
+
+    int sesgb_build_async( sesgb_ctx * c, const void * device_atoms, void * stream )
+    {
+        if ( !c )
+            return SESGB_ERR_INVALID;
+        return enqueue_build( c, static_cast<cudaStream_t>( stream ), device_atoms == nullptr, device_atoms );
+    }
+
+    int sesgb_finish( sesgb_ctx * c )
+    {
+        if ( !c )
+            return SESGB_ERR_INVALID;
+        return finish_build( c );
     }
 
     int sesgb_get_full( sesgb_ctx * c, sesgb_full_data * o )
@@ -546,7 +623,7 @@ extern "C"
         o->truncated_probe_neighbors    = h.snbrTruncated;
         o->degenerate_tori              = h.torusDegenerate;
         o->outside_atoms                = h.outside;
-        for ( int k = 0; k < 4; k++ )
+        for ( int k = 0; k < 5; k++ )
             o->fp64_decisions[ k ] = h.fp64[ k ];
         o->rebuilds = c->rebuilds;
         return SESGB_OK;
@@ -611,6 +688,26 @@ extern "C"
     uint16_t sesgb_max_intersections_per_circle( const sesgb_ctx * c ) { return c ? (uint16_t)c->b.segCap : 0; }
     uint16_t sesgb_max_intersection_neighbors( const sesgb_ctx * ) { return (uint16_t)kMaxProbeNbr; }
 
+    int sesgb_stage_times( sesgb_ctx * c, float * ms, uint32_t capacity, uint32_t * count )
+    {
+        if ( !c || ( capacity && !ms ) )
+            return SESGB_ERR_INVALID;
+        if ( !c->profiled )
+            return SESGB_ERR_NOT_BUILT;
+        for ( uint32_t k = 0; k < capacity && k < (uint32_t)sesgb_ctx::kStages; k++ )
+            ms[ k ] = c->stageMs[ k ];
+        if ( count )
+            *count = sesgb_ctx::kStages;
+        return SESGB_OK;
+    }
+
+    const char * sesgb_stage_name( uint32_t stage )
+    {
+        return stage < (uint32_t)sesgb_ctx::kStages ? kStageNames[ stage ] : "";
+    }
+
+    uint64_t sesgb_launch_count( void ) { return launch_count(); }
+
     const char * sesgb_error_string( int status )
     {
         const int k = -status;
@@ -627,6 +724,9 @@ extern "C"
             return;
         cudaDeviceSynchronize();
         destroy_graph( c );
+        for ( auto & e : c->ev )
+            if ( e )
+                cudaEventDestroy( e );
         free_list( c->dynAllocs );
         free_list( c->fixedAllocs );
         if ( c->g2t )

@@ -120,7 +120,7 @@ namespace sesgb
     __device__ __forceinline__ double dpseudo_angle( d3 u, d3 v, d3 n )
     {
         double c = __ddiv_rn( ddot( u, v ), __dmul_rn( __dsqrt_rn( ddot( u, u ) ), __dsqrt_rn( ddot( v, v ) ) ) );
-        c        = c < -1.0 ? -1.0 : ( c > 1.0 ? 1.0 : c );
+        c        = fmax( -1.0, fmin( c, 1.0 ) );
         const double det = ddot( u, dcross( v, n ) );
         return copysign( 1.0, det ) > 0.0 ? __dsub_rn( 1.0, c ) : __dadd_rn( 3.0, c );
     }

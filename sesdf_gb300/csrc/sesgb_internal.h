@@ -30,9 +30,9 @@ namespace sesgb
         uint32_t fineCells;  // cells of the neighbour grid in use
         float    fineCell;   // edge of a neighbour-grid cell (A)
         float    rmax;       // largest vdW radius
-        uint32_t probeSlots; // 2 * candidates (probe slots scanned by the partition)
+        uint32_t staged;     // probes written to the staging chunks
         uint32_t regTotal;   // regular (non-singular) probes
-        uint32_t P2;         // scratch total
+        uint32_t jobs;       // double-precision probe jobs
         uint32_t pad[ 2 ];
     };
 
@@ -48,6 +48,7 @@ namespace sesgb
         kOverflowTori    = 1u << 7,
         kOverflowCells   = 1u << 8,
         kOverflowList    = 1u << 9,
+        kOverflowAtomProbes = 1u << 10, // an atom owns more probes than one warp holds (128)
     };
 
     enum Fp64Stage : uint32_t
@@ -56,6 +57,7 @@ namespace sesgb
         kFp64Visibility,
         kFp64Occlusion,
         kFp64SingularNbr,
+        kFp64Solve, // probe candidates whose float32 screen hit the band
         kFp64Count
     };
 
@@ -75,6 +77,9 @@ namespace sesgb
     // out[n] = total; *total (device) = total when non-null. in == out allowed.
     void exclusive_scan( const uint32_t * in, uint32_t * out, uint64_t nHost, const uint32_t * nDevice, uint32_t * total,
                          void * scratch, cudaStream_t stream );
+
+    // host-side count of kernel launches (sesgb_launch_count)
+    void count_launches( uint32_t k );
 
     size_t radix_scratch_bytes( uint32_t n );
     // stable LSD radix sort of (keys, vals) on the low `bits` bits; result in keys/vals

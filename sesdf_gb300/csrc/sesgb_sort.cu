@@ -232,6 +232,7 @@ namespace sesgb
         k_scan_tile_sums<<<1, 1024, 0, stream>>>( tileSums, tiles, total, out, nHost, nDevice );
         if ( tiles > 0 )
             k_tile_scan<<<tiles, kScanThreads, 0, stream>>>( in, out, nHost, nDevice, tileSums );
+        count_launches( tiles > 0 ? 3 : 1 );
     }
 
     size_t radix_scratch_bytes( uint32_t n )
@@ -266,6 +267,7 @@ namespace sesgb
             k_radix_hist<<<tiles, kRadixThreads, 0, stream>>>( ka, n, shift, histBuf, tiles );
             exclusive_scan( histBuf, histBuf, hist, nullptr, nullptr, scanScratch, stream );
             k_radix_scatter<<<tiles, kRadixThreads, 0, stream>>>( ka, va, kb, vb, n, shift, histBuf, tiles );
+            count_launches( 2 );
             std::swap( ka, kb );
             std::swap( va, vb );
         }

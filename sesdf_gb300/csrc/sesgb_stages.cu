@@ -19,6 +19,7 @@
 // magnitudes involved, about 30x the float32 error bound) it is decided by the
 // double-precision twin in sesgb_device.cuh, which evaluates the reference's
 // formula exactly as the FP64 oracle does.
+#include <atomic>
 #include <cfloat>
 
 #include "sesgb_stages.cuh"
@@ -276,8 +277,13 @@ namespace sesgb
             const float  d  = dot( dj, dj );
             const float  t  = ( Ri * Ri - Rj * Rj + d ) / ( 2.f * d );
             const f3     c  = dj * t;
-            const float  r2 = fmaxf( Ri * Ri - dot( c, c ), 0.f );
+            const float  r2raw = Ri * Ri - dot( c, c );
+            const float  r2 = fmaxf( r2raw, 0.f );
             const f3     nr = dj * rsqrtf( d );
+            // (nearly) tangent SAS spheres: the reference's circle radius is
+            // sqrt of a negative number (NaN) and every test of the circle is
+            // false; the double-precision twin decides whether that happens
+            const bool   tangent = r2raw <= 4.f * kRel * Ri * Ri;
 
             bool    buried = false, touched = false, haveD = false;
             dcircle dc;
@@ -301,7 +307,7 @@ namespace sesgb
                 // divides by |v| and takes sqrt(1 - cos^2), which yields NaN (k
                 // ignored) exactly when |v| = 0 or |cos| > 1 in its arithmetic;
                 // only the double-precision twin reproduces that
-                if ( vv <= eA || p2 <= kRel * ( vv + 1.f ) )
+                if ( tangent || vv <= eA || p2 <= kRel * ( vv + 1.f ) )
                     decided = false;
                 else if ( A < -eA )
                 {
@@ -410,7 +416,7 @@ namespace sesgb
                 ref = F3( 0.f, 1.f, 0.f );
             const f3    nn = normalize( cross( cicj, ref ) );
             const f3    x  = cij + nn * radius;
-            const float c  = fminf( fmaxf( dot( cicj, x * ( 1.f / rirp ) ), -1.f ), 1.f );
+            const float c  = fmaxf( -1.f, fminf( dot( cicj, x * ( 1.f / rirp ) ), 1.f ) );
             return make_float4( cicj.x, cicj.y, cicj.z, acosf( c ) );
         }
 
@@ -481,7 +487,7 @@ namespace sesgb
                 atomicOr( &b.counts->overflow, ovf );
         }
 
-        // ---- probe candidates ------------------------------------------------
+        // ---- probes: enumeration, float32 screen, double-precision solve -------
         __device__ __forceinline__ int find_in_row( const uint32_t * row, uint32_t len, uint32_t target )
         {
             uint32_t lo = 0, hi = len;
@@ -496,201 +502,547 @@ namespace sesgb
             return ( lo < len && row[ lo ] == target ) ? (int)lo : -1;
         }
 
-        __global__ void k_candidates( Build b, bool write )
+        // ---- probe solve -----------------------------------------------------
+        // Double-precision solve of findIntersectionsBetweenCircles
+        // (operations.inl:384-398): the two points at distance R_i, R_j, R_k
+        // from the centres. Returns false when t < 0 (no point).
+        __device__ __forceinline__ bool solve_d( d3 ci, double ri, d3 cj, double rj, d3 ck, double rk, double rp, d3 & x1, d3 & x2 )
         {
-            const uint32_t C1 = min( b.counts->C1, b.capC1 );
-            uint32_t       ovf = 0;
-            for ( uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < C1; t += gridDim.x * blockDim.x )
-            {
-                const uint32_t   slot = b.trimSlot[ t ];
-                const uint32_t   i    = slot / b.cap;
-                const uint32_t   sj   = slot - i * b.cap;
-                const uint32_t   j    = b.nbr[ slot ];
-                const uint32_t   ni   = b.nbrCount[ i ];
-                const uint32_t   nj   = b.nbrCount[ j ];
-                const uint32_t * rowI = b.nbr + (size_t)i * b.cap;
-                const uint32_t * rowJ = b.nbr + (size_t)j * b.cap;
-                const uint8_t *  stI  = b.status + (size_t)i * b.cap;
-                uint32_t         cnt  = 0;
-                const uint32_t   off  = write ? b.candOff[ t ] : 0;
-                // k > j  <=>  slot of k after slot of j (rows are ascending)
-                for ( uint32_t sk = sj + 1; sk < ni; sk++ )
-                {
-                    if ( stI[ sk ] != 1 )
-                        continue;
-                    const int sjk = find_in_row( rowJ, nj, rowI[ sk ] );
-                    if ( sjk < 0 )
-                        continue;
-                    if ( write )
-                    {
-                        const uint32_t c = off + cnt;
-                        if ( c < b.capCand )
-                            b.cand[ c ] = make_uint4( t, i * b.cap + sk, j * b.cap + (uint32_t)sjk, 0u );
-                        else
-                            ovf |= kOverflowCand;
-                    }
-                    cnt++;
-                }
-                if ( !write )
-                    b.candCnt[ t ] = cnt;
-            }
-            if ( ovf )
-                atomicOr( &b.counts->overflow, ovf );
+            const dcircle cij = dcircle_geometry( ci, ri, cj, rj, rp );
+            const dcircle cik = dcircle_geometry( ci, ri, ck, rk, rp );
+            const d3      u   = dsub( cik.normal, dmul( cij.normal, ddot( cik.normal, cij.normal ) ) );
+            const double  den = ddot( u, cik.normal );
+            const d3 xc = dadd( cij.center, dmul( u, __ddiv_rn( ddot( dsub( cik.center, cij.center ), cik.normal ), den ) ) );
+            const d3     xci = dsub( xc, ci );
+            const double Ri  = __dadd_rn( ri, rp );
+            const double tt  = __dadd_rn( -ddot( xci, xci ), __dmul_rn( Ri, Ri ) );
+            if ( !( tt >= 0.0 ) )
+                return false;
+            const d3     nn   = dnrm( dcross( cij.normal, cik.normal ) );
+            const double root = __dsqrt_rn( tt );
+            x1                = dadd( xc, dmul( nn, root ) );
+            x2                = dsub( xc, dmul( nn, root ) );
+            return true;
         }
 
-        // ---- probe solve -----------------------------------------------------
-        __global__ void __launch_bounds__( 128 ) k_triplets( Build b )
+        // singular flag (operations.inl:441-451): probe closer than rp to the plane of the centres
+        __device__ __forceinline__ bool singular_d( d3 ci, d3 cj, d3 ck, d3 x, double rp )
         {
-            const uint32_t nc   = min( b.counts->cand, b.capCand );
-            if ( blockIdx.x == 0 && threadIdx.x == 0 )
-                b.counts->probeSlots = 2u * nc;
-            const double   rp   = (double)b.rp;
-            const double   tol  = (double)1e-4f;
-            uint32_t       fp64 = 0;
-            for ( uint32_t c = blockIdx.x * blockDim.x + threadIdx.x; c < nc; c += gridDim.x * blockDim.x )
+            const d3     p2p3 = dnrm( dsub( cj, ci ) );
+            const d3     p4p3 = dnrm( dsub( cj, ck ) );
+            const d3     pn   = dnrm( dcross( p2p3, p4p3 ) );
+            const double dd   = ddot( dsub( ci, x ), pn );
+            return __dsub_rn( __dmul_rn( dd, dd ), __dmul_rn( rp, rp ) ) < -(double)1e-4f;
+        }
+
+        // Occlusion of the double-precision points by N(i) \ {j, k} (operations.inl:401-430):
+        // float32 filter around the rounded relative positions, double precision in the band.
+        __device__ __forceinline__ void occlusion_d( const Build & b, uint32_t i, const float4 & ai, uint32_t sj, uint32_t sk,
+                                                     const d3 x[ 2 ], bool vis[ 2 ], uint32_t & fp64 )
+        {
+            const double rp = (double)b.rp;
+            const d3     ci = D3( ai );
+            f3           xr[ 2 ];
+            for ( int e = 0; e < 2; e++ )
+                xr[ e ] = F3( __double2float_rn( __dsub_rn( x[ e ].x, ci.x ) ), __double2float_rn( __dsub_rn( x[ e ].y, ci.y ) ),
+                              __double2float_rn( __dsub_rn( x[ e ].z, ci.z ) ) );
+            const uint32_t ni = b.nbrCount[ i ];
+            for ( uint32_t sl = 0; sl < ni && ( vis[ 0 ] || vis[ 1 ] ); sl++ )
             {
-                const uint4    cd     = b.cand[ c ];
-                const uint32_t t      = cd.x;
-                const uint32_t slotIK = cd.y, slotJK = cd.z;
-                const uint32_t slotIJ = b.trimSlot[ t ];
-                const uint32_t i      = slotIJ / b.cap;
-                const uint32_t sj     = slotIJ - i * b.cap;
-                const uint32_t sk     = slotIK - i * b.cap;
-                const uint32_t j      = b.nbr[ slotIJ ];
-                const uint32_t k      = b.nbr[ slotIK ];
-                const float4   ai = b.atoms[ i ], aj = b.atoms[ j ], ak = b.atoms[ k ];
-                const d3       ci = D3( ai ), cj = D3( aj ), ck = D3( ak );
-                const double   ri = ai.w;
-
-                const dcircle cij = dcircle_geometry( ci, ri, cj, (double)aj.w, rp );
-                const dcircle cik = dcircle_geometry( ci, ri, ck, (double)ak.w, rp );
-                const d3      u   = dsub( cik.normal, dmul( cij.normal, ddot( cik.normal, cij.normal ) ) );
-                const double  den = ddot( u, cik.normal );
-                const d3 xc = dadd( cij.center, dmul( u, __ddiv_rn( ddot( dsub( cik.center, cij.center ), cik.normal ), den ) ) );
-                const d3     xci = dsub( xc, ci );
-                const double Ri  = __dadd_rn( ri, rp );
-                const double tt  = __dadd_rn( -ddot( xci, xci ), __dmul_rn( Ri, Ri ) );
-
-                int  w[ 2 ] = { 0, 0 };
-                d3   x[ 2 ];
-                if ( tt >= 0.0 )
-                {
-                    const d3     nn   = dnrm( dcross( cij.normal, cik.normal ) );
-                    const double root = __dsqrt_rn( tt );
-                    x[ 0 ]            = dadd( xc, dmul( nn, root ) );
-                    x[ 1 ]            = dsub( xc, dmul( nn, root ) );
-                    bool vis[ 2 ]     = { true, true };
-                    f3   xr[ 2 ];
-                    for ( int e = 0; e < 2; e++ )
-                        xr[ e ] = F3( __double2float_rn( __dsub_rn( x[ e ].x, ci.x ) ),
-                                      __double2float_rn( __dsub_rn( x[ e ].y, ci.y ) ),
-                                      __double2float_rn( __dsub_rn( x[ e ].z, ci.z ) ) );
-                    const uint32_t ni = b.nbrCount[ i ];
-                    for ( uint32_t sl = 0; sl < ni && ( vis[ 0 ] || vis[ 1 ] ); sl++ )
-                    {
-                        if ( sl == sj || sl == sk )
-                            continue;
-                        const float4 al  = b.atoms[ b.nbr[ (size_t)i * b.cap + sl ] ];
-                        const f3     dl  = F3( al.x - ai.x, al.y - ai.y, al.z - ai.z );
-                        const float  Rl  = al.w + b.rp;
-                        const float  Rl2 = Rl * Rl;
-                        for ( int e = 0; e < 2; e++ )
-                        {
-                            if ( !vis[ e ] )
-                                continue;
-                            const f3    ev = dl - xr[ e ];
-                            const float ee = dot( ev, ev );
-                            const float m  = ee - Rl2;
-                            const float em = kRel * ( ee + Rl2 + 1.f );
-                            if ( m < -em )
-                                vis[ e ] = false;
-                            else if ( !( m > em ) )
-                            {
-                                const double Rld = __dadd_rn( (double)al.w, rp );
-                                const d3     dv  = dsub( D3( al ), x[ e ] );
-                                vis[ e ]         = __dsub_rn( ddot( dv, dv ), __dmul_rn( Rld, Rld ) ) > 0.0;
-                                fp64++;
-                            }
-                        }
-                    }
-                    if ( vis[ 0 ] || vis[ 1 ] )
-                    {
-                        const d3 p2p3 = dnrm( dsub( cj, ci ) );
-                        const d3 p4p3 = dnrm( dsub( cj, ck ) );
-                        const d3 pn   = dnrm( dcross( p2p3, p4p3 ) );
-                        for ( int e = 0; e < 2; e++ )
-                        {
-                            if ( !vis[ e ] )
-                                continue;
-                            const double dd       = ddot( dsub( ci, x[ e ] ), pn );
-                            const bool   singular = __dsub_rn( __dmul_rn( dd, dd ), __dmul_rn( rp, rp ) ) < -tol;
-                            w[ e ]                = ( e == 0 ? 1 : -1 ) * ( 1 + ( singular ? 1 : 0 ) );
-                        }
-                    }
-                }
+                if ( sl == sj || sl == sk )
+                    continue;
+                const float4 al  = b.atoms[ b.nbr[ (size_t)i * b.cap + sl ] ];
+                const f3     dl  = F3( al.x - ai.x, al.y - ai.y, al.z - ai.z );
+                const float  Rl  = al.w + b.rp;
+                const float  Rl2 = Rl * Rl;
                 for ( int e = 0; e < 2; e++ )
                 {
-                    const size_t q = 2ull * c + e;
-                    const int    s = w[ e ] == 2 || w[ e ] == -2;
-                    b.isSing[ q ]  = w[ e ] != 0 && s;
-                    b.isReg[ q ]   = w[ e ] != 0 && !s;
-                    if ( w[ e ] == 0 )
-                    {
-                        b.slotCid[ q ] = make_int4( 0, 0, 0, 0 );
+                    if ( !vis[ e ] )
                         continue;
+                    const f3    ev = dl - xr[ e ];
+                    const float ee = dot( ev, ev );
+                    const float m  = ee - Rl2;
+                    const float em = kRel * ( ee + Rl2 + 1.f );
+                    if ( m < -em )
+                        vis[ e ] = false;
+                    else if ( !( m > em ) )
+                    {
+                        const double Rld = __dadd_rn( (double)al.w, rp );
+                        const d3     dv  = dsub( D3( al ), x[ e ] );
+                        vis[ e ]         = __dsub_rn( ddot( dv, dv ), __dmul_rn( Rld, Rld ) ) > 0.0;
+                        fp64++;
                     }
-                    b.slotPos[ q ] = make_float4( __double2float_rn( x[ e ].x ), __double2float_rn( x[ e ].y ),
-                                                  __double2float_rn( x[ e ].z ), (float)w[ e ] );
-                    if ( b.mode == 0 )
-                        b.slotCid[ q ] = make_int4( (int)t, (int)b.slotTrim[ slotJK ], (int)b.slotTrim[ slotIK ], w[ e ] );
-                    else
-                        b.slotCid[ q ] = make_int4( (int)slotIJ, (int)slotIK, (int)slotJK, w[ e ] );
+                }
+            }
+        }
+
+        // Error scale of the float32 solve (relative, generous: about 60x the
+        // accumulated rounding of its ~25 dependent operations).
+        constexpr float kSolve = 1.0f / 262144.0f; // 2^-18
+
+        constexpr int kProbeWarps = 4;   // warps per block of k_probes
+        constexpr int kCandBuf    = 64;  // candidates queued per warp
+        constexpr int kProbeBuf   = 128; // probes of one atom (the reference's per-block buffer, operations.inl:248)
+
+        struct ProbeSmem
+        {
+            float4 *   rel;  // cap: neighbour centre - centre of i, R of the neighbour
+            uint32_t * nid;  // cap: neighbour ids
+            uint16_t * plist; // cap: slots of the partial circles (i, j), i < j
+            uint2 *    cand; // kCandBuf: (slot j | slot k << 16, slot of k in N(j))
+            float4 *   ppos; // kProbeBuf
+            int4 *     pcid; // kProbeBuf
+            int4 *     pids; // kProbeBuf
+        };
+
+        __host__ __device__ inline size_t probe_smem_per_warp( uint32_t cap )
+        {
+            size_t b = (size_t)cap * ( 16 + 4 + 2 );
+            b        = ( b + 15 ) & ~(size_t)15;
+            return b + kCandBuf * 8 + kProbeBuf * ( 16 + 16 + 16 );
+        }
+
+        __device__ inline ProbeSmem probe_smem( unsigned char * base, uint32_t cap )
+        {
+            ProbeSmem m;
+            m.rel   = reinterpret_cast<float4 *>( base );
+            m.nid   = reinterpret_cast<uint32_t *>( base + (size_t)cap * 16 );
+            m.plist = reinterpret_cast<uint16_t *>( base + (size_t)cap * 20 );
+            size_t o = ( (size_t)cap * 22 + 15 ) & ~(size_t)15;
+            m.cand  = reinterpret_cast<uint2 *>( base + o );
+            o += kCandBuf * 8;
+            m.ppos = reinterpret_cast<float4 *>( base + o );
+            o += kProbeBuf * 16;
+            m.pcid = reinterpret_cast<int4 *>( base + o );
+            o += kProbeBuf * 16;
+            m.pids = reinterpret_cast<int4 *>( base + o );
+            return m;
+        }
+
+        // float32 singular test (operations.inl:441-451) in coordinates relative to
+        // atom i: 1 singular, 0 regular, -1 inside the band (decide in double)
+        __device__ __forceinline__ int singular_f( f3 dj, f3 dk, f3 x, float ep, float rp )
+        {
+            const f3    a  = normalize( dj );
+            const f3    c  = normalize( dj - dk );
+            const f3    cr = cross( a, c );
+            const float s2 = dot( cr, cr );
+            if ( !( s2 > 1e-6f ) )
+                return -1;
+            const f3    pn = cr * rsqrtf( s2 );
+            const float d  = -dot( x, pn );
+            const float xn = sqrtf( dot( x, x ) );
+            const float ed = ep + xn * kSolve * ( 4.f + 4.f * rsqrtf( s2 ) );
+            const float ms = d * d - rp * rp + 1e-4f;
+            const float es = 2.f * ( fabsf( d ) + ed ) * ed + kRel * ( d * d + rp * rp + 1.f );
+            if ( ms < -es )
+                return 1;
+            if ( ms > es )
+                return 0;
+            return -1;
+        }
+
+        // Job of the double-precision pass: entry index, atom, slots, kind.
+        enum : uint32_t
+        {
+            kJobFill = 0, // one side decided visible in float32: exact position (and singular flag if pending)
+            kJobBand = 1, // the float32 screen hit the band: solve, occlusion and flags in double precision
+        };
+
+        // One (i, j, k) candidate, float32 screen in coordinates relative to atom i
+        // with a conservative error band. Returns the number of entries it needs in
+        // the atom's probe list: 0 (no kept point), 1 or 2 (kept sides, decided), or
+        // 2 with band = true (both entries reserved for the double-precision pass).
+        // w[e]: 0 none, +-1 regular, +-2 singular, +-3 kept with the singular flag undecided.
+        __device__ void probe_screen( const Build & b, const float4 & ai, const ProbeSmem & m, uint32_t ni, uint32_t sj,
+                                      uint32_t sk, int w[ 2 ], bool & band )
+        {
+            const float4 qj = m.rel[ sj ], qk = m.rel[ sk ];
+            const float  Ri = ai.w + b.rp, Rj = qj.w, Rk = qk.w;
+            const f3     dj = F3( qj.x, qj.y, qj.z ), dk = F3( qk.x, qk.y, qk.z );
+            const float  dJ = dot( dj, dj ), dK = dot( dk, dk );
+            const f3     cJ = dj * ( ( Ri * Ri - Rj * Rj + dJ ) / ( 2.f * dJ ) );
+            const f3     cK = dk * ( ( Ri * Ri - Rk * Rk + dK ) / ( 2.f * dK ) );
+            const f3     nJ = dj * rsqrtf( dJ );
+            const f3     nK = dk * rsqrtf( dK );
+            const f3     u  = nK - nJ * dot( nK, nJ );
+            const float  den = dot( u, nK ); // sin^2 of the angle between the circle axes
+            w[ 0 ] = w[ 1 ] = 0;
+            band            = !( den > 1e-3f );
+            if ( band )
+                return;
+            const f3    xc = cJ + u * ( dot( cK - cJ, nK ) / den );
+            const float xn = sqrtf( dot( xc, xc ) );
+            const float ex = kSolve * ( Ri + xn ) * ( 1.f + 1.f / den );
+            const float tt = Ri * Ri - xn * xn;
+            const float et = 2.f * ( xn + ex ) * ex + kSolve * Ri * Ri;
+            if ( tt < -et )
+                return; // no point
+            if ( !( tt > et ) )
+            {
+                band = true;
+                return;
+            }
+            const float root = sqrtf( tt );
+            const f3    nn   = normalize( cross( nJ, nK ) );
+            const float ep   = ex + et / ( 2.f * root ) + root * kSolve / sqrtf( den );
+            const f3    x1   = xc + nn * root;
+            const f3    x2   = xc - nn * root;
+            bool        vis[ 2 ] = { true, true };
+            for ( uint32_t sl = 0; sl < ni && ( vis[ 0 ] || vis[ 1 ] ); sl++ )
+            {
+                if ( sl == sj || sl == sk )
+                    continue;
+                const float4 ql  = m.rel[ sl ];
+                const float  Rl2 = ql.w * ql.w;
+#pragma unroll
+                for ( int e = 0; e < 2; e++ )
+                {
+                    if ( !vis[ e ] )
+                        continue;
+                    const f3    xe = e == 0 ? x1 : x2;
+                    const f3    ev = F3( ql.x - xe.x, ql.y - xe.y, ql.z - xe.z );
+                    const float ee = dot( ev, ev );
+                    const float mm = ee - Rl2;
+                    const float em = 2.f * sqrtf( ee ) * ep + ep * ep + kRel * ( ee + Rl2 + 1.f );
+                    if ( mm < -em )
+                        vis[ e ] = false;
+                    else if ( !( mm > em ) )
+                    {
+                        band = true;
+                        return;
+                    }
+                }
+            }
+            for ( int e = 0; e < 2; e++ )
+                if ( vis[ e ] )
+                {
+                    const int sg = singular_f( dj, dk, e == 0 ? x1 : x2, ep, b.rp );
+                    w[ e ]       = ( e == 0 ? 1 : -1 ) * ( sg < 0 ? 3 : 1 + sg );
+                }
+        }
+
+        // Warp per atom i: the partial circles (i, j), i < j, paired with every
+        // later partial circle (i, k) whose k is a neighbour of j. Entries of the
+        // atom's probe list are kept in order (circle (i, j), then k, then x1
+        // before x2) and written as one chunk; positions and undecided flags are
+        // completed by k_probe_jobs.
+        __global__ void __launch_bounds__( 32 * kProbeWarps ) k_probes( Build b )
+        {
+            extern __shared__ __align__( 16 ) unsigned char smemRaw[];
+            const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
+            const uint32_t i    = blockIdx.x * kProbeWarps + warp;
+            if ( i >= b.n )
+                return;
+            const ProbeSmem m  = probe_smem( smemRaw + warp * probe_smem_per_warp( b.cap ), b.cap );
+            const uint32_t  ni = b.nbrCount[ i ];
+            const float4    ai = b.atoms[ i ];
+            const size_t    row = (size_t)i * b.cap;
+
+            uint32_t p = 0;
+            for ( uint32_t base = 0; base < ni; base += 32 )
+            {
+                const uint32_t s   = base + lane;
+                bool           isP = false;
+                if ( s < ni )
+                {
+                    const uint32_t j  = b.nbr[ row + s ];
+                    const float4   aj = b.atoms[ j ];
+                    m.rel[ s ]        = make_float4( aj.x - ai.x, aj.y - ai.y, aj.z - ai.z, aj.w + b.rp );
+                    m.nid[ s ]        = j;
+                    isP               = b.status[ row + s ] == 1 && i < j;
+                }
+                const uint32_t mk = __ballot_sync( 0xffffffffu, isP );
+                if ( isP )
+                    m.plist[ p + __popc( mk & lanemask_lt() ) ] = (uint16_t)s;
+                p += __popc( mk );
+            }
+            __syncwarp();
+
+            uint32_t       nCand = 0, nEnt = 0, nSing = 0, nReg = 0, cands = 0;
+            const uint32_t pairs = p * ( p > 0 ? p - 1 : 0 ) / 2;
+            for ( uint32_t q0 = 0; q0 < pairs || nCand > 0; q0 += 32 )
+            {
+                if ( q0 < pairs )
+                {
+                    // pair q = (a, bb), a < bb, row-major over the partial circles
+                    const uint32_t q   = q0 + lane;
+                    bool           isC = false;
+                    uint32_t       sj = 0, sk = 0, sjk = 0;
+                    if ( q < pairs )
+                    {
+                        const float tp = 2.f * p - 1.f;
+                        int         a  = (int)floorf( 0.5f * ( tp - sqrtf( fmaxf( tp * tp - 8.f * (float)q, 0.f ) ) ) );
+                        a              = a < 0 ? 0 : a;
+                        while ( a > 0 && (uint32_t)( a * ( 2 * (int)p - a - 1 ) / 2 ) > q )
+                            a--;
+                        while ( (uint32_t)( ( a + 1 ) * ( 2 * (int)p - a - 2 ) / 2 ) <= q )
+                            a++;
+                        const uint32_t bb = (uint32_t)a + 1 + ( q - (uint32_t)( a * ( 2 * (int)p - a - 1 ) / 2 ) );
+                        sj                = m.plist[ a ];
+                        sk                = m.plist[ bb ];
+                        const uint32_t j  = m.nid[ sj ];
+                        const int      r  = find_in_row( b.nbr + (size_t)j * b.cap, b.nbrCount[ j ], m.nid[ sk ] );
+                        isC               = r >= 0;
+                        sjk               = (uint32_t)r;
+                    }
+                    const uint32_t mc = __ballot_sync( 0xffffffffu, isC );
+                    if ( isC )
+                        m.cand[ nCand + __popc( mc & lanemask_lt() ) ] = make_uint2( sj | ( sk << 16 ), sjk );
+                    nCand += __popc( mc );
+                    cands += __popc( mc );
+                }
+                __syncwarp();
+                // process full batches of 32 candidates (and the rest at the end)
+                while ( nCand >= 32 || ( nCand > 0 && q0 + 32 >= pairs ) )
+                {
+                    const uint32_t batch = nCand < 32 ? nCand : 32;
+                    int            w[ 2 ] = { 0, 0 };
+                    bool           band   = false;
+                    uint32_t       sj = 0, sk = 0, sjk = 0;
+                    if ( lane < batch )
+                    {
+                        const uint2 cd = m.cand[ lane ];
+                        sj             = cd.x & 0xffffu;
+                        sk             = cd.x >> 16;
+                        sjk            = cd.y;
+                        probe_screen( b, ai, m, ni, sj, sk, w, band );
+                    }
+                    const uint32_t need = band ? 2u : ( w[ 0 ] != 0 ) + ( w[ 1 ] != 0 );
+                    uint32_t       tot;
+                    uint32_t       at   = nEnt + warp_exclusive_sum( need, tot );
+                    if ( need )
+                    {
+                        const uint32_t j = m.nid[ sj ], k = m.nid[ sk ];
+                        const int4     ids = make_int4( (int)i, (int)j, (int)k, 0 );
+                        int4           cid;
+                        if ( b.mode == 0 )
+                            cid = make_int4( (int)b.slotTrim[ row + sj ], (int)b.slotTrim[ (size_t)j * b.cap + sjk ], (int)b.slotTrim[ row + sk ], 0 );
+                        else
+                            cid = make_int4( (int)( row + sj ), (int)( row + sk ), (int)( (size_t)j * b.cap + sjk ), 0 );
+                        for ( int e = 0; e < 2; e++ )
+                        {
+                            if ( !band && w[ e ] == 0 )
+                                continue;
+                            if ( at < (uint32_t)kProbeBuf )
+                            {
+                                cid.w        = band ? 0 : w[ e ];
+                                m.pcid[ at ] = cid;
+                                m.pids[ at ] = ids;
+                                // job description: slots, side, kind (entry index added when written out)
+                                m.ppos[ at ] = make_float4( __uint_as_float( sj | ( sk << 16 ) ), __uint_as_float( sjk ),
+                                                            __uint_as_float( (uint32_t)e | ( ( band ? kJobBand : kJobFill ) << 8 ) ), 0.f );
+                            }
+                            if ( !band )
+                            {
+                                const int aw = w[ e ] < 0 ? -w[ e ] : w[ e ];
+                                nSing += aw == 2;
+                                nReg += aw == 1;
+                            }
+                            at++;
+                        }
+                    }
+                    nEnt += tot;
+                    // drop the processed batch from the queue
+                    __syncwarp();
+                    const uint32_t rest = nCand - batch;
+                    uint2          keep[ 2 ];
+                    for ( uint32_t r = 0; r < 2; r++ )
+                        if ( lane + 32 * r < rest )
+                            keep[ r ] = m.cand[ batch + lane + 32 * r ];
+                    __syncwarp();
+                    for ( uint32_t r = 0; r < 2; r++ )
+                        if ( lane + 32 * r < rest )
+                            m.cand[ lane + 32 * r ] = keep[ r ];
+                    __syncwarp();
+                    nCand = rest;
                 }
             }
             for ( int o = 16; o > 0; o >>= 1 )
-                fp64 += __shfl_xor_sync( 0xffffffffu, fp64, o );
-            if ( lane_id() == 0 && fp64 )
-                atomicAdd( &b.counts->fp64[ kFp64Occlusion ], fp64 );
+            {
+                nSing += __shfl_xor_sync( 0xffffffffu, nSing, o );
+                nReg += __shfl_xor_sync( 0xffffffffu, nReg, o );
+            }
+            __syncwarp();
+            // one chunk per atom; one double-precision job per kept side or band candidate
+            const uint32_t kept = nEnt < (uint32_t)kProbeBuf ? nEnt : (uint32_t)kProbeBuf;
+            uint32_t       chunk = 0;
+            if ( lane == 0 )
+            {
+                if ( nEnt > (uint32_t)kProbeBuf )
+                    atomicOr( &b.counts->overflow, (uint32_t)kOverflowAtomProbes );
+                chunk = kept ? atomicAdd( &b.counts->staged, kept ) : 0u;
+                if ( cands )
+                    atomicAdd( &b.counts->cand, cands );
+            }
+            chunk           = __shfl_sync( 0xffffffffu, chunk, 0 );
+            const bool fits = chunk + kept <= b.capProbes;
+            for ( uint32_t q = lane; q < kept && fits; q += 32 )
+            {
+                b.stageCid[ chunk + q ] = m.pcid[ q ];
+                b.stageIds[ chunk + q ] = m.pids[ q ];
+                b.stagePos[ chunk + q ] = make_float4( 0.f, 0.f, 0.f, 0.f );
+            }
+            // jobs: a fill entry is one job; a band candidate's two entries are one job (on its first entry)
+            uint32_t jobsHere = 0;
+            for ( uint32_t q0 = 0; q0 < kept; q0 += 32 )
+            {
+                const uint32_t q     = q0 + lane;
+                bool           isJob = false;
+                if ( q < kept && fits )
+                {
+                    const uint32_t info = __float_as_uint( m.ppos[ q ].z );
+                    isJob               = ( info >> 8 ) == kJobFill || ( info & 0xffu ) == 0u;
+                }
+                jobsHere += __popc( __ballot_sync( 0xffffffffu, isJob ) );
+            }
+            uint32_t jbase = 0;
+            if ( lane == 0 && jobsHere )
+                jbase = atomicAdd( &b.counts->jobs, jobsHere );
+            jbase = __shfl_sync( 0xffffffffu, jbase, 0 );
+            for ( uint32_t q0 = 0; q0 < kept; q0 += 32 )
+            {
+                const uint32_t q     = q0 + lane;
+                bool           isJob = false;
+                float4         jb    = make_float4( 0.f, 0.f, 0.f, 0.f );
+                if ( q < kept && fits )
+                {
+                    jb                  = m.ppos[ q ];
+                    const uint32_t info = __float_as_uint( jb.z );
+                    isJob               = ( info >> 8 ) == kJobFill || ( info & 0xffu ) == 0u;
+                }
+                const uint32_t mj = __ballot_sync( 0xffffffffu, isJob );
+                if ( isJob )
+                {
+                    const uint32_t slot = jbase + __popc( mj & lanemask_lt() );
+                    if ( slot < b.capProbes )
+                        b.jobs[ slot ] = make_uint4( chunk + q, i, __float_as_uint( jb.x ),
+                                                     ( __float_as_uint( jb.y ) & 0xffffu ) | ( ( __float_as_uint( jb.z ) & 0xffffu ) << 16 ) );
+                }
+                jbase += __popc( mj );
+            }
+            if ( lane == 0 )
+            {
+                if ( !fits )
+                    atomicOr( &b.counts->overflow, (uint32_t)kOverflowProbes );
+                b.chunkStart[ i ] = chunk;
+                b.chunkLen[ i ]   = fits ? kept : 0u;
+                b.singCnt[ i ]    = fits ? nSing : 0u;
+                b.regCnt[ i ]     = fits ? nReg : 0u;
+            }
         }
 
-        // ---- stable partition (singular first) and fill ----------------------
-        __global__ void k_place( Build b )
+        // The double-precision pass, one job per thread with full warps: exact
+        // probe positions (the solve of findIntersectionsBetweenCircles in IEEE
+        // double, rounded once to float32) and the decisions the float32 screen
+        // left open.
+        __global__ void __launch_bounds__( 128 ) k_probe_jobs( Build b )
         {
-            const uint32_t ns  = 2u * min( b.counts->cand, b.capCand );
-            const uint32_t Q   = b.counts->Q;
-            uint32_t       ovf = 0;
-            if ( blockIdx.x == 0 && threadIdx.x == 0 )
-                b.counts->I = Q + b.counts->regTotal;
-            for ( uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < ns; q += gridDim.x * blockDim.x )
+            const uint32_t nj   = min( b.counts->jobs, b.capProbes );
+            const double   rp   = (double)b.rp;
+            uint32_t       fp64 = 0, full64 = 0;
+            for ( uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nj; t += gridDim.x * blockDim.x )
             {
-                const int4 cid = b.slotCid[ q ];
-                if ( cid.w == 0 )
-                    continue;
-                const bool     sing = cid.w == 2 || cid.w == -2;
-                const uint32_t idx  = sing ? b.isSing[ q ] : Q + b.isReg[ q ];
-                if ( idx >= b.capProbes )
+                const uint4    jb   = b.jobs[ t ];
+                const uint32_t ent  = jb.x, i = jb.y;
+                const uint32_t sj   = jb.z & 0xffffu, sk = jb.z >> 16;
+                const uint32_t info = jb.w >> 16;
+                const uint32_t side = info & 0xffu, kind = info >> 8;
+                const size_t   row  = (size_t)i * b.cap;
+                const float4   ai = b.atoms[ i ], aj = b.atoms[ b.nbr[ row + sj ] ], ak = b.atoms[ b.nbr[ row + sk ] ];
+                const d3       ci = D3( ai ), cj = D3( aj ), ck = D3( ak );
+                d3             x[ 2 ];
+                const bool     ok = solve_d( ci, (double)ai.w, cj, (double)aj.w, ck, (double)ak.w, rp, x[ 0 ], x[ 1 ] );
+                if ( kind == kJobFill )
                 {
-                    ovf |= kOverflowProbes;
+                    int4 cid = b.stageCid[ ent ];
+                    int  aw  = cid.w < 0 ? -cid.w : cid.w;
+                    if ( aw == 3 )
+                    {
+                        aw    = singular_d( ci, cj, ck, x[ side ], rp ) ? 2 : 1;
+                        cid.w = cid.w < 0 ? -aw : aw;
+                        b.stageCid[ ent ] = cid;
+                        atomicAdd( aw == 2 ? &b.singCnt[ i ] : &b.regCnt[ i ], 1u );
+                    }
+                    b.stagePos[ ent ] = make_float4( __double2float_rn( x[ side ].x ), __double2float_rn( x[ side ].y ),
+                                                     __double2float_rn( x[ side ].z ), (float)cid.w );
                     continue;
                 }
-                b.probePos[ idx ] = b.slotPos[ q ];
-                b.probeCid[ idx ] = cid;
-                uint32_t i, j, k;
+                // band candidate: entries ent (x1) and ent + 1 (x2)
+                full64++;
+                if ( !ok )
+                    continue;
+                bool vis[ 2 ] = { true, true };
+                occlusion_d( b, i, ai, sj, sk, x, vis, fp64 );
+                for ( int e = 0; e < 2; e++ )
+                {
+                    if ( !vis[ e ] )
+                        continue;
+                    int4      cid = b.stageCid[ ent + e ];
+                    const int aw  = singular_d( ci, cj, ck, x[ e ], rp ) ? 2 : 1;
+                    cid.w         = e == 0 ? aw : -aw;
+                    b.stageCid[ ent + e ] = cid;
+                    b.stagePos[ ent + e ] = make_float4( __double2float_rn( x[ e ].x ), __double2float_rn( x[ e ].y ),
+                                                         __double2float_rn( x[ e ].z ), (float)cid.w );
+                    atomicAdd( aw == 2 ? &b.singCnt[ i ] : &b.regCnt[ i ], 1u );
+                }
+            }
+            for ( int o = 16; o > 0; o >>= 1 )
+            {
+                fp64 += __shfl_xor_sync( 0xffffffffu, fp64, o );
+                full64 += __shfl_xor_sync( 0xffffffffu, full64, o );
+            }
+            if ( lane_id() == 0 )
+            {
+                if ( fp64 )
+                    atomicAdd( &b.counts->fp64[ kFp64Occlusion ], fp64 );
+                if ( full64 )
+                    atomicAdd( &b.counts->fp64[ kFp64Solve ], full64 );
+            }
+        }
+
+        // Stable placement, singular probes first (the reference partitions with an
+        // unstable sort, operations.inl:128-135), and the fill of
+        // fillIntersections (operations.cu:206-269; exterior ssesdf/operations.cu:287-329).
+        __global__ void __launch_bounds__( 32 * kWarpsPerBlock ) k_place( Build b )
+        {
+            const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
+            const uint32_t i    = blockIdx.x * kWarpsPerBlock + warp;
+            if ( i == 0 && lane == 0 )
+                b.counts->I = b.counts->Q + b.counts->regTotal;
+            if ( i >= b.n )
+                return;
+            const uint32_t Q     = b.counts->Q;
+            const uint32_t cnt   = b.chunkLen[ i ];
+            const uint32_t chunk = b.chunkStart[ i ];
+            uint32_t       so = b.singOff[ i ], ro = Q + b.regOff[ i ];
+            for ( uint32_t m0 = 0; m0 < cnt; m0 += 32 )
+            {
+                const uint32_t m     = m0 + lane;
+                const bool     valid = m < cnt;
+                int4           cid   = make_int4( 0, 0, 0, 0 );
+                if ( valid )
+                    cid = b.stageCid[ chunk + m ];
+                const bool     live = valid && cid.w != 0; // band entries without a point are holes
+                const bool     sing = live && ( cid.w == 2 || cid.w == -2 );
+                const uint32_t ms   = __ballot_sync( 0xffffffffu, sing );
+                const uint32_t mr   = __ballot_sync( 0xffffffffu, live && !sing );
+                const uint32_t dst  = sing ? so + __popc( ms & lanemask_lt() ) : ro + __popc( mr & lanemask_lt() );
+                so += __popc( ms );
+                ro += __popc( mr );
+                if ( !live )
+                    continue;
+                b.probePos[ dst ] = b.stagePos[ chunk + m ];
+                b.probeCid[ dst ] = cid;
+                b.probeIds[ dst ] = b.stageIds[ chunk + m ];
                 if ( b.mode == 0 )
                 {
-                    const uint32_t sIJ = b.trimSlot[ cid.x ];
-                    i                  = sIJ / b.cap;
-                    j                  = b.nbr[ sIJ ];
-                    k                  = b.nbr[ b.trimSlot[ cid.z ] ];
                     atomicAdd( &b.ccount[ cid.x ], 1u );
                     atomicAdd( &b.ccount[ cid.y ], 1u );
                     atomicAdd( &b.ccount[ cid.z ], 1u );
                 }
                 else
                 {
-                    i = (uint32_t)cid.x / b.cap;
-                    j = b.nbr[ cid.x ];
-                    k = b.nbr[ cid.y ];
                     // exterior: the probe's three circles become tori (status 1 -> 2)
                     if ( b.status[ cid.x ] == 1 )
                         b.status[ cid.x ] = 2;
@@ -699,10 +1051,7 @@ namespace sesgb
                     if ( b.status[ cid.z ] == 1 )
                         b.status[ cid.z ] = 2;
                 }
-                b.probeIds[ idx ] = make_int4( (int)i, (int)j, (int)k, 0 );
             }
-            if ( ovf )
-                atomicOr( &b.counts->overflow, ovf );
         }
 
         __global__ void k_lists( Build b )
@@ -1018,6 +1367,9 @@ namespace sesgb
             }
         }
 
+        std::atomic<uint64_t> g_launches { 0 };
+        inline void counted( uint32_t k = 1 ) { g_launches.fetch_add( k, std::memory_order_relaxed ); }
+
         inline uint32_t blocks_for( uint64_t n, uint32_t threads )
         {
             return (uint32_t)( ( n + threads - 1 ) / threads );
@@ -1031,14 +1383,22 @@ namespace sesgb
 
     void launch_hash( const Build & b, cudaStream_t s )
     {
-        if ( b.n )
-            k_hash<<<blocks_for( b.n, 256 ), 256, 0, s>>>( b );
+        if ( !b.n )
+            return;
+        k_hash<<<blocks_for( b.n, 256 ), 256, 0, s>>>( b );
+        counted();
     }
-    void launch_fine_params( const Build & b, float cutoff, uint32_t, cudaStream_t s ) { k_fine_params<<<1, 1, 0, s>>>( b, cutoff ); }
+    void launch_fine_params( const Build & b, float cutoff, uint32_t, cudaStream_t s )
+    {
+        k_fine_params<<<1, 1, 0, s>>>( b, cutoff );
+        counted();
+    }
     void launch_gather( const Build & b, cudaStream_t s )
     {
-        if ( b.n )
-            k_gather<<<blocks_for( b.n, 256 ), 256, 0, s>>>( b );
+        if ( !b.n )
+            return;
+        k_gather<<<blocks_for( b.n, 256 ), 256, 0, s>>>( b );
+        counted();
     }
     void launch_cells( const Build & b, const float4 * pos, uint32_t nHost, const uint32_t * nDevice, void * scanScratch,
                        cudaStream_t s )
@@ -1052,11 +1412,14 @@ namespace sesgb
         const uint32_t * cells = reinterpret_cast<const uint32_t *>( reinterpret_cast<const char *>( b.fine ) + offsetof( FineGrid, cells ) );
         exclusive_scan( b.cellCount, b.cellStart, b.capCells, cells, nullptr, scanScratch, s );
         k_cell_scatter<<<blocks, 256, 0, s>>>( b, pos, nHost, nDevice );
+        counted( 2 );
     }
     void launch_neighbors( const Build & b, cudaStream_t s )
     {
-        if ( b.n )
-            k_neighbors<<<blocks_for( b.n, kWarpsPerBlock ), 32 * kWarpsPerBlock, 0, s>>>( b );
+        if ( !b.n )
+            return;
+        k_neighbors<<<blocks_for( b.n, kWarpsPerBlock ), 32 * kWarpsPerBlock, 0, s>>>( b );
+        counted();
     }
     void launch_visibility( const Build & b, cudaStream_t s )
     {
@@ -1064,61 +1427,90 @@ namespace sesgb
             return;
         const size_t smem = sizeof( float4 ) * (size_t)b.cap * kWarpsPerBlock;
         k_visibility<<<blocks_for( b.n, kWarpsPerBlock ), 32 * kWarpsPerBlock, smem, s>>>( b );
+        counted();
     }
     void launch_emit( const Build & b, cudaStream_t s )
     {
-        if ( b.n )
-            k_emit<<<blocks_for( b.n, kWarpsPerBlock ), 32 * kWarpsPerBlock, 0, s>>>( b );
+        if ( !b.n )
+            return;
+        k_emit<<<blocks_for( b.n, kWarpsPerBlock ), 32 * kWarpsPerBlock, 0, s>>>( b );
+        counted();
     }
-    void launch_candidates( const Build & b, bool write, cudaStream_t s )
+    void launch_probes( const Build & b, cudaStream_t s )
     {
-        k_candidates<<<min( persistent_blocks( 256 ), blocks_for( b.capC1, 256 ) + 1 ), 256, 0, s>>>( b, write );
+        if ( !b.n )
+            return;
+        const size_t smem = probe_smem_per_warp( b.cap ) * kProbeWarps;
+        k_probes<<<blocks_for( b.n, kProbeWarps ), 32 * kProbeWarps, smem, s>>>( b );
+        counted();
     }
-    void launch_triplets( const Build & b, cudaStream_t s )
+    void launch_probe_jobs( const Build & b, cudaStream_t s )
     {
-        k_triplets<<<min( persistent_blocks( 128 ), blocks_for( b.capCand, 128 ) + 1 ), 128, 0, s>>>( b );
+        k_probe_jobs<<<min( persistent_blocks( 128 ), blocks_for( b.capProbes, 128 ) + 1 ), 128, 0, s>>>( b );
+        counted();
     }
     void launch_place( const Build & b, cudaStream_t s )
     {
-        k_place<<<min( persistent_blocks( 256 ), blocks_for( 2ull * b.capCand, 256 ) + 1 ), 256, 0, s>>>( b );
+        if ( !b.n )
+            return;
+        k_place<<<blocks_for( b.n, kWarpsPerBlock ), 32 * kWarpsPerBlock, 0, s>>>( b );
+        counted();
     }
     void launch_lists( const Build & b, cudaStream_t s )
     {
         k_lists<<<min( persistent_blocks( 256 ), blocks_for( b.capProbes, 256 ) + 1 ), 256, 0, s>>>( b );
+        counted();
     }
     void launch_segment_counts( const Build & b, cudaStream_t s )
     {
         k_segment_counts<<<min( persistent_blocks( 256 ), blocks_for( b.capC1, 256 ) + 1 ), 256, 0, s>>>( b );
+        counted();
     }
     void launch_segments( const Build & b, cudaStream_t s )
     {
         k_segments<<<min( persistent_blocks( 128 ), blocks_for( b.capC1, 128 ) + 1 ), 128, 0, s>>>( b );
+        counted();
     }
     void launch_probe_neighbors( const Build & b, cudaStream_t s )
     {
         k_probe_neighbors<<<min( persistent_blocks( 256 ), blocks_for( b.capProbes, kWarpsPerBlock ) + 1 ), 32 * kWarpsPerBlock, 0, s>>>( b );
+        counted();
         if ( b.mode == 1 )
+        {
             k_probe_w<<<min( persistent_blocks( 256 ), blocks_for( b.capProbes, 256 ) + 1 ), 256, 0, s>>>( b );
+            counted();
+        }
     }
     void launch_tori( const Build & b, cudaStream_t s )
     {
         if ( !b.n )
             return;
         k_tori_count<<<blocks_for( b.n, kWarpsPerBlock ), 32 * kWarpsPerBlock, 0, s>>>( b );
+        counted();
     }
     void launch_tori_emit( const Build & b, cudaStream_t s )
     {
-        if ( b.n )
-            k_tori<<<blocks_for( b.n, kWarpsPerBlock ), 32 * kWarpsPerBlock, 0, s>>>( b );
+        if ( !b.n )
+            return;
+        k_tori<<<blocks_for( b.n, kWarpsPerBlock ), 32 * kWarpsPerBlock, 0, s>>>( b );
+        counted();
     }
+    uint64_t launch_count() { return g_launches.load(); }
+    void     count_launches( uint32_t k ) { counted( k ); }
+
     cudaError_t configure_kernels( const Build & b )
     {
         const size_t smem = sizeof( float4 ) * (size_t)b.cap * kWarpsPerBlock;
-        return cudaFuncSetAttribute( k_visibility, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem );
+        cudaError_t  e    = cudaFuncSetAttribute( k_visibility, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem );
+        if ( e != cudaSuccess )
+            return e;
+        return cudaFuncSetAttribute( k_probes, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                     (int)( probe_smem_per_warp( b.cap ) * kProbeWarps ) );
     }
     void launch_reference_fill( const Build & b, uint32_t * globalToTrimmed, cudaStream_t s )
     {
         const uint64_t total = (uint64_t)b.n * b.cap + 1;
         k_reference_fill<<<min( persistent_blocks( 256 ), blocks_for( total, 256 ) ), 256, 0, s>>>( b, globalToTrimmed );
+        counted();
     }
 } // namespace sesgb

@@ -22,7 +22,7 @@ namespace sesgb
         GridRef  grid;
 
         // capacities of the count-dependent buffers
-        uint32_t capSectors, capFull, capC1, capCand, capProbes, capSeg, capTori, capCells;
+        uint32_t capSectors, capFull, capC1, capProbes, capSeg, capTori, capCells;
 
         // atoms
         float4 *       atomsIn; // input order (device copy)
@@ -55,15 +55,18 @@ namespace sesgb
 
         // partial circles
         uint32_t * trimSlot; // C1
-        uint32_t * candCnt;  // C1 + 1
-        uint32_t * candOff;  // C1 + 1
-        uint4 *    cand;     // capCand: (t, slotIK, slotJK, -)
 
-        // probe slots (two per candidate)
-        uint32_t * isSing;  // 2 capCand + 1
-        uint32_t * isReg;   // 2 capCand + 1
-        float4 *   slotPos; // 2 capCand
-        int4 *     slotCid; // 2 capCand
+        // probes of each atom, staged as one chunk per atom (capProbes)
+        float4 *   stagePos;
+        int4 *     stageCid;
+        int4 *     stageIds;
+        uint32_t * chunkStart; // n
+        uint32_t * chunkLen;   // n
+        uint4 *    jobs;       // capProbes: double-precision jobs
+        uint32_t * singCnt;    // n + 1
+        uint32_t * regCnt;     // n + 1
+        uint32_t * singOff;    // n + 1
+        uint32_t * regOff;     // n + 1
 
         // probes, final order (singular first)
         int4 *     probeIds;  // capProbes: output ids
@@ -93,8 +96,8 @@ namespace sesgb
     void launch_neighbors( const Build & b, cudaStream_t s );
     void launch_visibility( const Build & b, cudaStream_t s );
     void launch_emit( const Build & b, cudaStream_t s );
-    void launch_candidates( const Build & b, bool write, cudaStream_t s );
-    void launch_triplets( const Build & b, cudaStream_t s );
+    void launch_probes( const Build & b, cudaStream_t s );
+    void launch_probe_jobs( const Build & b, cudaStream_t s );
     void launch_place( const Build & b, cudaStream_t s );
     void launch_lists( const Build & b, cudaStream_t s );
     void launch_segment_counts( const Build & b, cudaStream_t s );
@@ -103,5 +106,6 @@ namespace sesgb
     void launch_tori( const Build & b, cudaStream_t s );
     void launch_tori_emit( const Build & b, cudaStream_t s );
     cudaError_t configure_kernels( const Build & b );
+    uint64_t    launch_count();
     void launch_reference_fill( const Build & b, uint32_t * globalToTrimmed, cudaStream_t s );
 } // namespace sesgb
