@@ -27,6 +27,7 @@ extern "C" {
 #define SESGB_ERR_NOT_BUILT -4 /* results requested before a build */
 #define SESGB_ERR_TIMEOUT -5   /* a bounded device wait gave up */
 #define SESGB_ERR_MODE -6      /* request does not match the context's mode */
+#define SESGB_ERR_TOO_LARGE -7 /* input larger than the no-allocation entry point's fixed scratch holds */
 
 #define SESGB_MODE_FULL 0     /* bcs::Sesdf */
 #define SESGB_MODE_EXTERIOR 1 /* bcs::Ssesdf */
@@ -182,6 +183,25 @@ uint16_t sesgb_max_intersection_neighbors( const sesgb_ctx * ctx );
  * The per-stage timers mirror app/detailed/sesdf_benchmark.inl of the reference. */
 int          sesgb_stage_times( sesgb_ctx * ctx, float * ms, uint32_t capacity, uint32_t * count );
 const char * sesgb_stage_name( uint32_t stage );
+
+/* No counterpart in the reference (it allocates on every build). Sorts n atoms
+ * (float4 x, y, z, vdW radius, device memory) into the order of the build's
+ * `atoms` output -- the reference grid's stable cell order for `aabb` (host,
+ * {min x, y, z, max x, y, z}) and `probe_radius` -- writing the sorted atoms and
+ * the sorted-to-input permutation to the caller's device buffers, without
+ * allocating any memory. It is for callers that cannot call cudaMalloc when
+ * they need the sort (a stream capture in progress, a host that owns a fixed
+ * device-memory budget, a loop that must not enter the allocator). Its scratch
+ * is a fixed array in this library's device image (about 3.3 MB on every GPU
+ * that loads the library, kept until the process exits), so n is limited to
+ * SESGB_NOALLOC_MAX_ATOMS (larger n: SESGB_ERR_TOO_LARGE, nothing launched).
+ * The first call on a device looks up the array's device address with that
+ * device current; make that first call before any stream capture. All calls on
+ * a device share the array: calls whose GPU work overlaps (other streams, other
+ * host threads) race on it and must be serialised by the caller. */
+#define SESGB_NOALLOC_MAX_ATOMS 262144u
+int sesgb_sort_atoms_noalloc( const void * device_atoms, uint32_t n, const float * aabb, float probe_radius,
+                              void * device_sorted_atoms, uint32_t * device_sorted_to_input, void * stream );
 
 /* Number of kernels this library has launched in this process (host-side count). */
 uint64_t sesgb_launch_count( void );

@@ -29,8 +29,9 @@ EXPORTS = [
     "sesgb_get_exterior", "sesgb_get_counts", "sesgb_atom_indices", "sesgb_analysis_buffer", "sesgb_copy_to_host",
     "sesgb_max_neighbor_per_atom", "sesgb_max_intersections_per_circle", "sesgb_max_intersection_neighbors",
     "sesgb_error_string", "sesgb_last_error", "sesgb_destroy", "sesgb_stage_times", "sesgb_stage_name",
-    "sesgb_launch_count", "sesgb_build_async", "sesgb_finish",
+    "sesgb_launch_count", "sesgb_build_async", "sesgb_finish", "sesgb_sort_atoms_noalloc",
 ]
+NOALLOC_MAX_ATOMS = 262144
 
 
 class SesgbError(RuntimeError):
@@ -109,6 +110,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         lib.sesgb_stage_times.argtypes = [P, P, U32, ctypes.POINTER(U32)]
         lib.sesgb_stage_name.argtypes = [U32]
         lib.sesgb_stage_name.restype = ctypes.c_char_p
+        lib.sesgb_sort_atoms_noalloc.argtypes = [P, U32, P, F32, P, P, P]
         lib.sesgb_build_async.argtypes = [P, P, P]
         lib.sesgb_finish.argtypes = [P]
         lib.sesgb_launch_count.argtypes = []

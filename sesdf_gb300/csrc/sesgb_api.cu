@@ -63,7 +63,7 @@ struct sesgb_ctx
 namespace
 {
     const char * kStatusNames[] = { "ok", "invalid argument", "CUDA error", "capacity overflow", "not built", "timeout",
-                                    "wrong mode" };
+                                    "wrong mode", "input exceeds the no-allocation limit (SESGB_NOALLOC_MAX_ATOMS)" };
 
     bool cuda_ok( sesgb_ctx * c, cudaError_t e, const char * what )
     {
