@@ -204,6 +204,7 @@ namespace
         b.clist       = dalloc<uint32_t>( c, L, 3 * PR, ok );
         b.segCnt      = dalloc<uint32_t>( c, L, C1 + 1, ok );
         b.segOff      = dalloc<uint32_t>( c, L, C1 + 1, ok );
+        b.segList     = dalloc<uint32_t>( c, L, C1 + 1, ok );
         b.segments    = dalloc<uint4>( c, L, b.capSeg, ok );
         b.torPos      = dalloc<float4>( c, L, b.capTori, ok );
         b.torAxis     = dalloc<float4>( c, L, b.capTori, ok );
@@ -623,7 +624,7 @@ extern "C"
         o->truncated_probe_neighbors    = h.snbrTruncated;
         o->degenerate_tori              = h.torusDegenerate;
         o->outside_atoms                = h.outside;
-        for ( int k = 0; k < 5; k++ )
+        for ( int k = 0; k < 6; k++ )
             o->fp64_decisions[ k ] = h.fp64[ k ];
         o->rebuilds = c->rebuilds;
         return SESGB_OK;

@@ -33,7 +33,8 @@ namespace sesgb
         uint32_t staged;     // probes written to the staging chunks
         uint32_t regTotal;   // regular (non-singular) probes
         uint32_t jobs;       // double-precision probe jobs
-        uint32_t pad[ 2 ];
+        uint32_t segCircles; // circles carrying at least two probes
+        uint32_t pad[ 1 ];
     };
 
     enum Overflow : uint32_t
@@ -57,7 +58,8 @@ namespace sesgb
         kFp64Visibility,
         kFp64Occlusion,
         kFp64SingularNbr,
-        kFp64Solve, // probe candidates whose float32 screen hit the band
+        kFp64Solve,    // probe candidates whose float32 screen hit the band
+        kFp64Segments, // circles whose float32 angle order was ambiguous
         kFp64Count
     };
 

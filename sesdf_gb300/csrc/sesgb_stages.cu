@@ -265,10 +265,15 @@ namespace sesgb
         }
 
         // ---- circle visibility ----------------------------------------------
-        // Status of the directed circle (i, slot s): float32 filter per k, double
-        // precision for the k whose margin is inside the band.
-        __device__ uint8_t circle_status( const Build & b, uint32_t i, const float4 & ai, const float4 * rel, uint32_t ni,
-                                          uint32_t s, uint32_t & fp64 )
+        constexpr int kBandSlots = 8; // band tests a lane defers per circle to the warp's double-precision pass
+
+        // Float32 pass over the k of circle (i, slot s). Decided tests update
+        // buried/touched; tests inside the band are queued (up to kBandSlots) for
+        // the warp-cooperative double-precision pass, further ones are decided
+        // here in double precision.
+        __device__ void circle_screen( const Build & b, uint32_t i, const float4 & ai, const float4 * rel, uint32_t ni,
+                                       uint32_t s, bool & buried, bool & touched, uint16_t * queue, uint32_t & nq,
+                                       uint32_t & fp64 )
         {
             const float  Ri = ai.w + b.rp;
             const float4 q  = rel[ s ];
@@ -284,9 +289,8 @@ namespace sesgb
             // sqrt of a negative number (NaN) and every test of the circle is
             // false; the double-precision twin decides whether that happens
             const bool   tangent = r2raw <= 4.f * kRel * Ri * Ri;
-
-            bool    buried = false, touched = false, haveD = false;
-            dcircle dc;
+            buried = touched = false;
+            nq               = 0;
             for ( uint32_t k = 0; k < ni; k++ )
             {
                 if ( k == s )
@@ -328,33 +332,35 @@ namespace sesgb
                     decided = false;
                 if ( !decided )
                 {
-                    if ( !haveD )
+                    if ( nq < (uint32_t)kBandSlots )
                     {
-                        const uint32_t j  = b.nbr[ (size_t)i * b.cap + s ];
-                        const float4   aj = b.atoms[ j ];
-                        dc                = dcircle_geometry( D3( ai ), ai.w, D3( aj ), aj.w, (double)b.rp );
-                        haveD             = true;
+                        queue[ nq++ ] = (uint16_t)k;
+                        continue;
                     }
-                    const uint32_t kid = b.nbr[ (size_t)i * b.cap + k ];
-                    const float4   ak  = b.atoms[ kid ];
-                    const int      r   = dcircle_vs_atom( dc, D3( ak ), __dadd_rn( (double)ak.w, (double)b.rp ) );
-                    bk                 = r & 1;
-                    tk                 = r & 2;
+                    const uint32_t j  = b.nbr[ (size_t)i * b.cap + s ];
+                    const float4   aj = b.atoms[ j ];
+                    const dcircle  dc = dcircle_geometry( D3( ai ), ai.w, D3( aj ), aj.w, (double)b.rp );
+                    const float4   ak = b.atoms[ b.nbr[ (size_t)i * b.cap + k ] ];
+                    const int      r  = dcircle_vs_atom( dc, D3( ak ), __dadd_rn( (double)ak.w, (double)b.rp ) );
+                    bk                = r & 1;
+                    tk                = r & 2;
                     fp64++;
                 }
                 touched = touched || tk;
                 if ( bk )
                 {
                     buried = true;
-                    break;
+                    nq     = 0; // buried: the deferred tests cannot change the status
+                    return;
                 }
             }
-            return buried ? 0 : ( touched ? 1 : 2 );
         }
 
-        __global__ void __launch_bounds__( 32 * kWarpsPerBlock ) k_visibility( Build b )
+        __global__ void __launch_bounds__( 32 * kWarpsPerBlock, 4 ) k_visibility( Build b )
         {
             extern __shared__ float4 smem[];
+            __shared__ uint16_t      bandQ[ kWarpsPerBlock ][ 32 ][ kBandSlots ];
+            __shared__ uint32_t      bandRes[ kWarpsPerBlock ][ 32 ];
             const uint32_t           warp = threadIdx.x >> 5, lane = lane_id();
             const uint32_t           i    = blockIdx.x * kWarpsPerBlock + warp;
             if ( i >= b.n )
@@ -369,12 +375,54 @@ namespace sesgb
             }
             __syncwarp();
             uint32_t vis = 0, part = 0, full = 0, fp64 = 0;
-            for ( uint32_t s = lane; s < ni; s += 32 )
+            for ( uint32_t base = 0; base < ni; base += 32 )
             {
-                const uint32_t j  = b.nbr[ (size_t)i * b.cap + s ];
-                uint8_t        st = 0;
-                if ( b.mode == 0 || i < j )
-                    st = circle_status( b, i, ai, rel, ni, s, fp64 );
+                const uint32_t s      = base + lane;
+                const bool     active = s < ni;
+                const uint32_t j      = active ? b.nbr[ (size_t)i * b.cap + s ] : 0u;
+                const bool     eval   = active && ( b.mode == 0 || i < j );
+                bool           buried = false, touched = false;
+                uint32_t       nq     = 0;
+                if ( eval )
+                    circle_screen( b, i, ai, rel, ni, s, buried, touched, bandQ[ warp ][ lane ], nq, fp64 );
+                // warp-cooperative double precision for the deferred tests of this round
+                bandRes[ warp ][ lane ] = 0;
+                uint32_t       total;
+                const uint32_t first = warp_exclusive_sum( nq, total );
+                __syncwarp();
+                for ( uint32_t t0 = 0; t0 < total; t0 += 32 )
+                {
+                    const uint32_t t = t0 + lane;
+                    // owner lane of job t: the last lane whose first job index is <= t
+                    uint32_t owner = 0;
+                    for ( int o = 0; o < 32; o++ )
+                    {
+                        const uint32_t fo = __shfl_sync( 0xffffffffu, first, o );
+                        const uint32_t no = __shfl_sync( 0xffffffffu, nq, o );
+                        if ( no > 0 && fo <= t )
+                            owner = (uint32_t)o;
+                    }
+                    const uint32_t fOwner = __shfl_sync( 0xffffffffu, first, owner );
+                    if ( t < total )
+                    {
+                        const uint32_t k  = bandQ[ warp ][ owner ][ t - fOwner ];
+                        const uint32_t so = base + owner;
+                        const float4   aj = b.atoms[ b.nbr[ (size_t)i * b.cap + so ] ];
+                        const dcircle  dc = dcircle_geometry( D3( ai ), ai.w, D3( aj ), aj.w, (double)b.rp );
+                        const float4   ak = b.atoms[ b.nbr[ (size_t)i * b.cap + k ] ];
+                        const int      r  = dcircle_vs_atom( dc, D3( ak ), __dadd_rn( (double)ak.w, (double)b.rp ) );
+                        if ( r )
+                            atomicOr( &bandRes[ warp ][ owner ], (uint32_t)r );
+                    }
+                }
+                __syncwarp();
+                fp64 += total > lane ? ( total - lane + 31 ) / 32 : 0;
+                if ( !active )
+                    continue;
+                const uint32_t r = bandRes[ warp ][ lane ];
+                buried           = buried || ( r & 1 );
+                touched          = touched || ( r & 2 );
+                const uint8_t st = eval ? ( buried ? 0 : ( touched ? 1 : 2 ) ) : 0;
                 b.status[ (size_t)i * b.cap + s ] = st;
                 vis += st != 0;
                 part += ( st == 1 && i < j );
@@ -584,38 +632,40 @@ namespace sesgb
         constexpr int kCandBuf    = 64;  // candidates queued per warp
         constexpr int kProbeBuf   = 128; // probes of one atom (the reference's per-block buffer, operations.inl:248)
 
+        // Per-warp staging of atom i's neighbourhood. For a point x on the SAS
+        // sphere of i (|x| = R_i in coordinates relative to i), x lies inside the
+        // SAS sphere of neighbour l exactly when x . d_l > K_l with
+        // K_l = (R_i^2 + |d_l|^2 - R_l^2) / 2: the occlusion test is one plane test.
         struct ProbeSmem
         {
-            float4 *   rel;  // cap: neighbour centre - centre of i, R of the neighbour
-            uint32_t * nid;  // cap: neighbour ids
+            float4 *   rel;   // cap: d_l (neighbour centre - centre of i), K_l
+            float *    rad;   // cap: R_l (vdW radius + probe radius)
+            uint32_t * nid;   // cap: neighbour ids
             uint16_t * plist; // cap: slots of the partial circles (i, j), i < j
-            uint2 *    cand; // kCandBuf: (slot j | slot k << 16, slot of k in N(j))
-            float4 *   ppos; // kProbeBuf
-            int4 *     pcid; // kProbeBuf
-            int4 *     pids; // kProbeBuf
+            uint8_t *  full;  // cap: 1 if the neighbour list of that neighbour may be truncated
+            uint32_t * cand;  // kCandBuf: slot j | slot k << 16
+            uint2 *    ent;   // kProbeBuf: (slot j | slot k << 16, side | kind << 1 | (w + 4) << 2)
         };
 
         __host__ __device__ inline size_t probe_smem_per_warp( uint32_t cap )
         {
-            size_t b = (size_t)cap * ( 16 + 4 + 2 );
+            size_t b = (size_t)cap * ( 16 + 4 + 4 + 2 + 1 );
             b        = ( b + 15 ) & ~(size_t)15;
-            return b + kCandBuf * 8 + kProbeBuf * ( 16 + 16 + 16 );
+            return b + kCandBuf * 4 + kProbeBuf * 8;
         }
 
         __device__ inline ProbeSmem probe_smem( unsigned char * base, uint32_t cap )
         {
             ProbeSmem m;
-            m.rel   = reinterpret_cast<float4 *>( base );
-            m.nid   = reinterpret_cast<uint32_t *>( base + (size_t)cap * 16 );
-            m.plist = reinterpret_cast<uint16_t *>( base + (size_t)cap * 20 );
-            size_t o = ( (size_t)cap * 22 + 15 ) & ~(size_t)15;
-            m.cand  = reinterpret_cast<uint2 *>( base + o );
-            o += kCandBuf * 8;
-            m.ppos = reinterpret_cast<float4 *>( base + o );
-            o += kProbeBuf * 16;
-            m.pcid = reinterpret_cast<int4 *>( base + o );
-            o += kProbeBuf * 16;
-            m.pids = reinterpret_cast<int4 *>( base + o );
+            m.rel    = reinterpret_cast<float4 *>( base );
+            m.rad    = reinterpret_cast<float *>( base + (size_t)cap * 16 );
+            m.nid    = reinterpret_cast<uint32_t *>( base + (size_t)cap * 20 );
+            m.plist  = reinterpret_cast<uint16_t *>( base + (size_t)cap * 24 );
+            m.full   = reinterpret_cast<uint8_t *>( base + (size_t)cap * 26 );
+            size_t o = ( (size_t)cap * 27 + 15 ) & ~(size_t)15;
+            m.cand   = reinterpret_cast<uint32_t *>( base + o );
+            o += kCandBuf * 4;
+            m.ent = reinterpret_cast<uint2 *>( base + o );
             return m;
         }
 
@@ -649,20 +699,54 @@ namespace sesgb
             kJobBand = 1, // the float32 screen hit the band: solve, occlusion and flags in double precision
         };
 
+        // Bounds of atom i's staged neighbourhood that size the error bands of the
+        // float32 screens: the largest |d_l| and |d_l|^2 and the half-width of the
+        // plane-test band due to rounding (kRel (R_i^2 + |d_l|^2 + R_l^2 + 1) / 2).
+        struct ProbeBounds
+        {
+            float dmax, d2max, eK;
+        };
+
+        // Is k (slot sk) in the neighbour list of j (slot sj)? The lists hold every
+        // atom that satisfies the neighbour predicate (k_neighbors decides it
+        // exactly), in ascending order, cut at the capacity: for a list that is
+        // not full the predicate itself answers, with the double-precision twin
+        // inside the band; a full list is searched.
+        __device__ __forceinline__ bool pair_is_neighbor( const Build & b, const ProbeSmem & m, const ProbeBounds & pb,
+                                                          uint32_t sj, uint32_t sk, uint32_t & fp64 )
+        {
+            const uint32_t j = m.nid[ sj ], k = m.nid[ sk ];
+            if ( m.full[ sj ] )
+                return find_in_row( b.nbr + (size_t)j * b.cap, b.nbrCount[ j ], k ) >= 0;
+            const float4 qj = m.rel[ sj ], qk = m.rel[ sk ];
+            const f3     v  = F3( qj.x - qk.x, qj.y - qk.y, qj.z - qk.z );
+            const float  d  = dot( v, v );
+            const float  R  = m.rad[ sj ] + m.rad[ sk ];
+            const float  mm = d - R * R - 1e-4f;
+            // the float32 difference of two relative positions adds at most a few
+            // ulps of |d_j| + |d_k| to v: covered by the d2max term
+            const float e = kRel * ( d + R * R + pb.d2max + 1.f );
+            if ( mm < -e )
+                return true;
+            if ( mm > e )
+                return false;
+            fp64++;
+            const float4 aj = b.atoms[ j ], ak = b.atoms[ k ];
+            return dneighbor( D3( aj ), aj.w, D3( ak ), ak.w, (double)b.rp );
+        }
+
         // One (i, j, k) candidate, float32 screen in coordinates relative to atom i
-        // with a conservative error band. Returns the number of entries it needs in
-        // the atom's probe list: 0 (no kept point), 1 or 2 (kept sides, decided), or
-        // 2 with band = true (both entries reserved for the double-precision pass).
-        // w[e]: 0 none, +-1 regular, +-2 singular, +-3 kept with the singular flag undecided.
-        __device__ void probe_screen( const Build & b, const float4 & ai, const ProbeSmem & m, uint32_t ni, uint32_t sj,
-                                      uint32_t sk, int w[ 2 ], bool & band )
+        // with a conservative error band. Sets w[e]: 0 none, +-1 regular, +-2
+        // singular, +-3 kept with the singular flag undecided; or band = true
+        // (both entries reserved for the double-precision pass).
+        __device__ __forceinline__ void probe_screen( const ProbeSmem & m, const ProbeBounds & pb, float Ri, float rp,
+                                                      uint32_t ni, uint32_t sj, uint32_t sk, int w[ 2 ], bool & band )
         {
             const float4 qj = m.rel[ sj ], qk = m.rel[ sk ];
-            const float  Ri = ai.w + b.rp, Rj = qj.w, Rk = qk.w;
             const f3     dj = F3( qj.x, qj.y, qj.z ), dk = F3( qk.x, qk.y, qk.z );
             const float  dJ = dot( dj, dj ), dK = dot( dk, dk );
-            const f3     cJ = dj * ( ( Ri * Ri - Rj * Rj + dJ ) / ( 2.f * dJ ) );
-            const f3     cK = dk * ( ( Ri * Ri - Rk * Rk + dK ) / ( 2.f * dK ) );
+            const f3     cJ = dj * ( qj.w / dJ ); // (R_i^2 - R_j^2 + |d_j|^2) / (2 |d_j|^2) = K_j / |d_j|^2
+            const f3     cK = dk * ( qk.w / dK );
             const f3     nJ = dj * rsqrtf( dJ );
             const f3     nK = dk * rsqrtf( dK );
             const f3     u  = nK - nJ * dot( nK, nJ );
@@ -686,47 +770,44 @@ namespace sesgb
             const float root = sqrtf( tt );
             const f3    nn   = normalize( cross( nJ, nK ) );
             const float ep   = ex + et / ( 2.f * root ) + root * kSolve / sqrtf( den );
-            const f3    x1   = xc + nn * root;
-            const f3    x2   = xc - nn * root;
-            bool        vis[ 2 ] = { true, true };
-            for ( uint32_t sl = 0; sl < ni && ( vis[ 0 ] || vis[ 1 ] ); sl++ )
+            // x1,2 = xc +- root nn lie within ep of the exact points: a plane test
+            // moves by at most ep |d_l|, rounding by at most eK
+            const float eh = ep * pb.dmax + pb.eK;
+            bool        v1 = true, v2 = true;
+            for ( uint32_t sl = 0; sl < ni; sl++ )
             {
                 if ( sl == sj || sl == sk )
                     continue;
-                const float4 ql  = m.rel[ sl ];
-                const float  Rl2 = ql.w * ql.w;
-#pragma unroll
-                for ( int e = 0; e < 2; e++ )
+                const float4 ql = m.rel[ sl ];
+                const float  a  = ql.w - ( xc.x * ql.x + xc.y * ql.y + xc.z * ql.z );
+                const float  c  = root * ( nn.x * ql.x + nn.y * ql.y + nn.z * ql.z );
+                const float  h1 = a - c, h2 = a + c; // K_l - x . d_l for x1 and x2
+                if ( ( v1 && fabsf( h1 ) <= eh ) || ( v2 && fabsf( h2 ) <= eh ) || ( v1 && h1 != h1 ) || ( v2 && h2 != h2 ) )
                 {
-                    if ( !vis[ e ] )
-                        continue;
-                    const f3    xe = e == 0 ? x1 : x2;
-                    const f3    ev = F3( ql.x - xe.x, ql.y - xe.y, ql.z - xe.z );
-                    const float ee = dot( ev, ev );
-                    const float mm = ee - Rl2;
-                    const float em = 2.f * sqrtf( ee ) * ep + ep * ep + kRel * ( ee + Rl2 + 1.f );
-                    if ( mm < -em )
-                        vis[ e ] = false;
-                    else if ( !( mm > em ) )
-                    {
-                        band = true;
-                        return;
-                    }
+                    band = true;
+                    return;
                 }
+                v1 = v1 && h1 > 0.f;
+                v2 = v2 && h2 > 0.f;
+                if ( !( v1 || v2 ) )
+                    return;
             }
-            for ( int e = 0; e < 2; e++ )
-                if ( vis[ e ] )
-                {
-                    const int sg = singular_f( dj, dk, e == 0 ? x1 : x2, ep, b.rp );
-                    w[ e ]       = ( e == 0 ? 1 : -1 ) * ( sg < 0 ? 3 : 1 + sg );
-                }
+            if ( v1 )
+            {
+                const int sg = singular_f( dj, dk, xc + nn * root, ep, rp );
+                w[ 0 ]       = sg < 0 ? 3 : 1 + sg;
+            }
+            if ( v2 )
+            {
+                const int sg = singular_f( dj, dk, xc - nn * root, ep, rp );
+                w[ 1 ]       = -( sg < 0 ? 3 : 1 + sg );
+            }
         }
 
-        // Warp per atom i: the partial circles (i, j), i < j, paired with every
-        // later partial circle (i, k) whose k is a neighbour of j. Entries of the
-        // atom's probe list are kept in order (circle (i, j), then k, then x1
-        // before x2) and written as one chunk; positions and undecided flags are
-        // completed by k_probe_jobs.
+        // Warp per atom i: every pair of partial circles (i, j), (i, k), i < j < k,
+        // whose far atoms are neighbours. Entries of the atom's probe list are kept
+        // in order (circle (i, j), then k, then x1 before x2) and written as one
+        // chunk; positions and undecided flags are completed by k_probe_jobs.
         __global__ void __launch_bounds__( 32 * kProbeWarps ) k_probes( Build b )
         {
             extern __shared__ __align__( 16 ) unsigned char smemRaw[];
@@ -734,12 +815,14 @@ namespace sesgb
             const uint32_t i    = blockIdx.x * kProbeWarps + warp;
             if ( i >= b.n )
                 return;
-            const ProbeSmem m  = probe_smem( smemRaw + warp * probe_smem_per_warp( b.cap ), b.cap );
-            const uint32_t  ni = b.nbrCount[ i ];
-            const float4    ai = b.atoms[ i ];
+            const ProbeSmem m   = probe_smem( smemRaw + warp * probe_smem_per_warp( b.cap ), b.cap );
+            const uint32_t  ni  = b.nbrCount[ i ];
+            const float4    ai  = b.atoms[ i ];
+            const float     Ri  = ai.w + b.rp;
             const size_t    row = (size_t)i * b.cap;
 
             uint32_t p = 0;
+            float    d2max = 0.f, bmax = 0.f;
             for ( uint32_t base = 0; base < ni; base += 32 )
             {
                 const uint32_t s   = base + lane;
@@ -748,18 +831,34 @@ namespace sesgb
                 {
                     const uint32_t j  = b.nbr[ row + s ];
                     const float4   aj = b.atoms[ j ];
-                    m.rel[ s ]        = make_float4( aj.x - ai.x, aj.y - ai.y, aj.z - ai.z, aj.w + b.rp );
+                    const f3       d  = F3( aj.x - ai.x, aj.y - ai.y, aj.z - ai.z );
+                    const float    dd = dot( d, d );
+                    const float    Rl = aj.w + b.rp;
+                    m.rel[ s ]        = make_float4( d.x, d.y, d.z, 0.5f * ( ( Ri * Ri + dd ) - Rl * Rl ) );
+                    m.rad[ s ]        = Rl;
                     m.nid[ s ]        = j;
+                    m.full[ s ]       = b.nbrCount[ j ] >= b.cap;
                     isP               = b.status[ row + s ] == 1 && i < j;
+                    d2max             = fmaxf( d2max, dd );
+                    bmax              = fmaxf( bmax, Ri * Ri + dd + Rl * Rl );
                 }
                 const uint32_t mk = __ballot_sync( 0xffffffffu, isP );
                 if ( isP )
                     m.plist[ p + __popc( mk & lanemask_lt() ) ] = (uint16_t)s;
                 p += __popc( mk );
             }
+            for ( int o = 16; o > 0; o >>= 1 )
+            {
+                d2max = fmaxf( d2max, __shfl_xor_sync( 0xffffffffu, d2max, o ) );
+                bmax  = fmaxf( bmax, __shfl_xor_sync( 0xffffffffu, bmax, o ) );
+            }
+            ProbeBounds pb;
+            pb.d2max = d2max;
+            pb.dmax  = sqrtf( d2max ) * ( 1.f + kRel );
+            pb.eK    = 0.5f * kRel * ( bmax + 1.f );
             __syncwarp();
 
-            uint32_t       nCand = 0, nEnt = 0, nSing = 0, nReg = 0, cands = 0;
+            uint32_t       nCand = 0, nEnt = 0, nSing = 0, nReg = 0, cands = 0, fp64 = 0;
             const uint32_t pairs = p * ( p > 0 ? p - 1 : 0 ) / 2;
             for ( uint32_t q0 = 0; q0 < pairs || nCand > 0; q0 += 32 )
             {
@@ -768,7 +867,7 @@ namespace sesgb
                     // pair q = (a, bb), a < bb, row-major over the partial circles
                     const uint32_t q   = q0 + lane;
                     bool           isC = false;
-                    uint32_t       sj = 0, sk = 0, sjk = 0;
+                    uint32_t       sj = 0, sk = 0;
                     if ( q < pairs )
                     {
                         const float tp = 2.f * p - 1.f;
@@ -781,14 +880,11 @@ namespace sesgb
                         const uint32_t bb = (uint32_t)a + 1 + ( q - (uint32_t)( a * ( 2 * (int)p - a - 1 ) / 2 ) );
                         sj                = m.plist[ a ];
                         sk                = m.plist[ bb ];
-                        const uint32_t j  = m.nid[ sj ];
-                        const int      r  = find_in_row( b.nbr + (size_t)j * b.cap, b.nbrCount[ j ], m.nid[ sk ] );
-                        isC               = r >= 0;
-                        sjk               = (uint32_t)r;
+                        isC               = pair_is_neighbor( b, m, pb, sj, sk, fp64 );
                     }
                     const uint32_t mc = __ballot_sync( 0xffffffffu, isC );
                     if ( isC )
-                        m.cand[ nCand + __popc( mc & lanemask_lt() ) ] = make_uint2( sj | ( sk << 16 ), sjk );
+                        m.cand[ nCand + __popc( mc & lanemask_lt() ) ] = sj | ( sk << 16 );
                     nCand += __popc( mc );
                     cands += __popc( mc );
                 }
@@ -799,54 +895,35 @@ namespace sesgb
                     const uint32_t batch = nCand < 32 ? nCand : 32;
                     int            w[ 2 ] = { 0, 0 };
                     bool           band   = false;
-                    uint32_t       sj = 0, sk = 0, sjk = 0;
+                    uint32_t       sjk    = 0;
                     if ( lane < batch )
                     {
-                        const uint2 cd = m.cand[ lane ];
-                        sj             = cd.x & 0xffffu;
-                        sk             = cd.x >> 16;
-                        sjk            = cd.y;
-                        probe_screen( b, ai, m, ni, sj, sk, w, band );
+                        sjk = m.cand[ lane ];
+                        probe_screen( m, pb, Ri, b.rp, ni, sjk & 0xffffu, sjk >> 16, w, band );
                     }
                     const uint32_t need = band ? 2u : ( w[ 0 ] != 0 ) + ( w[ 1 ] != 0 );
                     uint32_t       tot;
-                    uint32_t       at   = nEnt + warp_exclusive_sum( need, tot );
-                    if ( need )
+                    uint32_t       at = nEnt + warp_exclusive_sum( need, tot );
+                    for ( int e = 0; e < 2 && need; e++ )
                     {
-                        const uint32_t j = m.nid[ sj ], k = m.nid[ sk ];
-                        const int4     ids = make_int4( (int)i, (int)j, (int)k, 0 );
-                        int4           cid;
-                        if ( b.mode == 0 )
-                            cid = make_int4( (int)b.slotTrim[ row + sj ], (int)b.slotTrim[ (size_t)j * b.cap + sjk ], (int)b.slotTrim[ row + sk ], 0 );
-                        else
-                            cid = make_int4( (int)( row + sj ), (int)( row + sk ), (int)( (size_t)j * b.cap + sjk ), 0 );
-                        for ( int e = 0; e < 2; e++ )
+                        if ( !band && w[ e ] == 0 )
+                            continue;
+                        if ( at < (uint32_t)kProbeBuf )
+                            m.ent[ at ] = make_uint2( sjk, (uint32_t)e | ( ( band ? kJobBand : kJobFill ) << 1 ) |
+                                                               ( (uint32_t)( ( band ? 0 : w[ e ] ) + 4 ) << 2 ) );
+                        if ( !band )
                         {
-                            if ( !band && w[ e ] == 0 )
-                                continue;
-                            if ( at < (uint32_t)kProbeBuf )
-                            {
-                                cid.w        = band ? 0 : w[ e ];
-                                m.pcid[ at ] = cid;
-                                m.pids[ at ] = ids;
-                                // job description: slots, side, kind (entry index added when written out)
-                                m.ppos[ at ] = make_float4( __uint_as_float( sj | ( sk << 16 ) ), __uint_as_float( sjk ),
-                                                            __uint_as_float( (uint32_t)e | ( ( band ? kJobBand : kJobFill ) << 8 ) ), 0.f );
-                            }
-                            if ( !band )
-                            {
-                                const int aw = w[ e ] < 0 ? -w[ e ] : w[ e ];
-                                nSing += aw == 2;
-                                nReg += aw == 1;
-                            }
-                            at++;
+                            const int aw = w[ e ] < 0 ? -w[ e ] : w[ e ];
+                            nSing += aw == 2;
+                            nReg += aw == 1;
                         }
+                        at++;
                     }
                     nEnt += tot;
                     // drop the processed batch from the queue
                     __syncwarp();
                     const uint32_t rest = nCand - batch;
-                    uint2          keep[ 2 ];
+                    uint32_t       keep[ 2 ];
                     for ( uint32_t r = 0; r < 2; r++ )
                         if ( lane + 32 * r < rest )
                             keep[ r ] = m.cand[ batch + lane + 32 * r ];
@@ -862,10 +939,11 @@ namespace sesgb
             {
                 nSing += __shfl_xor_sync( 0xffffffffu, nSing, o );
                 nReg += __shfl_xor_sync( 0xffffffffu, nReg, o );
+                fp64 += __shfl_xor_sync( 0xffffffffu, fp64, o );
             }
             __syncwarp();
             // one chunk per atom; one double-precision job per kept side or band candidate
-            const uint32_t kept = nEnt < (uint32_t)kProbeBuf ? nEnt : (uint32_t)kProbeBuf;
+            const uint32_t kept  = nEnt < (uint32_t)kProbeBuf ? nEnt : (uint32_t)kProbeBuf;
             uint32_t       chunk = 0;
             if ( lane == 0 )
             {
@@ -874,15 +952,11 @@ namespace sesgb
                 chunk = kept ? atomicAdd( &b.counts->staged, kept ) : 0u;
                 if ( cands )
                     atomicAdd( &b.counts->cand, cands );
+                if ( fp64 )
+                    atomicAdd( &b.counts->fp64[ kFp64Neighbor ], fp64 );
             }
             chunk           = __shfl_sync( 0xffffffffu, chunk, 0 );
             const bool fits = chunk + kept <= b.capProbes;
-            for ( uint32_t q = lane; q < kept && fits; q += 32 )
-            {
-                b.stageCid[ chunk + q ] = m.pcid[ q ];
-                b.stageIds[ chunk + q ] = m.pids[ q ];
-                b.stagePos[ chunk + q ] = make_float4( 0.f, 0.f, 0.f, 0.f );
-            }
             // jobs: a fill entry is one job; a band candidate's two entries are one job (on its first entry)
             uint32_t jobsHere = 0;
             for ( uint32_t q0 = 0; q0 < kept; q0 += 32 )
@@ -891,8 +965,8 @@ namespace sesgb
                 bool           isJob = false;
                 if ( q < kept && fits )
                 {
-                    const uint32_t info = __float_as_uint( m.ppos[ q ].z );
-                    isJob               = ( info >> 8 ) == kJobFill || ( info & 0xffu ) == 0u;
+                    const uint32_t info = m.ent[ q ].y;
+                    isJob               = ( ( info >> 1 ) & 1u ) == kJobFill || ( info & 1u ) == 0u;
                 }
                 jobsHere += __popc( __ballot_sync( 0xffffffffu, isJob ) );
             }
@@ -904,20 +978,33 @@ namespace sesgb
             {
                 const uint32_t q     = q0 + lane;
                 bool           isJob = false;
-                float4         jb    = make_float4( 0.f, 0.f, 0.f, 0.f );
+                uint2          en    = make_uint2( 0u, 0u );
                 if ( q < kept && fits )
                 {
-                    jb                  = m.ppos[ q ];
-                    const uint32_t info = __float_as_uint( jb.z );
-                    isJob               = ( info >> 8 ) == kJobFill || ( info & 0xffu ) == 0u;
+                    en                  = m.ent[ q ];
+                    const uint32_t sj   = en.x & 0xffffu, sk = en.x >> 16;
+                    const uint32_t side = en.y & 1u, kind = ( en.y >> 1 ) & 1u;
+                    const int      wv   = (int)( en.y >> 2 ) - 4;
+                    const uint32_t j = m.nid[ sj ], k = m.nid[ sk ];
+                    const uint32_t sjk  = (uint32_t)find_in_row( b.nbr + (size_t)j * b.cap, b.nbrCount[ j ], k );
+                    int4           cid;
+                    if ( b.mode == 0 )
+                        cid = make_int4( (int)b.slotTrim[ row + sj ], (int)b.slotTrim[ (size_t)j * b.cap + sjk ],
+                                         (int)b.slotTrim[ row + sk ], wv );
+                    else
+                        cid = make_int4( (int)( row + sj ), (int)( row + sk ), (int)( (size_t)j * b.cap + sjk ), wv );
+                    b.stageCid[ chunk + q ] = cid;
+                    b.stageIds[ chunk + q ] = make_int4( (int)i, (int)j, (int)k, 0 );
+                    b.stagePos[ chunk + q ] = make_float4( 0.f, 0.f, 0.f, 0.f );
+                    isJob                   = kind == kJobFill || side == 0u;
+                    en.y                    = side | ( kind << 8 );
                 }
                 const uint32_t mj = __ballot_sync( 0xffffffffu, isJob );
                 if ( isJob )
                 {
                     const uint32_t slot = jbase + __popc( mj & lanemask_lt() );
                     if ( slot < b.capProbes )
-                        b.jobs[ slot ] = make_uint4( chunk + q, i, __float_as_uint( jb.x ),
-                                                     ( __float_as_uint( jb.y ) & 0xffffu ) | ( ( __float_as_uint( jb.z ) & 0xffffu ) << 16 ) );
+                        b.jobs[ slot ] = make_uint4( chunk + q, i, en.x, en.y << 16 );
                 }
                 jbase += __popc( mj );
             }
@@ -1075,23 +1162,35 @@ namespace sesgb
             const uint32_t C1 = min( b.counts->C1, b.capC1 );
             for ( uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < C1; t += gridDim.x * blockDim.x )
             {
-                const uint32_t c = min( b.ccount[ t ], b.segCap );
-                b.segCnt[ t ]    = c / 2u;
-                if ( b.ccount[ t ] > b.segCap )
+                const uint32_t cc = b.ccount[ t ];
+                const uint32_t c  = min( cc, b.segCap );
+                b.segCnt[ t ]     = c / 2u;
+                if ( cc > b.segCap )
                     atomicAdd( &b.counts->segTruncated, 1u );
+                if ( cc >= 2 )
+                {
+                    // circles carrying segments, in any order (each writes at its own offset)
+                    const uint32_t at = atomicAdd( &b.counts->segCircles, 1u );
+                    if ( at < b.capC1 )
+                        b.segList[ at ] = t;
+                }
             }
         }
 
         // ---- segments (buildSegments, operations.inl:552-668) ---------------
+        constexpr float kKeyTol = 1.0f / 32768.0f; // 2^-15: float32 pseudo-angles closer than this go to double
+
+        // Orders the probes of circle t along the circle and writes its segments:
+        // float32 keys first; when two keys (or a key and the start) are closer than
+        // kKeyTol, or a side test is ambiguous, the double-precision keys decide.
         __global__ void __launch_bounds__( 128 ) k_segments( Build b )
         {
-            const uint32_t C1  = min( b.counts->C1, b.capC1 );
-            uint32_t       ovf = 0;
-            for ( uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < C1; t += gridDim.x * blockDim.x )
+            const uint32_t nc  = min( b.counts->segCircles, b.capC1 );
+            uint32_t       ovf = 0, fp64 = 0;
+            for ( uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < nc; idx += gridDim.x * blockDim.x )
             {
+                const uint32_t t   = b.segList[ idx ];
                 const uint32_t cnt = b.ccount[ t ];
-                if ( cnt < 2 )
-                    continue;
                 if ( cnt > (uint32_t)kSegBuf )
                 {
                     ovf |= kOverflowList;
@@ -1116,46 +1215,94 @@ namespace sesgb
                 const uint32_t i   = sIJ / b.cap;
                 const uint32_t j   = b.nbr[ sIJ ];
                 const float4   ai = b.atoms[ i ], aj = b.atoms[ j ];
-                const dcircle  geo = dcircle_geometry( D3( ai ), (double)ai.w, D3( aj ), (double)aj.w, (double)b.rp );
 
                 const uint32_t st          = lst[ 0 ];
                 const int4     sids        = b.probeIds[ st ];
                 const float4   spos        = b.probePos[ st ];
                 const bool     isSecondary = (int)i == sids.x && (int)j == sids.z;
-                const double   direction   = copysign( 1.0, (double)spos.w ) * ( isSecondary ? -1.0 : 1.0 );
-                const d3       ref         = dsub( D3( spos ), geo.center );
+                const bool     reverse     = ( spos.w < 0.f ) != isSecondary; // direction < 0
 
-                double  key[ kSegBuf ];
+                // float32 keys, coordinates relative to atom i
+                float   key[ kSegBuf ];
                 uint8_t ord[ kSegBuf ];
-                key[ 0 ] = 0.0;
-                ord[ 0 ] = 0;
-                for ( uint32_t m = 1; m < nb; m++ )
+                bool    exact = true;
                 {
-                    d3 v1 = ref;
-                    d3 v2 = dnrm( dsub( D3( b.probePos[ lst[ m ] ] ), geo.center ) );
-                    if ( direction < 0.0 )
+                    const float Ri = ai.w + b.rp, Rj = aj.w + b.rp;
+                    const f3    dj = F3( aj.x - ai.x, aj.y - ai.y, aj.z - ai.z );
+                    const float d  = dot( dj, dj );
+                    const f3    c  = dj * ( ( Ri * Ri - Rj * Rj + d ) / ( 2.f * d ) );
+                    const f3    n  = dj * rsqrtf( d );
+                    const f3    rf = F3( spos.x - ai.x, spos.y - ai.y, spos.z - ai.z ) - c;
+                    key[ 0 ]       = 0.f;
+                    ord[ 0 ]       = 0;
+                    for ( uint32_t m = 1; m < nb && exact; m++ )
                     {
-                        const d3 tmp = v1;
-                        v1           = v2;
-                        v2           = tmp;
+                        const float4 pm = b.probePos[ lst[ m ] ];
+                        f3           v1 = rf;
+                        f3           v2 = normalize( F3( pm.x - ai.x, pm.y - ai.y, pm.z - ai.z ) - c );
+                        if ( reverse )
+                        {
+                            const f3 tmp = v1;
+                            v1           = v2;
+                            v2           = tmp;
+                        }
+                        const float l   = sqrtf( dot( v1, v1 ) * dot( v2, v2 ) );
+                        const float cs  = fmaxf( -1.f, fminf( dot( v1, v2 ) / l, 1.f ) );
+                        const float det = dot( v1, cross( v2, n ) ) / l;
+                        // next to angle 0 the side test decides between key 0 and key 4
+                        if ( fabsf( det ) < kKeyTol && cs > 0.f )
+                            exact = false;
+                        const float kv = det > 0.f ? 1.f - cs : 3.f + cs;
+                        uint32_t    p  = m;
+                        while ( p > 0 && key[ p - 1 ] > kv )
+                        {
+                            key[ p ] = key[ p - 1 ];
+                            ord[ p ] = ord[ p - 1 ];
+                            p--;
+                        }
+                        key[ p ] = kv;
+                        ord[ p ] = (uint8_t)m;
                     }
-                    const double kv = dpseudo_angle( v1, v2, geo.normal );
-                    // stable insertion by (key, m)
-                    uint32_t p = m;
-                    while ( p > 0 && key[ p - 1 ] > kv )
+                    for ( uint32_t m = 1; m < nb && exact; m++ )
+                        if ( key[ m ] - key[ m - 1 ] < kKeyTol )
+                            exact = false;
+                }
+                if ( !exact )
+                {
+                    // double-precision keys (the oracle's), same stable ordering
+                    fp64++;
+                    const dcircle geo = dcircle_geometry( D3( ai ), (double)ai.w, D3( aj ), (double)aj.w, (double)b.rp );
+                    const d3      ref = dsub( D3( spos ), geo.center );
+                    double        dk[ kSegBuf ];
+                    dk[ 0 ]  = 0.0;
+                    ord[ 0 ] = 0;
+                    for ( uint32_t m = 1; m < nb; m++ )
                     {
-                        key[ p ] = key[ p - 1 ];
-                        ord[ p ] = ord[ p - 1 ];
-                        p--;
+                        d3 v1 = ref;
+                        d3 v2 = dnrm( dsub( D3( b.probePos[ lst[ m ] ] ), geo.center ) );
+                        if ( reverse )
+                        {
+                            const d3 tmp = v1;
+                            v1           = v2;
+                            v2           = tmp;
+                        }
+                        const double kv = dpseudo_angle( v1, v2, geo.normal );
+                        uint32_t     p  = m;
+                        while ( p > 0 && dk[ p - 1 ] > kv )
+                        {
+                            dk[ p ]  = dk[ p - 1 ];
+                            ord[ p ] = ord[ p - 1 ];
+                            p--;
+                        }
+                        dk[ p ]  = kv;
+                        ord[ p ] = (uint8_t)m;
                     }
-                    key[ p ] = kv;
-                    ord[ p ] = (uint8_t)m;
                 }
                 uint32_t out = b.segOff[ t ];
                 for ( uint32_t m = 0; m + 1 < nb; m += 2, out++ )
                 {
                     uint32_t a1 = lst[ ord[ m ] ], a2 = lst[ ord[ m + 1 ] ];
-                    if ( direction < 0.0 )
+                    if ( reverse )
                     {
                         const uint32_t tmp = a1;
                         a1                 = a2;
@@ -1169,6 +1316,8 @@ namespace sesgb
             }
             if ( ovf )
                 atomicOr( &b.counts->overflow, ovf );
+            if ( fp64 )
+                atomicAdd( &b.counts->fp64[ kFp64Segments ], fp64 );
         }
 
         // ---- neighbours of singular probes -------------------------------------

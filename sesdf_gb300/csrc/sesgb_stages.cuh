@@ -79,6 +79,7 @@ namespace sesgb
         uint32_t * clist;     // 3 capProbes
         uint32_t * segCnt;    // C1 + 1
         uint32_t * segOff;    // C1 + 1
+        uint32_t * segList;   // C1: circles with at least two probes
         uint4 *    segments;  // capSeg
 
         // exterior tori
