@@ -160,7 +160,9 @@ namespace
         b.cellCursor      = dalloc<uint32_t>( c, L, b.capCells + 1ull, ok );
         b.nbr             = dalloc<uint32_t>( c, L, n * b.cap, ok );
         b.nbrCount        = dalloc<uint32_t>( c, L, n + 1, ok );
-        b.status          = dalloc<uint8_t>( c, L, n * b.cap + 1, ok );
+        b.status          = dalloc<uint8_t>( c, L, n * b.cap + 4, ok );
+        b.capVisBand      = (uint32_t)std::max<size_t>( 1u << 16, 2 * n );
+        b.visBand         = dalloc<uint2>( c, L, b.capVisBand, ok );
         b.slotTrim        = dalloc<uint32_t>( c, L, n * b.cap, ok );
         uint32_t ** per[] = { &b.visCnt,  &b.partCnt, &b.fullCnt, &b.torCnt,  &b.visOff,    &b.partOff, &b.fullOff,
                               &b.torOff,  &b.singCnt, &b.regCnt,  &b.singOff, &b.regOff,    &b.chunkStart,
@@ -174,7 +176,7 @@ namespace
         c->radixScratch = dalloc<char>( c, L, radix_scratch_bytes( c->n ), ok );
         if ( ok )
         {
-            cudaMemset( b.status, 0, n * b.cap + 1 );
+            cudaMemset( b.status, 0, n * b.cap + 4 );
             cudaMemset( b.nbrCount, 0, sizeof( uint32_t ) * ( n + 1 ) );
         }
         return ok;

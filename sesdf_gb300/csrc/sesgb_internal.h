@@ -34,7 +34,7 @@ namespace sesgb
         uint32_t regTotal;   // regular (non-singular) probes
         uint32_t jobs;       // double-precision probe jobs
         uint32_t segCircles; // circles carrying at least two probes
-        uint32_t pad[ 1 ];
+        uint32_t visBand;    // visibility tests queued for double precision
     };
 
     enum Overflow : uint32_t

@@ -265,165 +265,308 @@ namespace sesgb
         }
 
         // ---- circle visibility ----------------------------------------------
-        constexpr int kBandSlots = 8; // band tests a lane defers per circle to the warp's double-precision pass
+        // Warp per atom i. The circles (i, s) are processed kVisCircles at a time,
+        // one group of kVisGroup lanes per circle, each lane testing the k of its
+        // residue class (k = lane in group + kVisGroup u). The neighbourhood is
+        // staged in shared memory as (d_k, K_k, |d_k|^2) relative to atom i; a test
+        // is then sqrt- and division-free: with t the axial offset of the circle
+        // (centre c = t d_j), g = d_j . d_k and p^2 = |d_k|^2 - g^2 / |d_j|^2 (k's
+        // distance from the circle axis, squared)
+        //     A = R_i^2 + |d_k|^2 - R_k^2 - 1e-4 - 2 t g      (= |c - d_k|^2 + r^2 - R_k^2 - 1e-4)
+        //     G = A^2 - 4 r^2 p^2,
+        // k holds the whole circle iff A < 0 and G > 0 and touches it iff A < 0
+        // or G < 0 (the two extremes A +- 2 r p of computeCirclesVisibilityStatus,
+        // operations.cu:164-197). Tests inside the float32 error band go to a
+        // queue that k_visibility_band decides in double precision with full
+        // warps; k_visibility_final turns the flags into statuses and counts.
+        constexpr int kVisGroup   = 8;              // lanes per circle
+        constexpr int kVisCircles = 32 / kVisGroup; // circles per warp step
+        constexpr int kVisQueue   = 128;            // band tests a warp holds before they go to the global queue
 
-        // Float32 pass over the k of circle (i, slot s). Decided tests update
-        // buried/touched; tests inside the band are queued (up to kBandSlots) for
-        // the warp-cooperative double-precision pass, further ones are decided
-        // here in double precision.
-        __device__ void circle_screen( const Build & b, uint32_t i, const float4 & ai, const float4 * rel, uint32_t ni,
-                                       uint32_t s, bool & buried, bool & touched, uint16_t * queue, uint32_t & nq,
-                                       uint32_t & fp64 )
+        // status flags between the three visibility kernels
+        enum : uint8_t
         {
-            const float  Ri = ai.w + b.rp;
-            const float4 q  = rel[ s ];
-            const f3     dj = F3( q.x, q.y, q.z );
-            const float  Rj = q.w;
-            const float  d  = dot( dj, dj );
-            const float  t  = ( Ri * Ri - Rj * Rj + d ) / ( 2.f * d );
-            const f3     c  = dj * t;
-            const float  r2raw = Ri * Ri - dot( c, c );
-            const float  r2 = fmaxf( r2raw, 0.f );
-            const f3     nr = dj * rsqrtf( d );
+            kVisBuried    = 1,
+            kVisTouched   = 2,
+            kVisEvaluated = 4,
+        };
+
+        __host__ __device__ inline uint32_t staged_rows( uint32_t cap ) { return cap < (uint32_t)kNbrBuf ? cap : (uint32_t)kNbrBuf; }
+
+        struct VisSmem
+        {
+            float4 *   rel;   // rows + kVisGroup: d_k, R_i^2 + |d_k|^2 - R_k^2 - 1e-4 (padding: never touches)
+            float *    dd;    // rows + kVisGroup: |d_k|^2
+            uint8_t *  res;   // rows: kVis* flags
+            uint16_t * list;  // rows: circles to evaluate
+            uint32_t * queue; // kVisQueue: s | k << 16
+        };
+
+        __host__ __device__ inline size_t vis_smem_per_warp( uint32_t cap )
+        {
+            const size_t r = staged_rows( cap ) + kVisGroup;
+            return ( ( r * ( 16 + 4 + 1 + 2 ) + 15 ) & ~(size_t)15 ) + kVisQueue * 4;
+        }
+
+        __device__ inline VisSmem vis_smem( unsigned char * base, uint32_t cap )
+        {
+            const size_t r = staged_rows( cap ) + kVisGroup;
+            VisSmem      m;
+            m.rel   = reinterpret_cast<float4 *>( base );
+            m.dd    = reinterpret_cast<float *>( base + r * 16 );
+            m.res   = base + r * 20;
+            m.list  = reinterpret_cast<uint16_t *>( base + ( ( r * 21 + 1 ) & ~(size_t)1 ) );
+            m.queue = reinterpret_cast<uint32_t *>( base + ( ( r * 23 + 15 ) & ~(size_t)15 ) );
+            return m;
+        }
+
+        // Per-circle constants of the test, with the error bands: every float32
+        // rounding of A stays below eA = kRel Mc and every rounding of G below
+        // alpha |A| + beta p^2 + gamma, Mc bounding R_i^2 + |d_k|^2 + R_k^2 + 2 |c| |d_k| + 1
+        // over the atom's neighbours. theta: k closer to the axis than that is
+        // left to double precision (infinite for a nearly tangent circle).
+        struct VisCircle
+        {
+            f3    dj;
+            float m2t, inv, r2x4, eA, alpha, beta, gamma, theta;
+        };
+
+        __device__ __forceinline__ VisCircle vis_circle( float Ri, float Mc, float theta, const float4 & q, float dJ )
+        {
+            VisCircle   v;
+            v.dj              = F3( q.x, q.y, q.z );
+            const float t     = __fdividef( q.w + 1e-4f, 2.f * dJ ); // (R_i^2 - R_j^2 + |d_j|^2) / (2 |d_j|^2)
+            const f3    c     = v.dj * t;
+            const float r2raw = Ri * Ri - dot( c, c );
+            const float r2    = fmaxf( r2raw, 0.f );
             // (nearly) tangent SAS spheres: the reference's circle radius is
             // sqrt of a negative number (NaN) and every test of the circle is
             // false; the double-precision twin decides whether that happens
-            const bool   tangent = r2raw <= 4.f * kRel * Ri * Ri;
-            buried = touched = false;
-            nq               = 0;
-            for ( uint32_t k = 0; k < ni; k++ )
-            {
-                if ( k == s )
-                    continue;
-                const float4 qk  = rel[ k ];
-                const f3     v   = c - F3( qk.x, qk.y, qk.z );
-                const float  vv  = dot( v, v );
-                const float  sv  = dot( v, nr );
-                const float  p2  = fmaxf( vv - sv * sv, 0.f );
-                const float  Rk2 = qk.w * qk.w;
-                const float  A   = vv + r2 - Rk2 - 1e-4f;
-                const float  M   = vv + r2 + Rk2 + 1.f;
-                const float  eA  = kRel * M;
-                const float  G   = A * A - 4.f * p2 * r2;
-                const float  eG  = kRel * ( A * A + 4.f * p2 * r2 + 2.f * fabsf( A ) * M + 4.f * M * ( r2 + p2 ) );
-                bool         bk = false, tk = false, decided = true;
-                // k on (or next to) the axis of the circle: the reference formula
-                // divides by |v| and takes sqrt(1 - cos^2), which yields NaN (k
-                // ignored) exactly when |v| = 0 or |cos| > 1 in its arithmetic;
-                // only the double-precision twin reproduces that
-                if ( tangent || vv <= eA || p2 <= kRel * ( vv + 1.f ) )
-                    decided = false;
-                else if ( A < -eA )
-                {
-                    tk = true;
-                    if ( G > eG )
-                        bk = true;
-                    else if ( !( G < -eG ) )
-                        decided = false;
-                }
-                else if ( A > eA )
-                {
-                    if ( G < -eG )
-                        tk = true;
-                    else if ( !( G > eG ) )
-                        decided = false;
-                }
-                else
-                    decided = false;
-                if ( !decided )
-                {
-                    if ( nq < (uint32_t)kBandSlots )
-                    {
-                        queue[ nq++ ] = (uint16_t)k;
-                        continue;
-                    }
-                    const uint32_t j  = b.nbr[ (size_t)i * b.cap + s ];
-                    const float4   aj = b.atoms[ j ];
-                    const dcircle  dc = dcircle_geometry( D3( ai ), ai.w, D3( aj ), aj.w, (double)b.rp );
-                    const float4   ak = b.atoms[ b.nbr[ (size_t)i * b.cap + k ] ];
-                    const int      r  = dcircle_vs_atom( dc, D3( ak ), __dadd_rn( (double)ak.w, (double)b.rp ) );
-                    bk                = r & 1;
-                    tk                = r & 2;
-                    fp64++;
-                }
-                touched = touched || tk;
-                if ( bk )
-                {
-                    buried = true;
-                    nq     = 0; // buried: the deferred tests cannot change the status
-                    return;
-                }
-            }
+            v.theta = r2raw <= 4.f * kRel * Ri * Ri ? __int_as_float( 0x7f800000 ) : theta;
+            v.m2t   = -2.f * t;
+            v.inv   = __fdividef( 1.f, dJ );
+            v.r2x4  = 4.f * r2;
+            v.eA    = kRel * Mc;
+            v.alpha = 3.f * kRel * Mc;
+            v.beta  = 4.f * kRel * ( r2 + Mc );
+            v.gamma = 4.f * kRel * Mc * r2;
+            return v;
         }
 
-        __global__ void __launch_bounds__( 32 * kWarpsPerBlock, 4 ) k_visibility( Build b )
+        // double-precision twin of one test (computeCirclesVisibilityStatus in IEEE double)
+        __device__ __noinline__ int circle_test_d( const Build & b, const float4 & ai, uint32_t i, uint32_t s, uint32_t k )
         {
-            extern __shared__ float4 smem[];
-            __shared__ uint16_t      bandQ[ kWarpsPerBlock ][ 32 ][ kBandSlots ];
-            __shared__ uint32_t      bandRes[ kWarpsPerBlock ][ 32 ];
-            const uint32_t           warp = threadIdx.x >> 5, lane = lane_id();
-            const uint32_t           i    = blockIdx.x * kWarpsPerBlock + warp;
+            const float4  aj = b.atoms[ b.nbr[ (size_t)i * b.cap + s ] ];
+            const float4  ak = b.atoms[ b.nbr[ (size_t)i * b.cap + k ] ];
+            const dcircle dc = dcircle_geometry( D3( ai ), ai.w, D3( aj ), aj.w, (double)b.rp );
+            return dcircle_vs_atom( dc, D3( ak ), __dadd_rn( (double)ak.w, (double)b.rp ) );
+        }
+
+        __global__ void __launch_bounds__( 32 * kWarpsPerBlock ) k_visibility( Build b )
+        {
+            extern __shared__ __align__( 16 ) unsigned char smemRaw[];
+            const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
+            const uint32_t i    = blockIdx.x * kWarpsPerBlock + warp;
             if ( i >= b.n )
                 return;
-            float4 *       rel = smem + (size_t)warp * b.cap;
+            const VisSmem  m   = vis_smem( smemRaw + warp * vis_smem_per_warp( b.cap ), b.cap );
             const uint32_t ni  = b.nbrCount[ i ];
             const float4   ai  = b.atoms[ i ];
-            for ( uint32_t s = lane; s < ni; s += 32 )
+            const float    Ri  = ai.w + b.rp;
+            const size_t   row = (size_t)i * b.cap;
+            const uint32_t U   = ( ni + kVisGroup - 1 ) / kVisGroup; // tests per lane and circle
+
+            // stage the neighbourhood and the list of circles to evaluate (the
+            // exterior build evaluates circles (i, j) with i < j only)
+            float    d2max = 0.f, r2max = 0.f;
+            uint32_t nc    = 0;
+            for ( uint32_t base = 0; base < U * kVisGroup; base += 32 )
             {
-                const float4 aj = b.atoms[ b.nbr[ (size_t)i * b.cap + s ] ];
-                rel[ s ]        = make_float4( aj.x - ai.x, aj.y - ai.y, aj.z - ai.z, aj.w + b.rp );
+                const uint32_t s    = base + lane;
+                bool           eval = false;
+                if ( s < ni )
+                {
+                    const uint32_t j  = b.nbr[ row + s ];
+                    const float4   aj = b.atoms[ j ];
+                    const f3       d  = F3( aj.x - ai.x, aj.y - ai.y, aj.z - ai.z );
+                    const float    dd = dot( d, d );
+                    const float    Rk = aj.w + b.rp;
+                    m.rel[ s ]        = make_float4( d.x, d.y, d.z, ( ( Ri * Ri + dd ) - Rk * Rk ) - 1e-4f );
+                    m.dd[ s ]         = dd;
+                    m.res[ s ]        = 0;
+                    d2max             = fmaxf( d2max, dd );
+                    r2max             = fmaxf( r2max, Rk * Rk );
+                    eval              = b.mode == 0 || i < j;
+                }
+                else if ( s < U * kVisGroup )
+                {
+                    // padding up to a whole number of tests per lane: far away, never undecided
+                    m.rel[ s ] = make_float4( 0.f, 0.f, 0.f, 1e15f );
+                    m.dd[ s ]  = 1e15f;
+                }
+                const uint32_t mk = __ballot_sync( 0xffffffffu, eval );
+                if ( eval )
+                    m.list[ nc + __popc( mk & lanemask_lt() ) ] = (uint16_t)s;
+                nc += __popc( mk );
+            }
+            for ( int o = 16; o > 0; o >>= 1 )
+            {
+                d2max = fmaxf( d2max, __shfl_xor_sync( 0xffffffffu, d2max, o ) );
+                r2max = fmaxf( r2max, __shfl_xor_sync( 0xffffffffu, r2max, o ) );
+            }
+            const float Mc    = Ri * Ri + d2max + r2max + 2.f * Ri * sqrtf( d2max ) * ( 1.f + kRel ) + 1.f;
+            const float theta = kRel * ( d2max + 1.f );
+            __syncwarp();
+
+            const uint32_t grp = lane / kVisGroup, gl = lane % kVisGroup;
+            const uint32_t gmask = ( ( 1u << kVisGroup ) - 1u ) << ( grp * kVisGroup );
+            uint32_t       nq = 0, fp64 = 0;
+            for ( uint32_t c0 = 0; c0 < nc; c0 += kVisCircles )
+            {
+                const uint32_t  ci    = c0 + grp;
+                const bool      valid = ci < nc;
+                const uint32_t  s     = m.list[ valid ? ci : 0u ];
+                const VisCircle v     = vis_circle( Ri, Mc, theta, m.rel[ s ], m.dd[ s ] );
+                bool            bur = false, tch = false;
+                for ( uint32_t u0 = 0; u0 < U; u0 += 32 )
+                {
+                    const uint32_t uN  = U - u0 < 32 ? U - u0 : 32;
+                    uint32_t       und = 0; // bit u: the test of k = gl + kVisGroup (u0 + u) is left to double precision
+                    const float4 * qp  = m.rel + gl + kVisGroup * u0;
+                    const float *  dp  = m.dd + gl + kVisGroup * u0;
+#pragma unroll 2
+                    for ( uint32_t u = 0; u < uN; u++ )
+                    {
+                        const float4 q  = qp[ kVisGroup * u ];
+                        const float  dk = dp[ kVisGroup * u ];
+                        const float  g  = v.dj.x * q.x + v.dj.y * q.y + v.dj.z * q.z;
+                        const float  A  = fmaf( v.m2t, g, q.w );
+                        const float  p2 = fmaf( -g * v.inv, g, dk );
+                        const float  G  = fmaf( A, A, -v.r2x4 * p2 );
+                        const float  eG = fmaf( v.alpha, fabsf( A ), fmaf( v.beta, p2, v.gamma ) );
+                        // false on NaN: the test is then left to double precision
+                        const bool ok = ( p2 > v.theta ) & ( fabsf( A ) > v.eA ) & ( fabsf( G ) > eG );
+                        const bool neg = A < 0.f;
+                        bur            = bur | ( ok & neg & ( G > 0.f ) );
+                        tch            = tch | ( ok & ( neg | ( G < 0.f ) ) );
+                        und |= (uint32_t)!ok << u;
+                    }
+                    // the circle's own j (always undecided) and the idle groups queue nothing
+                    const uint32_t us = s / kVisGroup;
+                    if ( gl == s % kVisGroup && us >= u0 && us < u0 + uN )
+                        und &= ~( 1u << ( us - u0 ) );
+                    const uint32_t buriedLanes = __ballot_sync( 0xffffffffu, bur ); // every lane takes part
+                    if ( !valid || ( buriedLanes & gmask ) )
+                        und = 0;
+                    uint32_t       tot;
+                    uint32_t       at = nq + warp_exclusive_sum( (uint32_t)__popc( und ), tot );
+                    for ( uint32_t w = und; w; w &= w - 1 )
+                    {
+                        const uint32_t k = gl + kVisGroup * ( u0 + (uint32_t)( __ffs( w ) - 1 ) );
+                        if ( at < (uint32_t)kVisQueue )
+                            m.queue[ at ] = s | ( k << 16 );
+                        else
+                        {
+                            const int rd = circle_test_d( b, ai, i, s, k );
+                            bur          = bur || ( rd & 1 );
+                            tch          = tch || ( rd & 2 );
+                            fp64++;
+                        }
+                        at++;
+                    }
+                    nq = min( nq + tot, (uint32_t)kVisQueue );
+                }
+                const bool gb = ( __ballot_sync( 0xffffffffu, bur ) & gmask ) != 0;
+                const bool gt = ( __ballot_sync( 0xffffffffu, tch ) & gmask ) != 0;
+                if ( valid && gl == 0 )
+                    m.res[ s ] = kVisEvaluated | ( gb ? kVisBuried : 0 ) | ( gt ? kVisTouched : 0 );
             }
             __syncwarp();
-            uint32_t vis = 0, part = 0, full = 0, fp64 = 0;
-            for ( uint32_t base = 0; base < ni; base += 32 )
+            // hand the band tests of circles not buried in float32 to the double-precision pass
+            uint32_t nKeep = 0;
+            for ( uint32_t e0 = 0; e0 < nq; e0 += 32 )
             {
-                const uint32_t s      = base + lane;
-                const bool     active = s < ni;
-                const uint32_t j      = active ? b.nbr[ (size_t)i * b.cap + s ] : 0u;
-                const bool     eval   = active && ( b.mode == 0 || i < j );
-                bool           buried = false, touched = false;
-                uint32_t       nq     = 0;
-                if ( eval )
-                    circle_screen( b, i, ai, rel, ni, s, buried, touched, bandQ[ warp ][ lane ], nq, fp64 );
-                // warp-cooperative double precision for the deferred tests of this round
-                bandRes[ warp ][ lane ] = 0;
-                uint32_t       total;
-                const uint32_t first = warp_exclusive_sum( nq, total );
-                __syncwarp();
-                for ( uint32_t t0 = 0; t0 < total; t0 += 32 )
+                const uint32_t e    = e0 + lane;
+                const uint32_t q    = e < nq ? m.queue[ e ] : 0u;
+                const bool     keep = e < nq && !( m.res[ q & 0xffffu ] & kVisBuried );
+                nKeep += __popc( __ballot_sync( 0xffffffffu, keep ) );
+            }
+            uint32_t qbase = 0;
+            if ( lane == 0 && nKeep )
+                qbase = atomicAdd( &b.counts->visBand, nKeep );
+            qbase = __shfl_sync( 0xffffffffu, qbase, 0 );
+            for ( uint32_t e0 = 0; e0 < nq; e0 += 32 )
+            {
+                const uint32_t e    = e0 + lane;
+                const uint32_t q    = e < nq ? m.queue[ e ] : 0u;
+                const bool     keep = e < nq && !( m.res[ q & 0xffffu ] & kVisBuried );
+                const uint32_t mk   = __ballot_sync( 0xffffffffu, keep );
+                const uint32_t at   = qbase + __popc( mk & lanemask_lt() );
+                if ( keep && at < b.capVisBand )
+                    b.visBand[ at ] = make_uint2( i, q );
+                else if ( keep )
                 {
-                    const uint32_t t = t0 + lane;
-                    // owner lane of job t: the last lane whose first job index is <= t
-                    uint32_t owner = 0;
-                    for ( int o = 0; o < 32; o++ )
-                    {
-                        const uint32_t fo = __shfl_sync( 0xffffffffu, first, o );
-                        const uint32_t no = __shfl_sync( 0xffffffffu, nq, o );
-                        if ( no > 0 && fo <= t )
-                            owner = (uint32_t)o;
-                    }
-                    const uint32_t fOwner = __shfl_sync( 0xffffffffu, first, owner );
-                    if ( t < total )
-                    {
-                        const uint32_t k  = bandQ[ warp ][ owner ][ t - fOwner ];
-                        const uint32_t so = base + owner;
-                        const float4   aj = b.atoms[ b.nbr[ (size_t)i * b.cap + so ] ];
-                        const dcircle  dc = dcircle_geometry( D3( ai ), ai.w, D3( aj ), aj.w, (double)b.rp );
-                        const float4   ak = b.atoms[ b.nbr[ (size_t)i * b.cap + k ] ];
-                        const int      r  = dcircle_vs_atom( dc, D3( ak ), __dadd_rn( (double)ak.w, (double)b.rp ) );
-                        if ( r )
-                            atomicOr( &bandRes[ warp ][ owner ], (uint32_t)r );
-                    }
+                    // queue full: decide here
+                    const uint32_t s  = q & 0xffffu;
+                    const int      rd = circle_test_d( b, ai, i, s, q >> 16 );
+                    if ( rd & 3 )
+                        atomicOr( reinterpret_cast<uint32_t *>( m.res ) + ( s >> 2 ), (uint32_t)( rd & 3 ) << ( 8 * ( s & 3 ) ) );
+                    fp64++;
                 }
-                __syncwarp();
-                fp64 += total > lane ? ( total - lane + 31 ) / 32 : 0;
-                if ( !active )
+                qbase += __popc( mk );
+            }
+            __syncwarp();
+            for ( uint32_t s = lane; s < ni; s += 32 )
+                b.status[ row + s ] = m.res[ s ];
+            for ( int o = 16; o > 0; o >>= 1 )
+                fp64 += __shfl_xor_sync( 0xffffffffu, fp64, o );
+            if ( lane == 0 && fp64 )
+                atomicAdd( &b.counts->fp64[ kFp64Visibility ], fp64 );
+        }
+
+        // Band tests in double precision, one per thread with full warps; the
+        // result bits go into the circle's status flags.
+        __global__ void __launch_bounds__( 128 ) k_visibility_band( Build b )
+        {
+            const uint32_t nb   = min( b.counts->visBand, b.capVisBand );
+            uint32_t       fp64 = 0;
+            for ( uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nb; t += gridDim.x * blockDim.x )
+            {
+                const uint2    e   = b.visBand[ t ];
+                const uint32_t i   = e.x, s = e.y & 0xffffu, k = e.y >> 16;
+                if ( i >= b.n || s >= b.nbrCount[ i ] || k >= b.nbrCount[ i ] )
+                    continue; // not written by k_visibility
+                const size_t pos = (size_t)i * b.cap + s;
+                if ( b.status[ pos ] & kVisBuried )
                     continue;
-                const uint32_t r = bandRes[ warp ][ lane ];
-                buried           = buried || ( r & 1 );
-                touched          = touched || ( r & 2 );
-                const uint8_t st = eval ? ( buried ? 0 : ( touched ? 1 : 2 ) ) : 0;
-                b.status[ (size_t)i * b.cap + s ] = st;
+                const int rd = circle_test_d( b, b.atoms[ i ], i, s, k );
+                if ( rd & 3 )
+                    atomicOr( reinterpret_cast<uint32_t *>( b.status + ( pos & ~(size_t)3 ) ), (uint32_t)( rd & 3 ) << ( 8 * ( pos & 3 ) ) );
+                fp64++;
+            }
+            for ( int o = 16; o > 0; o >>= 1 )
+                fp64 += __shfl_xor_sync( 0xffffffffu, fp64, o );
+            if ( lane_id() == 0 && fp64 )
+                atomicAdd( &b.counts->fp64[ kFp64Visibility ], fp64 );
+        }
+
+        // statuses (0 buried, 1 partial, 2 complete; circles not evaluated 0) and
+        // the per-atom counts, warp per atom
+        __global__ void __launch_bounds__( 32 * kWarpsPerBlock ) k_visibility_final( Build b )
+        {
+            const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
+            const uint32_t i    = blockIdx.x * kWarpsPerBlock + warp;
+            if ( i >= b.n )
+                return;
+            const uint32_t ni  = b.nbrCount[ i ];
+            const size_t   row = (size_t)i * b.cap;
+            uint32_t       vis = 0, part = 0, full = 0;
+            for ( uint32_t s = lane; s < ni; s += 32 )
+            {
+                const uint32_t j  = b.nbr[ row + s ];
+                const uint32_t r  = b.status[ row + s ];
+                const uint8_t  st = ( r & kVisEvaluated ) ? ( ( r & kVisBuried ) ? 0 : ( ( r & kVisTouched ) ? 1 : 2 ) ) : 0;
+                b.status[ row + s ] = st;
                 vis += st != 0;
                 part += ( st == 1 && i < j );
                 full += ( st == 2 && i < j );
@@ -433,17 +576,16 @@ namespace sesgb
                 vis += __shfl_xor_sync( 0xffffffffu, vis, o );
                 part += __shfl_xor_sync( 0xffffffffu, part, o );
                 full += __shfl_xor_sync( 0xffffffffu, full, o );
-                fp64 += __shfl_xor_sync( 0xffffffffu, fp64, o );
             }
             if ( lane == 0 )
             {
                 b.visCnt[ i ]  = vis;
                 b.partCnt[ i ] = part;
                 b.fullCnt[ i ] = full;
-                if ( fp64 )
-                    atomicAdd( &b.counts->fp64[ kFp64Visibility ], fp64 );
             }
         }
+
+        __host__ inline size_t visibility_smem( uint32_t cap ) { return vis_smem_per_warp( cap ) * kWarpsPerBlock; }
 
         // ---- sectors, complete circles, partial-circle numbering -----------
         // sector of buildConvexPatchesSectors (operations.inl:186-213) in
@@ -649,14 +791,15 @@ namespace sesgb
 
         __host__ __device__ inline size_t probe_smem_per_warp( uint32_t cap )
         {
-            size_t b = (size_t)cap * ( 16 + 4 + 4 + 2 + 1 );
+            size_t b = (size_t)staged_rows( cap ) * ( 16 + 4 + 4 + 2 + 1 );
             b        = ( b + 15 ) & ~(size_t)15;
             return b + kCandBuf * 4 + kProbeBuf * 8;
         }
 
-        __device__ inline ProbeSmem probe_smem( unsigned char * base, uint32_t cap )
+        __device__ inline ProbeSmem probe_smem( unsigned char * base, uint32_t capacity )
         {
-            ProbeSmem m;
+            const size_t cap = staged_rows( capacity );
+            ProbeSmem    m;
             m.rel    = reinterpret_cast<float4 *>( base );
             m.rad    = reinterpret_cast<float *>( base + (size_t)cap * 16 );
             m.nid    = reinterpret_cast<uint32_t *>( base + (size_t)cap * 20 );
@@ -1574,9 +1717,10 @@ namespace sesgb
     {
         if ( !b.n )
             return;
-        const size_t smem = sizeof( float4 ) * (size_t)b.cap * kWarpsPerBlock;
-        k_visibility<<<blocks_for( b.n, kWarpsPerBlock ), 32 * kWarpsPerBlock, smem, s>>>( b );
-        counted();
+        k_visibility<<<blocks_for( b.n, kWarpsPerBlock ), 32 * kWarpsPerBlock, visibility_smem( b.cap ), s>>>( b );
+        k_visibility_band<<<min( persistent_blocks( 128 ), blocks_for( b.capVisBand, 128 ) + 1 ), 128, 0, s>>>( b );
+        k_visibility_final<<<blocks_for( b.n, kWarpsPerBlock ), 32 * kWarpsPerBlock, 0, s>>>( b );
+        counted( 3 );
     }
     void launch_emit( const Build & b, cudaStream_t s )
     {
@@ -1649,8 +1793,7 @@ namespace sesgb
 
     cudaError_t configure_kernels( const Build & b )
     {
-        const size_t smem = sizeof( float4 ) * (size_t)b.cap * kWarpsPerBlock;
-        cudaError_t  e    = cudaFuncSetAttribute( k_visibility, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem );
+        cudaError_t e = cudaFuncSetAttribute( k_visibility, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)visibility_smem( b.cap ) );
         if ( e != cudaSuccess )
             return e;
         return cudaFuncSetAttribute( k_probes, cudaFuncAttributeMaxDynamicSharedMemorySize,

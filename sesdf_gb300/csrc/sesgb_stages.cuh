@@ -41,7 +41,9 @@ namespace sesgb
         // neighbour lists and circles, slot = i * cap + s (the reference layout)
         uint32_t * nbr;
         uint32_t * nbrCount;
-        uint8_t *  status;
+        uint8_t *  status;   // n * cap + 4 (whole 32-bit words for the flag updates)
+        uint2 *    visBand;  // capVisBand: visibility tests left to double precision (i, s | k << 16)
+        uint32_t   capVisBand;
         uint32_t * slotTrim; // partial-circle number of each slot (exclusive count)
 
         // per-atom counts and offsets
