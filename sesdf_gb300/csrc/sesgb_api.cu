@@ -161,8 +161,6 @@ namespace
         b.nbr             = dalloc<uint32_t>( c, L, n * b.cap, ok );
         b.nbrCount        = dalloc<uint32_t>( c, L, n + 1, ok );
         b.status          = dalloc<uint8_t>( c, L, n * b.cap + 4, ok );
-        b.capVisBand      = (uint32_t)std::max<size_t>( 1u << 16, 2 * n );
-        b.visBand         = dalloc<uint2>( c, L, b.capVisBand, ok );
         b.slotTrim        = dalloc<uint32_t>( c, L, n * b.cap, ok );
         uint32_t ** per[] = { &b.visCnt,  &b.partCnt, &b.fullCnt, &b.torCnt,  &b.visOff,    &b.partOff, &b.fullOff,
                               &b.torOff,  &b.singCnt, &b.regCnt,  &b.singOff, &b.regOff,    &b.chunkStart,
@@ -208,6 +206,7 @@ namespace
         b.segOff      = dalloc<uint32_t>( c, L, C1 + 1, ok );
         b.segList     = dalloc<uint32_t>( c, L, C1 + 1, ok );
         b.segments    = dalloc<uint4>( c, L, b.capSeg, ok );
+        b.visBand     = dalloc<uint2>( c, L, b.capVisBand, ok );
         b.torPos      = dalloc<float4>( c, L, b.capTori, ok );
         b.torAxis     = dalloc<float4>( c, L, b.capTori, ok );
         b.torVs       = dalloc<float4>( c, L, b.capTori, ok );
@@ -328,6 +327,7 @@ namespace
         fix( b.capProbes, h.I );
         fix( b.capSeg, h.S );
         fix( b.capTori, h.T );
+        fix( b.capVisBand, h.visBand );
         if ( h.overflow & ( kOverflowProbes | kOverflowList ) )
         {
             // sizes follow I; a list overflow means a circle with more probes than one
@@ -402,7 +402,8 @@ namespace
         const DeviceCounts & h = *c->hCounts;
         const Build &        b = c->b;
         return ( h.overflow & ~(uint32_t)kOverflowNbr ) == 0 && h.V <= b.capSectors && h.F <= b.capFull && h.C1 <= b.capC1
-               && h.staged <= b.capProbes && h.I <= b.capProbes && h.S <= b.capSeg && h.T <= b.capTori;
+               && h.staged <= b.capProbes && h.I <= b.capProbes && h.S <= b.capSeg && h.T <= b.capTori
+               && h.visBand <= b.capVisBand;
     }
 
     // waits for the enqueued build; on a capacity overflow regrows and builds again
@@ -502,6 +503,7 @@ extern "C"
         b.capFull    = grow( 4ull * n );
         b.capC1      = grow( 24ull * n );
         b.capProbes  = grow( 8ull * n );
+        b.capVisBand = grow( std::max<uint64_t>( 1u << 16, n / 2 ) );
         b.capSeg     = grow( 8ull * n );
         b.capTori    = grow( 16ull * n );
         if ( !allocate_fixed( c ) || !allocate_dynamic( c ) || !cuda_ok( c, configure_kernels( c->b ), "configure" ) )

@@ -50,6 +50,7 @@ namespace sesgb
         kOverflowCells   = 1u << 8,
         kOverflowList    = 1u << 9,
         kOverflowAtomProbes = 1u << 10, // an atom owns more probes than one warp holds (128)
+        kOverflowVisBand    = 1u << 11, // more visibility tests in the float32 band than the queue holds
     };
 
     enum Fp64Stage : uint32_t

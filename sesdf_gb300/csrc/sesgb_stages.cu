@@ -279,7 +279,7 @@ namespace sesgb
         // operations.cu:164-197). Tests inside the float32 error band go to a
         // queue that k_visibility_band decides in double precision with full
         // warps; k_visibility_final turns the flags into statuses and counts.
-        constexpr int kVisGroup   = 8;              // lanes per circle
+        constexpr int kVisGroup   = 4;              // lanes per circle
         constexpr int kVisCircles = 32 / kVisGroup; // circles per warp step
         constexpr int kVisQueue   = 128;            // band tests a warp holds before they go to the global queue
 
@@ -362,6 +362,16 @@ namespace sesgb
             return dcircle_vs_atom( dc, D3( ak ), __dadd_rn( (double)ak.w, (double)b.rp ) );
         }
 
+        // one test to the global double-precision queue (capacity exceeded: the build is redone larger)
+        __device__ __forceinline__ void band_push( const Build & b, uint32_t i, uint32_t sk )
+        {
+            const uint32_t at = atomicAdd( &b.counts->visBand, 1u );
+            if ( at < b.capVisBand )
+                b.visBand[ at ] = make_uint2( i, sk );
+            else
+                atomicOr( &b.counts->overflow, (uint32_t)kOverflowVisBand );
+        }
+
         __global__ void __launch_bounds__( 32 * kWarpsPerBlock ) k_visibility( Build b )
         {
             extern __shared__ __align__( 16 ) unsigned char smemRaw[];
@@ -393,10 +403,10 @@ namespace sesgb
                     const float    Rk = aj.w + b.rp;
                     m.rel[ s ]        = make_float4( d.x, d.y, d.z, ( ( Ri * Ri + dd ) - Rk * Rk ) - 1e-4f );
                     m.dd[ s ]         = dd;
-                    m.res[ s ]        = 0;
+                    eval              = b.mode == 0 || i < j;
+                    m.res[ s ]        = eval ? kVisEvaluated : 0;
                     d2max             = fmaxf( d2max, dd );
                     r2max             = fmaxf( r2max, Rk * Rk );
-                    eval              = b.mode == 0 || i < j;
                 }
                 else if ( s < U * kVisGroup )
                 {
@@ -420,66 +430,78 @@ namespace sesgb
 
             const uint32_t grp = lane / kVisGroup, gl = lane % kVisGroup;
             const uint32_t gmask = ( ( 1u << kVisGroup ) - 1u ) << ( grp * kVisGroup );
-            uint32_t       nq = 0, fp64 = 0;
+            uint32_t       nq = 0;
+            // queues the tests of bits w (k = gl + kVisGroup (u0 + bit)) of circle s
+            auto queue_tests = [ & ]( uint32_t w, uint32_t u0, uint32_t s ) {
+                uint32_t tot;
+                uint32_t at = nq + warp_exclusive_sum( (uint32_t)__popc( w ), tot );
+                for ( ; w; w &= w - 1 )
+                {
+                    const uint32_t k = gl + kVisGroup * ( u0 + (uint32_t)( __ffs( w ) - 1 ) );
+                    if ( at < (uint32_t)kVisQueue )
+                        m.queue[ at ] = s | ( k << 16 );
+                    else
+                        band_push( b, i, s | ( k << 16 ) ); // the warp's queue is full
+                    at++;
+                }
+                nq = min( nq + tot, (uint32_t)kVisQueue );
+            };
             for ( uint32_t c0 = 0; c0 < nc; c0 += kVisCircles )
             {
-                const uint32_t  ci    = c0 + grp;
-                const bool      valid = ci < nc;
-                const uint32_t  s     = m.list[ valid ? ci : 0u ];
-                const VisCircle v     = vis_circle( Ri, Mc, theta, m.rel[ s ], m.dd[ s ] );
-                bool            bur = false, tch = false;
-                for ( uint32_t u0 = 0; u0 < U; u0 += 32 )
+                const uint32_t ci    = c0 + grp;
+                const bool     valid = ci < nc;
+                const uint32_t s     = m.list[ valid ? ci : 0u ];
+                bool           bur = false, tch = false;
+                uint32_t       und = 0; // bit u: the test of k = gl + kVisGroup (u0 + u) is left to double precision
+                uint32_t       u0  = 0;
                 {
-                    const uint32_t uN  = U - u0 < 32 ? U - u0 : 32;
-                    uint32_t       und = 0; // bit u: the test of k = gl + kVisGroup (u0 + u) is left to double precision
-                    const float4 * qp  = m.rel + gl + kVisGroup * u0;
-                    const float *  dp  = m.dd + gl + kVisGroup * u0;
-#pragma unroll 2
-                    for ( uint32_t u = 0; u < uN; u++ )
+                    const VisCircle v = vis_circle( Ri, Mc, theta, m.rel[ s ], m.dd[ s ] );
+                    for ( ;; )
                     {
-                        const float4 q  = qp[ kVisGroup * u ];
-                        const float  dk = dp[ kVisGroup * u ];
-                        const float  g  = v.dj.x * q.x + v.dj.y * q.y + v.dj.z * q.z;
-                        const float  A  = fmaf( v.m2t, g, q.w );
-                        const float  p2 = fmaf( -g * v.inv, g, dk );
-                        const float  G  = fmaf( A, A, -v.r2x4 * p2 );
-                        const float  eG = fmaf( v.alpha, fabsf( A ), fmaf( v.beta, p2, v.gamma ) );
-                        // false on NaN: the test is then left to double precision
-                        const bool ok = ( p2 > v.theta ) & ( fabsf( A ) > v.eA ) & ( fabsf( G ) > eG );
-                        const bool neg = A < 0.f;
-                        bur            = bur | ( ok & neg & ( G > 0.f ) );
-                        tch            = tch | ( ok & ( neg | ( G < 0.f ) ) );
-                        und |= (uint32_t)!ok << u;
-                    }
-                    // the circle's own j (always undecided) and the idle groups queue nothing
-                    const uint32_t us = s / kVisGroup;
-                    if ( gl == s % kVisGroup && us >= u0 && us < u0 + uN )
-                        und &= ~( 1u << ( us - u0 ) );
-                    const uint32_t buriedLanes = __ballot_sync( 0xffffffffu, bur ); // every lane takes part
-                    if ( !valid || ( buriedLanes & gmask ) )
-                        und = 0;
-                    uint32_t       tot;
-                    uint32_t       at = nq + warp_exclusive_sum( (uint32_t)__popc( und ), tot );
-                    for ( uint32_t w = und; w; w &= w - 1 )
-                    {
-                        const uint32_t k = gl + kVisGroup * ( u0 + (uint32_t)( __ffs( w ) - 1 ) );
-                        if ( at < (uint32_t)kVisQueue )
-                            m.queue[ at ] = s | ( k << 16 );
-                        else
+                        const uint32_t uN = U - u0 < 32 ? U - u0 : 32;
+                        const float4 * qp = m.rel + gl + kVisGroup * u0;
+                        const float *  dp = m.dd + gl + kVisGroup * u0;
+#pragma unroll 3
+                        for ( uint32_t u = 0; u < uN; u++ )
                         {
-                            const int rd = circle_test_d( b, ai, i, s, k );
-                            bur          = bur || ( rd & 1 );
-                            tch          = tch || ( rd & 2 );
-                            fp64++;
+                            const float4 q  = qp[ kVisGroup * u ];
+                            const float  dk = dp[ kVisGroup * u ];
+                            const float  g  = v.dj.x * q.x + v.dj.y * q.y + v.dj.z * q.z;
+                            const float  A  = fmaf( v.m2t, g, q.w );
+                            const float  p2 = fmaf( -g * v.inv, g, dk );
+                            const float  G  = fmaf( A, A, -v.r2x4 * p2 );
+                            const float  eG = fmaf( v.alpha, fabsf( A ), fmaf( v.beta, p2, v.gamma ) );
+                            // false on NaN: the test is then left to double precision
+                            const bool ok  = ( p2 > v.theta ) & ( fabsf( A ) > v.eA ) & ( fabsf( G ) > eG );
+                            const bool neg = A < 0.f;
+                            bur            = bur | ( ok & neg & ( G > 0.f ) );
+                            tch            = tch | ( ok & ( neg | ( G < 0.f ) ) );
+                            und |= (uint32_t)!ok << u;
                         }
-                        at++;
+                        // the circle's own j is always undecided and never tested
+                        const uint32_t us = s / kVisGroup;
+                        if ( gl == s % kVisGroup && us >= u0 && us < u0 + uN )
+                            und &= ~( 1u << ( us - u0 ) );
+                        if ( u0 + 32 >= U )
+                            break;
+                        // more than 32 tests per lane: earlier bits go out now (no buried filter)
+                        if ( !valid )
+                            und = 0;
+                        if ( __any_sync( 0xffffffffu, und != 0 ) )
+                            queue_tests( und, u0, s );
+                        und = 0;
+                        u0 += 32;
                     }
-                    nq = min( nq + tot, (uint32_t)kVisQueue );
                 }
                 const bool gb = ( __ballot_sync( 0xffffffffu, bur ) & gmask ) != 0;
                 const bool gt = ( __ballot_sync( 0xffffffffu, tch ) & gmask ) != 0;
-                if ( valid && gl == 0 )
-                    m.res[ s ] = kVisEvaluated | ( gb ? kVisBuried : 0 ) | ( gt ? kVisTouched : 0 );
+                if ( valid && gl == 0 && ( gb || gt ) )
+                    atomicOr( reinterpret_cast<uint32_t *>( m.res ) + ( s >> 2 ),
+                              (uint32_t)( ( gb ? kVisBuried : 0 ) | ( gt ? kVisTouched : 0 ) ) << ( 8 * ( s & 3 ) ) );
+                if ( !valid || gb )
+                    und = 0;
+                if ( __any_sync( 0xffffffffu, und != 0 ) )
+                    queue_tests( und, u0, s );
             }
             __syncwarp();
             // hand the band tests of circles not buried in float32 to the double-precision pass
@@ -505,23 +527,12 @@ namespace sesgb
                 if ( keep && at < b.capVisBand )
                     b.visBand[ at ] = make_uint2( i, q );
                 else if ( keep )
-                {
-                    // queue full: decide here
-                    const uint32_t s  = q & 0xffffu;
-                    const int      rd = circle_test_d( b, ai, i, s, q >> 16 );
-                    if ( rd & 3 )
-                        atomicOr( reinterpret_cast<uint32_t *>( m.res ) + ( s >> 2 ), (uint32_t)( rd & 3 ) << ( 8 * ( s & 3 ) ) );
-                    fp64++;
-                }
+                    atomicOr( &b.counts->overflow, (uint32_t)kOverflowVisBand );
                 qbase += __popc( mk );
             }
             __syncwarp();
             for ( uint32_t s = lane; s < ni; s += 32 )
                 b.status[ row + s ] = m.res[ s ];
-            for ( int o = 16; o > 0; o >>= 1 )
-                fp64 += __shfl_xor_sync( 0xffffffffu, fp64, o );
-            if ( lane == 0 && fp64 )
-                atomicAdd( &b.counts->fp64[ kFp64Visibility ], fp64 );
         }
 
         // Band tests in double precision, one per thread with full warps; the
