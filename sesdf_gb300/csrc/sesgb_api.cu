@@ -164,7 +164,7 @@ namespace
         b.slotTrim        = dalloc<uint32_t>( c, L, n * b.cap, ok );
         uint32_t ** per[] = { &b.visCnt,  &b.partCnt, &b.fullCnt, &b.torCnt,  &b.visOff,    &b.partOff, &b.fullOff,
                               &b.torOff,  &b.singCnt, &b.regCnt,  &b.singOff, &b.regOff,    &b.chunkStart,
-                              &b.chunkLen };
+                              &b.chunkLen, &b.pairOff };
         for ( uint32_t ** p : per )
             *p = dalloc<uint32_t>( c, L, n + 1, ok );
         b.convex = dalloc<uint2>( c, L, n, ok );
@@ -207,6 +207,7 @@ namespace
         b.segList     = dalloc<uint32_t>( c, L, C1 + 1, ok );
         b.segments    = dalloc<uint4>( c, L, b.capSeg, ok );
         b.visBand     = dalloc<uint2>( c, L, b.capVisBand, ok );
+        b.touch       = dalloc<uint64_t>( c, L, b.capPairs, ok );
         b.torPos      = dalloc<float4>( c, L, b.capTori, ok );
         b.torAxis     = dalloc<float4>( c, L, b.capTori, ok );
         b.torVs       = dalloc<float4>( c, L, b.capTori, ok );
@@ -259,12 +260,12 @@ namespace
 
         // B, C: visibility, sectors, complete and partial circles
         mark( 2 );
+        exclusive_scan( b.nbrCount, b.pairOff, n, nullptr, &d->P, sc, s );
         launch_visibility( b, s );
         mark( 3 );
         exclusive_scan( b.visCnt, b.visOff, n, nullptr, &d->V, sc, s );
         exclusive_scan( b.partCnt, b.partOff, n, nullptr, &d->C1, sc, s );
         exclusive_scan( b.fullCnt, b.fullOff, n, nullptr, &d->F, sc, s );
-        exclusive_scan( b.nbrCount, b.torOff, n, nullptr, &d->P, sc, s );
         launch_emit( b, s );
 
         // D, E: probes
@@ -328,6 +329,7 @@ namespace
         fix( b.capSeg, h.S );
         fix( b.capTori, h.T );
         fix( b.capVisBand, h.visBand );
+        fix( b.capPairs, h.P );
         if ( h.overflow & ( kOverflowProbes | kOverflowList ) )
         {
             // sizes follow I; a list overflow means a circle with more probes than one
@@ -403,7 +405,7 @@ namespace
         const Build &        b = c->b;
         return ( h.overflow & ~(uint32_t)kOverflowNbr ) == 0 && h.V <= b.capSectors && h.F <= b.capFull && h.C1 <= b.capC1
                && h.staged <= b.capProbes && h.I <= b.capProbes && h.S <= b.capSeg && h.T <= b.capTori
-               && h.visBand <= b.capVisBand;
+               && h.visBand <= b.capVisBand && h.P <= b.capPairs;
     }
 
     // waits for the enqueued build; on a capacity overflow regrows and builds again
@@ -504,6 +506,7 @@ extern "C"
         b.capC1      = grow( 24ull * n );
         b.capProbes  = grow( 8ull * n );
         b.capVisBand = grow( std::max<uint64_t>( 1u << 16, n / 2 ) );
+        b.capPairs   = grow( 40ull * n );
         b.capSeg     = grow( 8ull * n );
         b.capTori    = grow( 16ull * n );
         if ( !allocate_fixed( c ) || !allocate_dynamic( c ) || !cuda_ok( c, configure_kernels( c->b ), "configure" ) )

@@ -51,6 +51,7 @@ namespace sesgb
         kOverflowList    = 1u << 9,
         kOverflowAtomProbes = 1u << 10, // an atom owns more probes than one warp holds (128)
         kOverflowVisBand    = 1u << 11, // more visibility tests in the float32 band than the queue holds
+        kOverflowPairs      = 1u << 12, // more neighbour pairs than the touch-mask buffer holds
     };
 
     enum Fp64Stage : uint32_t

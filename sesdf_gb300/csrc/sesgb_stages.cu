@@ -282,6 +282,7 @@ namespace sesgb
         constexpr int kVisGroup   = 4;              // lanes per circle
         constexpr int kVisCircles = 32 / kVisGroup; // circles per warp step
         constexpr int kVisQueue   = 128;            // band tests a warp holds before they go to the global queue
+        constexpr int kMaskSlots  = 64;             // atoms with at most this many neighbours keep touch masks
 
         // status flags between the three visibility kernels
         enum : uint8_t
@@ -289,6 +290,7 @@ namespace sesgb
             kVisBuried    = 1,
             kVisTouched   = 2,
             kVisEvaluated = 4,
+            kVisUpper     = 8, // circle (i, j) with i < j: its touch mask is kept
         };
 
         __host__ __device__ inline uint32_t staged_rows( uint32_t cap ) { return cap < (uint32_t)kNbrBuf ? cap : (uint32_t)kNbrBuf; }
@@ -404,7 +406,7 @@ namespace sesgb
                     m.rel[ s ]        = make_float4( d.x, d.y, d.z, ( ( Ri * Ri + dd ) - Rk * Rk ) - 1e-4f );
                     m.dd[ s ]         = dd;
                     eval              = b.mode == 0 || i < j;
-                    m.res[ s ]        = eval ? kVisEvaluated : 0;
+                    m.res[ s ]        = ( eval ? kVisEvaluated : 0 ) | ( i < j ? kVisUpper : 0 );
                     d2max             = fmaxf( d2max, dd );
                     r2max             = fmaxf( r2max, Rk * Rk );
                 }
@@ -453,6 +455,7 @@ namespace sesgb
                 const uint32_t s     = m.list[ valid ? ci : 0u ];
                 bool           bur = false, tch = false;
                 uint32_t       und = 0; // bit u: the test of k = gl + kVisGroup (u0 + u) is left to double precision
+                uint32_t       tou = 0; // bit u: that k touches the circle or is undecided
                 uint32_t       u0  = 0;
                 {
                     const VisCircle v = vis_circle( Ri, Mc, theta, m.rel[ s ], m.dd[ s ] );
@@ -477,6 +480,7 @@ namespace sesgb
                             bur            = bur | ( ok & neg & ( G > 0.f ) );
                             tch            = tch | ( ok & ( neg | ( G < 0.f ) ) );
                             und |= (uint32_t)!ok << u;
+                            tou |= (uint32_t)( !ok | neg | ( G < 0.f ) ) << u;
                         }
                         // the circle's own j is always undecided and never tested
                         const uint32_t us = s / kVisGroup;
@@ -491,6 +495,27 @@ namespace sesgb
                             queue_tests( und, u0, s );
                         und = 0;
                         u0 += 32;
+                    }
+                }
+                if ( U <= (uint32_t)( kMaskSlots / kVisGroup ) )
+                {
+                    // touch mask of the circle over slots 0..63 (slot gl + kVisGroup u from lane gl, bit u):
+                    // the atoms that may hold a point of it; k_probes tests only those
+                    uint64_t x = tou & 0xffffu;
+                    x          = ( x | ( x << 24 ) ) & 0x000000FF000000FFull;
+                    x          = ( x | ( x << 12 ) ) & 0x000F000F000F000Full;
+                    x          = ( x | ( x << 6 ) ) & 0x0303030303030303ull;
+                    x          = ( x | ( x << 3 ) ) & 0x1111111111111111ull;
+                    x <<= gl;
+                    x |= __shfl_xor_sync( 0xffffffffu, x, 1 );
+                    x |= __shfl_xor_sync( 0xffffffffu, x, 2 );
+                    if ( valid && gl == 0 && ( m.res[ s ] & kVisUpper ) )
+                    {
+                        const uint32_t at = b.pairOff[ i ] + s;
+                        if ( at < b.capPairs )
+                            b.touch[ at ] = x;
+                        else
+                            atomicOr( &b.counts->overflow, (uint32_t)kOverflowPairs );
                     }
                 }
                 const bool gb = ( __ballot_sync( 0xffffffffu, bur ) & gmask ) != 0;
@@ -798,13 +823,14 @@ namespace sesgb
             uint8_t *  full;  // cap: 1 if the neighbour list of that neighbour may be truncated
             uint32_t * cand;  // kCandBuf: slot j | slot k << 16
             uint2 *    ent;   // kProbeBuf: (slot j | slot k << 16, side | kind << 1 | (w + 4) << 2)
+            uint64_t * touch; // kMaskSlots: slots of the atoms touching the partial circle (i, slot)
         };
 
         __host__ __device__ inline size_t probe_smem_per_warp( uint32_t cap )
         {
             size_t b = (size_t)staged_rows( cap ) * ( 16 + 4 + 4 + 2 + 1 );
             b        = ( b + 15 ) & ~(size_t)15;
-            return b + kCandBuf * 4 + kProbeBuf * 8;
+            return b + kCandBuf * 4 + kProbeBuf * 8 + kMaskSlots * 8;
         }
 
         __device__ inline ProbeSmem probe_smem( unsigned char * base, uint32_t capacity )
@@ -820,6 +846,8 @@ namespace sesgb
             m.cand   = reinterpret_cast<uint32_t *>( base + o );
             o += kCandBuf * 4;
             m.ent = reinterpret_cast<uint2 *>( base + o );
+            o += kProbeBuf * 8;
+            m.touch = reinterpret_cast<uint64_t *>( base + o );
             return m;
         }
 
@@ -864,8 +892,8 @@ namespace sesgb
         // Is k (slot sk) in the neighbour list of j (slot sj)? The lists hold every
         // atom that satisfies the neighbour predicate (k_neighbors decides it
         // exactly), in ascending order, cut at the capacity: for a list that is
-        // not full the predicate itself answers, with the double-precision twin
-        // inside the band; a full list is searched.
+        // not full the float32 predicate answers outside its error band; a full
+        // list, or a pair inside the band, is searched.
         __device__ __forceinline__ bool pair_is_neighbor( const Build & b, const ProbeSmem & m, const ProbeBounds & pb,
                                                           uint32_t sj, uint32_t sk, uint32_t & fp64 )
         {
@@ -884,9 +912,8 @@ namespace sesgb
                 return true;
             if ( mm > e )
                 return false;
-            fp64++;
-            const float4 aj = b.atoms[ j ], ak = b.atoms[ k ];
-            return dneighbor( D3( aj ), aj.w, D3( ak ), ak.w, (double)b.rp );
+            fp64++; // inside the band: the list itself answers
+            return find_in_row( b.nbr + (size_t)j * b.cap, b.nbrCount[ j ], k ) >= 0;
         }
 
         // One (i, j, k) candidate, float32 screen in coordinates relative to atom i
@@ -894,7 +921,8 @@ namespace sesgb
         // singular, +-3 kept with the singular flag undecided; or band = true
         // (both entries reserved for the double-precision pass).
         __device__ __forceinline__ void probe_screen( const ProbeSmem & m, const ProbeBounds & pb, float Ri, float rp,
-                                                      uint32_t ni, uint32_t sj, uint32_t sk, int w[ 2 ], bool & band )
+                                                      uint32_t ni, bool useMask, uint32_t sj, uint32_t sk, int w[ 2 ],
+                                                      bool & band )
         {
             const float4 qj = m.rel[ sj ], qk = m.rel[ sk ];
             const f3     dj = F3( qj.x, qj.y, qj.z ), dk = F3( qk.x, qk.y, qk.z );
@@ -928,23 +956,44 @@ namespace sesgb
             // moves by at most ep |d_l|, rounding by at most eK
             const float eh = ep * pb.dmax + pb.eK;
             bool        v1 = true, v2 = true;
-            for ( uint32_t sl = 0; sl < ni; sl++ )
-            {
-                if ( sl == sj || sl == sk )
-                    continue;
+            // 0: go on, 1: inside the band, 2: both points buried
+            auto occlude = [ & ]( uint32_t sl ) -> int {
                 const float4 ql = m.rel[ sl ];
                 const float  a  = ql.w - ( xc.x * ql.x + xc.y * ql.y + xc.z * ql.z );
                 const float  c  = root * ( nn.x * ql.x + nn.y * ql.y + nn.z * ql.z );
                 const float  h1 = a - c, h2 = a + c; // K_l - x . d_l for x1 and x2
                 if ( ( v1 && fabsf( h1 ) <= eh ) || ( v2 && fabsf( h2 ) <= eh ) || ( v1 && h1 != h1 ) || ( v2 && h2 != h2 ) )
-                {
-                    band = true;
-                    return;
-                }
+                    return 1;
                 v1 = v1 && h1 > 0.f;
                 v2 = v2 && h2 > 0.f;
-                if ( !( v1 || v2 ) )
-                    return;
+                return ( v1 || v2 ) ? 0 : 2;
+            };
+            if ( useMask )
+            {
+                // only an atom that touches both circles (i, j) and (i, k) can hold a point of both
+                for ( uint64_t occ = m.touch[ sj ] & m.touch[ sk ] & ~( ( 1ull << sj ) | ( 1ull << sk ) ); occ; occ &= occ - 1 )
+                {
+                    const int r = occlude( (uint32_t)( __ffsll( (long long)occ ) - 1 ) );
+                    if ( r )
+                    {
+                        band = r == 1;
+                        return;
+                    }
+                }
+            }
+            else
+            {
+                for ( uint32_t sl = 0; sl < ni; sl++ )
+                {
+                    if ( sl == sj || sl == sk )
+                        continue;
+                    const int r = occlude( sl );
+                    if ( r )
+                    {
+                        band = r == 1;
+                        return;
+                    }
+                }
             }
             if ( v1 )
             {
@@ -962,7 +1011,7 @@ namespace sesgb
         // whose far atoms are neighbours. Entries of the atom's probe list are kept
         // in order (circle (i, j), then k, then x1 before x2) and written as one
         // chunk; positions and undecided flags are completed by k_probe_jobs.
-        __global__ void __launch_bounds__( 32 * kProbeWarps ) k_probes( Build b )
+        __global__ void __launch_bounds__( 32 * kProbeWarps, 8 ) k_probes( Build b )
         {
             extern __shared__ __align__( 16 ) unsigned char smemRaw[];
             const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
@@ -975,8 +1024,10 @@ namespace sesgb
             const float     Ri  = ai.w + b.rp;
             const size_t    row = (size_t)i * b.cap;
 
-            uint32_t p = 0;
-            float    d2max = 0.f, bmax = 0.f;
+            const bool useMask = ni <= (uint32_t)kMaskSlots;
+            uint32_t   p       = 0;
+            uint64_t   partial = 0; // slots of the partial circles (i, j), i < j
+            float      d2max = 0.f, bmax = 0.f;
             for ( uint32_t base = 0; base < ni; base += 32 )
             {
                 const uint32_t s   = base + lane;
@@ -993,13 +1044,17 @@ namespace sesgb
                     m.nid[ s ]        = j;
                     m.full[ s ]       = b.nbrCount[ j ] >= b.cap;
                     isP               = b.status[ row + s ] == 1 && i < j;
-                    d2max             = fmaxf( d2max, dd );
-                    bmax              = fmaxf( bmax, Ri * Ri + dd + Rl * Rl );
+                    if ( isP && useMask )
+                        m.touch[ s ] = b.touch[ b.pairOff[ i ] + s ];
+                    d2max = fmaxf( d2max, dd );
+                    bmax  = fmaxf( bmax, Ri * Ri + dd + Rl * Rl );
                 }
                 const uint32_t mk = __ballot_sync( 0xffffffffu, isP );
                 if ( isP )
                     m.plist[ p + __popc( mk & lanemask_lt() ) ] = (uint16_t)s;
                 p += __popc( mk );
+                if ( base < 64 )
+                    partial |= (uint64_t)mk << base;
             }
             for ( int o = 16; o > 0; o >>= 1 )
             {
@@ -1012,39 +1067,10 @@ namespace sesgb
             pb.eK    = 0.5f * kRel * ( bmax + 1.f );
             __syncwarp();
 
-            uint32_t       nCand = 0, nEnt = 0, nSing = 0, nReg = 0, cands = 0, fp64 = 0;
-            const uint32_t pairs = p * ( p > 0 ? p - 1 : 0 ) / 2;
-            for ( uint32_t q0 = 0; q0 < pairs || nCand > 0; q0 += 32 )
-            {
-                if ( q0 < pairs )
-                {
-                    // pair q = (a, bb), a < bb, row-major over the partial circles
-                    const uint32_t q   = q0 + lane;
-                    bool           isC = false;
-                    uint32_t       sj = 0, sk = 0;
-                    if ( q < pairs )
-                    {
-                        const float tp = 2.f * p - 1.f;
-                        int         a  = (int)floorf( 0.5f * ( tp - sqrtf( fmaxf( tp * tp - 8.f * (float)q, 0.f ) ) ) );
-                        a              = a < 0 ? 0 : a;
-                        while ( a > 0 && (uint32_t)( a * ( 2 * (int)p - a - 1 ) / 2 ) > q )
-                            a--;
-                        while ( (uint32_t)( ( a + 1 ) * ( 2 * (int)p - a - 2 ) / 2 ) <= q )
-                            a++;
-                        const uint32_t bb = (uint32_t)a + 1 + ( q - (uint32_t)( a * ( 2 * (int)p - a - 1 ) / 2 ) );
-                        sj                = m.plist[ a ];
-                        sk                = m.plist[ bb ];
-                        isC               = pair_is_neighbor( b, m, pb, sj, sk, fp64 );
-                    }
-                    const uint32_t mc = __ballot_sync( 0xffffffffu, isC );
-                    if ( isC )
-                        m.cand[ nCand + __popc( mc & lanemask_lt() ) ] = sj | ( sk << 16 );
-                    nCand += __popc( mc );
-                    cands += __popc( mc );
-                }
-                __syncwarp();
-                // process full batches of 32 candidates (and the rest at the end)
-                while ( nCand >= 32 || ( nCand > 0 && q0 + 32 >= pairs ) )
+            uint32_t nCand = 0, nEnt = 0, nSing = 0, nReg = 0, cands = 0, fp64 = 0;
+            // screens queued candidates 32 at a time (all of them when last)
+            auto screen_batches = [ & ]( bool last ) {
+                while ( nCand >= 32 || ( last && nCand > 0 ) )
                 {
                     const uint32_t batch = nCand < 32 ? nCand : 32;
                     int            w[ 2 ] = { 0, 0 };
@@ -1053,7 +1079,7 @@ namespace sesgb
                     if ( lane < batch )
                     {
                         sjk = m.cand[ lane ];
-                        probe_screen( m, pb, Ri, b.rp, ni, sjk & 0xffffu, sjk >> 16, w, band );
+                        probe_screen( m, pb, Ri, b.rp, ni, useMask, sjk & 0xffffu, sjk >> 16, w, band );
                     }
                     const uint32_t need = band ? 2u : ( w[ 0 ] != 0 ) + ( w[ 1 ] != 0 );
                     uint32_t       tot;
@@ -1087,6 +1113,65 @@ namespace sesgb
                             m.cand[ lane + 32 * r ] = keep[ r ];
                     __syncwarp();
                     nCand = rest;
+                }
+            };
+            auto enqueue = [ & ]( bool isC, uint32_t sj, uint32_t sk ) {
+                const uint32_t mc = __ballot_sync( 0xffffffffu, isC );
+                if ( isC )
+                    m.cand[ nCand + __popc( mc & lanemask_lt() ) ] = sj | ( sk << 16 );
+                nCand += __popc( mc );
+                cands += __popc( mc );
+                __syncwarp();
+            };
+            if ( useMask )
+            {
+                // circle by circle: the partial circles (i, k), k > j, whose far atom
+                // touches circle (i, j) and is a neighbour of j, in slot order
+                for ( uint32_t a = 0; a < p; a++ )
+                {
+                    const uint32_t sj = m.plist[ a ];
+                    const uint64_t w  = m.touch[ sj ] & partial & ( sj >= 63 ? 0ull : ~0ull << ( sj + 1 ) );
+                    for ( uint32_t h = 0; h < 2; h++ )
+                    {
+                        const uint32_t word = (uint32_t)( w >> ( 32 * h ) );
+                        if ( !word )
+                            continue;
+                        const uint32_t sk  = 32 * h + lane;
+                        const bool     isC = ( ( word >> lane ) & 1u ) && pair_is_neighbor( b, m, pb, sj, sk, fp64 );
+                        enqueue( isC, sj, sk );
+                        screen_batches( false );
+                    }
+                }
+                screen_batches( true );
+            }
+            else
+            {
+                const uint32_t pairs = p * ( p > 0 ? p - 1 : 0 ) / 2;
+                for ( uint32_t q0 = 0; q0 < pairs || nCand > 0; q0 += 32 )
+                {
+                    if ( q0 < pairs )
+                    {
+                        // pair q = (a, bb), a < bb, row-major over the partial circles
+                        const uint32_t q   = q0 + lane;
+                        bool           isC = false;
+                        uint32_t       sj = 0, sk = 0;
+                        if ( q < pairs )
+                        {
+                            const float tp = 2.f * p - 1.f;
+                            int         a  = (int)floorf( 0.5f * ( tp - sqrtf( fmaxf( tp * tp - 8.f * (float)q, 0.f ) ) ) );
+                            a              = a < 0 ? 0 : a;
+                            while ( a > 0 && (uint32_t)( a * ( 2 * (int)p - a - 1 ) / 2 ) > q )
+                                a--;
+                            while ( (uint32_t)( ( a + 1 ) * ( 2 * (int)p - a - 2 ) / 2 ) <= q )
+                                a++;
+                            const uint32_t bb = (uint32_t)a + 1 + ( q - (uint32_t)( a * ( 2 * (int)p - a - 1 ) / 2 ) );
+                            sj                = m.plist[ a ];
+                            sk                = m.plist[ bb ];
+                            isC               = pair_is_neighbor( b, m, pb, sj, sk, fp64 );
+                        }
+                        enqueue( isC, sj, sk );
+                    }
+                    screen_batches( q0 + 32 >= pairs );
                 }
             }
             for ( int o = 16; o > 0; o >>= 1 )

@@ -44,6 +44,9 @@ namespace sesgb
         uint8_t *  status;   // n * cap + 4 (whole 32-bit words for the flag updates)
         uint2 *    visBand;  // capVisBand: visibility tests left to double precision (i, s | k << 16)
         uint32_t   capVisBand;
+        uint32_t * pairOff;  // n + 1: first pair of each atom (exclusive count of the neighbour lists)
+        uint64_t * touch;    // capPairs, at pairOff[i] + s: neighbours that may hold a point of circle (i, s)
+        uint32_t   capPairs;
         uint32_t * slotTrim; // partial-circle number of each slot (exclusive count)
 
         // per-atom counts and offsets
