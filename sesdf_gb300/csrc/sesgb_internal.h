@@ -22,7 +22,8 @@ namespace sesgb
         uint32_t maxNbr;   // largest neighbour count seen (before truncation)
         uint32_t overflow; // bitmask, see Overflow
         uint32_t outside;  // atoms outside the reference grid
-        uint32_t fp64[ 8 ]; // predicate evaluations settled in double precision, see Fp64Stage
+        uint32_t fp64[ 7 ]; // predicate evaluations settled in double precision, see Fp64Stage
+        uint32_t bandJobs;  // probe candidates whose float32 screen hit the band (jobs from the top)
         uint32_t nbrTruncated;
         uint32_t segTruncated;
         uint32_t snbrTruncated;

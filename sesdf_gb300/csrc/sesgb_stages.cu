@@ -824,13 +824,14 @@ namespace sesgb
             uint32_t * cand;  // kCandBuf: slot j | slot k << 16
             uint2 *    ent;   // kProbeBuf: (slot j | slot k << 16, side | kind << 1 | (w + 4) << 2)
             uint64_t * touch; // kMaskSlots: slots of the atoms touching the partial circle (i, slot)
+            uint16_t * coff;  // kMaskSlots: first candidate of each partial circle (touch-mask enumeration)
         };
 
         __host__ __device__ inline size_t probe_smem_per_warp( uint32_t cap )
         {
             size_t b = (size_t)staged_rows( cap ) * ( 16 + 4 + 4 + 2 + 1 );
             b        = ( b + 15 ) & ~(size_t)15;
-            return b + kCandBuf * 4 + kProbeBuf * 8 + kMaskSlots * 8;
+            return b + kCandBuf * 4 + kProbeBuf * 8 + kMaskSlots * ( 8 + 2 );
         }
 
         __device__ inline ProbeSmem probe_smem( unsigned char * base, uint32_t capacity )
@@ -848,6 +849,8 @@ namespace sesgb
             m.ent = reinterpret_cast<uint2 *>( base + o );
             o += kProbeBuf * 8;
             m.touch = reinterpret_cast<uint64_t *>( base + o );
+            o += kMaskSlots * 8;
+            m.coff = reinterpret_cast<uint16_t *>( base + o );
             return m;
         }
 
@@ -1125,22 +1128,50 @@ namespace sesgb
             };
             if ( useMask )
             {
-                // circle by circle: the partial circles (i, k), k > j, whose far atom
-                // touches circle (i, j) and is a neighbour of j, in slot order
-                for ( uint32_t a = 0; a < p; a++ )
-                {
+                // for each partial circle (i, j): the partial circles (i, k), k > j, whose
+                // far atom touches circle (i, j); flattened over the circles in (j, k)
+                // slot order, 32 at a time, and kept when k is a neighbour of j
+                auto later = [ & ]( uint32_t a ) {
                     const uint32_t sj = m.plist[ a ];
-                    const uint64_t w  = m.touch[ sj ] & partial & ( sj >= 63 ? 0ull : ~0ull << ( sj + 1 ) );
-                    for ( uint32_t h = 0; h < 2; h++ )
+                    return m.touch[ sj ] & partial & ( sj >= 63 ? 0ull : ~0ull << ( sj + 1 ) );
+                };
+                uint32_t total = 0;
+                for ( uint32_t a0 = 0; a0 < p; a0 += 32 )
+                {
+                    const uint32_t a = a0 + lane;
+                    const uint32_t c = a < p ? (uint32_t)__popcll( later( a ) ) : 0u;
+                    uint32_t       tot;
+                    const uint32_t first = total + warp_exclusive_sum( c, tot );
+                    if ( a < p )
+                        m.coff[ a ] = (uint16_t)first;
+                    total += tot;
+                }
+                __syncwarp();
+                for ( uint32_t c0 = 0; c0 < total; c0 += 32 )
+                {
+                    const uint32_t c   = c0 + lane;
+                    bool           isC = false;
+                    uint32_t       sj = 0, sk = 0;
+                    if ( c < total )
                     {
-                        const uint32_t word = (uint32_t)( w >> ( 32 * h ) );
-                        if ( !word )
-                            continue;
-                        const uint32_t sk  = 32 * h + lane;
-                        const bool     isC = ( ( word >> lane ) & 1u ) && pair_is_neighbor( b, m, pb, sj, sk, fp64 );
-                        enqueue( isC, sj, sk );
-                        screen_batches( false );
+                        uint32_t lo = 0, hi = p; // last circle whose first candidate is <= c
+                        while ( hi - lo > 1 )
+                        {
+                            const uint32_t mid = ( lo + hi ) >> 1;
+                            if ( m.coff[ mid ] <= c )
+                                lo = mid;
+                            else
+                                hi = mid;
+                        }
+                        uint64_t w = later( lo );
+                        for ( uint32_t r = c - m.coff[ lo ]; r; r-- )
+                            w &= w - 1;
+                        sj  = m.plist[ lo ];
+                        sk  = (uint32_t)( __ffsll( (long long)w ) - 1 );
+                        isC = pair_is_neighbor( b, m, pb, sj, sk, fp64 );
                     }
+                    enqueue( isC, sj, sk );
+                    screen_batches( false );
                 }
                 screen_batches( true );
             }
@@ -1196,23 +1227,30 @@ namespace sesgb
             }
             chunk           = __shfl_sync( 0xffffffffu, chunk, 0 );
             const bool fits = chunk + kept <= b.capProbes;
-            // jobs: a fill entry is one job; a band candidate's two entries are one job (on its first entry)
-            uint32_t jobsHere = 0;
+            // jobs: a fill entry is one job (counted up from the bottom of the job array); a
+            // band candidate's two entries are one job on its first entry (counted down
+            // from the top), so that each kind runs with full warps
+            uint32_t fillHere = 0, bandHere = 0;
             for ( uint32_t q0 = 0; q0 < kept; q0 += 32 )
             {
-                const uint32_t q     = q0 + lane;
-                bool           isJob = false;
+                const uint32_t q    = q0 + lane;
+                bool           fill = false, band = false;
                 if ( q < kept && fits )
                 {
                     const uint32_t info = m.ent[ q ].y;
-                    isJob               = ( ( info >> 1 ) & 1u ) == kJobFill || ( info & 1u ) == 0u;
+                    fill                = ( ( info >> 1 ) & 1u ) == kJobFill;
+                    band                = !fill && ( info & 1u ) == 0u;
                 }
-                jobsHere += __popc( __ballot_sync( 0xffffffffu, isJob ) );
+                fillHere += __popc( __ballot_sync( 0xffffffffu, fill ) );
+                bandHere += __popc( __ballot_sync( 0xffffffffu, band ) );
             }
-            uint32_t jbase = 0;
-            if ( lane == 0 && jobsHere )
-                jbase = atomicAdd( &b.counts->jobs, jobsHere );
+            uint32_t jbase = 0, gbase = 0;
+            if ( lane == 0 && fillHere )
+                jbase = atomicAdd( &b.counts->jobs, fillHere );
+            if ( lane == 0 && bandHere )
+                gbase = atomicAdd( &b.counts->bandJobs, bandHere );
             jbase = __shfl_sync( 0xffffffffu, jbase, 0 );
+            gbase = __shfl_sync( 0xffffffffu, gbase, 0 );
             for ( uint32_t q0 = 0; q0 < kept; q0 += 32 )
             {
                 const uint32_t q     = q0 + lane;
@@ -1238,14 +1276,18 @@ namespace sesgb
                     isJob                   = kind == kJobFill || side == 0u;
                     en.y                    = side | ( kind << 8 );
                 }
-                const uint32_t mj = __ballot_sync( 0xffffffffu, isJob );
+                const bool     fill = isJob && ( en.y >> 8 ) == kJobFill;
+                const uint32_t mf   = __ballot_sync( 0xffffffffu, fill );
+                const uint32_t mb   = __ballot_sync( 0xffffffffu, isJob && !fill );
                 if ( isJob )
                 {
-                    const uint32_t slot = jbase + __popc( mj & lanemask_lt() );
+                    const uint32_t slot = fill ? jbase + __popc( mf & lanemask_lt() )
+                                               : b.capProbes - 1u - ( gbase + __popc( mb & lanemask_lt() ) );
                     if ( slot < b.capProbes )
                         b.jobs[ slot ] = make_uint4( chunk + q, i, en.x, en.y << 16 );
                 }
-                jbase += __popc( mj );
+                jbase += __popc( mf );
+                gbase += __popc( mb );
             }
             if ( lane == 0 )
             {
@@ -1264,12 +1306,14 @@ namespace sesgb
         // left open.
         __global__ void __launch_bounds__( 128 ) k_probe_jobs( Build b )
         {
-            const uint32_t nj   = min( b.counts->jobs, b.capProbes );
-            const double   rp   = (double)b.rp;
+            const uint32_t nFill = min( b.counts->jobs, b.capProbes );
+            const uint32_t nBand = min( b.counts->bandJobs, b.capProbes - nFill );
+            const double   rp    = (double)b.rp;
             uint32_t       fp64 = 0, full64 = 0;
-            for ( uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nj; t += gridDim.x * blockDim.x )
+            // fill jobs first, then the band jobs stored from the top of the array
+            for ( uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nFill + nBand; t += gridDim.x * blockDim.x )
             {
-                const uint4    jb   = b.jobs[ t ];
+                const uint4    jb   = b.jobs[ t < nFill ? t : b.capProbes - 1u - ( t - nFill ) ];
                 const uint32_t ent  = jb.x, i = jb.y;
                 const uint32_t sj   = jb.z & 0xffffu, sk = jb.z >> 16;
                 const uint32_t info = jb.w >> 16;
