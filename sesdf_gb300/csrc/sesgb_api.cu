@@ -263,9 +263,10 @@ namespace
         exclusive_scan( b.nbrCount, b.pairOff, n, nullptr, &d->P, sc, s );
         launch_visibility( b, s );
         mark( 3 );
-        exclusive_scan( b.visCnt, b.visOff, n, nullptr, &d->V, sc, s );
-        exclusive_scan( b.partCnt, b.partOff, n, nullptr, &d->C1, sc, s );
-        exclusive_scan( b.fullCnt, b.fullOff, n, nullptr, &d->F, sc, s );
+        {
+            const ScanJob jobs[] = { { b.visCnt, b.visOff, &d->V }, { b.partCnt, b.partOff, &d->C1 }, { b.fullCnt, b.fullOff, &d->F } };
+            exclusive_scan_many( jobs, 3, n, nullptr, sc, s );
+        }
         launch_emit( b, s );
 
         // D, E: probes
@@ -273,8 +274,10 @@ namespace
         launch_probes( b, s );
         launch_probe_jobs( b, s );
         mark( 5 );
-        exclusive_scan( b.singCnt, b.singOff, n, nullptr, &d->Q, sc, s );
-        exclusive_scan( b.regCnt, b.regOff, n, nullptr, &d->regTotal, sc, s );
+        {
+            const ScanJob jobs[] = { { b.singCnt, b.singOff, &d->Q }, { b.regCnt, b.regOff, &d->regTotal } };
+            exclusive_scan_many( jobs, 2, n, nullptr, sc, s );
+        }
         cudaMemsetAsync( b.ccount, 0, sizeof( uint32_t ) * ( b.capC1 + 1ull ), s );
         launch_place( b, s );
         mark( 6 );

@@ -82,6 +82,15 @@ namespace sesgb
     // out[n] = total; *total (device) = total when non-null. in == out allowed.
     void exclusive_scan( const uint32_t * in, uint32_t * out, uint64_t nHost, const uint32_t * nDevice, uint32_t * total,
                          void * scratch, cudaStream_t stream );
+    // up to three scans of the same length in two launches
+    struct ScanJob
+    {
+        const uint32_t * in;
+        uint32_t *       out;
+        uint32_t *       total;
+    };
+    void exclusive_scan_many( const ScanJob * jobs, int count, uint64_t nHost, const uint32_t * nDevice, void * scratch,
+                              cudaStream_t stream );
 
     // host-side count of kernel launches (sesgb_launch_count)
     void count_launches( uint32_t k );

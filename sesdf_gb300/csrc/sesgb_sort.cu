@@ -14,6 +14,7 @@ namespace sesgb
         constexpr int kScanThreads = 256;
         constexpr int kScanItems   = 8;
         constexpr int kScanTile    = kScanThreads * kScanItems;
+        constexpr int kScanArrays  = 3;
 
         __device__ __forceinline__ uint64_t scan_len( uint64_t nHost, const uint32_t * nDevice )
         {
@@ -49,13 +50,25 @@ namespace sesgb
             return r;
         }
 
-        __global__ void __launch_bounds__( kScanThreads ) k_tile_sums( const uint32_t * in, uint64_t nHost, const uint32_t * nDevice,
-                                                                        uint32_t * tileSums )
+        // Up to kScanArrays independent scans of the same length in one launch
+        // (blockIdx.y selects the array).
+        struct ScanArrays
+        {
+            const uint32_t * in[ kScanArrays ];
+            uint32_t *       out[ kScanArrays ];
+            uint32_t *       total[ kScanArrays ];
+        };
+
+        __global__ void __launch_bounds__( kScanThreads ) k_tile_sums( ScanArrays a, uint64_t nHost, const uint32_t * nDevice,
+                                                                        uint32_t * tileSums, uint32_t tiles )
         {
             __shared__ uint32_t warpSums[ 33 ];
             const uint64_t      n    = scan_len( nHost, nDevice );
             const uint64_t      base = (uint64_t)blockIdx.x * kScanTile;
-            uint32_t            s    = 0;
+            const uint32_t *    in   = a.in[ blockIdx.y ];
+            if ( base >= n )
+                return;
+            uint32_t s = 0;
 #pragma unroll
             for ( int k = 0; k < kScanItems; k++ )
             {
@@ -66,42 +79,39 @@ namespace sesgb
             uint32_t total;
             block_exclusive_sum( s, total, warpSums );
             if ( threadIdx.x == 0 )
-                tileSums[ blockIdx.x ] = total;
+                tileSums[ blockIdx.y * tiles + blockIdx.x ] = total;
         }
 
-        // single block: exclusive scan of the tile sums in place
-        __global__ void __launch_bounds__( 1024 ) k_scan_tile_sums( uint32_t * tileSums, uint32_t tiles, uint32_t * total,
-                                                                     uint32_t * outEnd, uint64_t nHost, const uint32_t * nDevice )
-        {
-            __shared__ uint32_t warpSums[ 33 ];
-            uint32_t            carry = 0;
-            for ( uint32_t base = 0; base < tiles; base += blockDim.x )
-            {
-                const uint32_t i = base + threadIdx.x;
-                const uint32_t v = i < tiles ? tileSums[ i ] : 0u;
-                uint32_t       t;
-                const uint32_t e = block_exclusive_sum( v, t, warpSums );
-                if ( i < tiles )
-                    tileSums[ i ] = e + carry;
-                carry += t;
-            }
-            if ( threadIdx.x == 0 )
-            {
-                if ( total )
-                    *total = carry;
-                outEnd[ scan_len( nHost, nDevice ) ] = carry;
-            }
-        }
-
-        __global__ void __launch_bounds__( kScanThreads ) k_tile_scan( const uint32_t * in, uint32_t * out, uint64_t nHost,
-                                                                        const uint32_t * nDevice, const uint32_t * tileOffsets )
+        // Each tile adds up the sums of the tiles before it (a few hundred at most
+        // for the sizes of the build), scans itself, and the tile holding the last
+        // element writes out[n] and the total.
+        __global__ void __launch_bounds__( kScanThreads ) k_tile_scan( ScanArrays a, uint64_t nHost, const uint32_t * nDevice,
+                                                                        const uint32_t * tileSums, uint32_t tiles )
         {
             __shared__ uint32_t tile[ kScanTile + kScanTile / 32 ];
             __shared__ uint32_t warpSums[ 33 ];
             const uint64_t      n    = scan_len( nHost, nDevice );
             const uint64_t      base = (uint64_t)blockIdx.x * kScanTile;
+            const uint32_t *    in   = a.in[ blockIdx.y ];
+            uint32_t *          out  = a.out[ blockIdx.y ];
+            if ( n == 0 )
+            {
+                if ( blockIdx.x == 0 && threadIdx.x == 0 )
+                {
+                    out[ 0 ] = 0;
+                    if ( a.total[ blockIdx.y ] )
+                        *a.total[ blockIdx.y ] = 0;
+                }
+                return;
+            }
             if ( base >= n )
                 return;
+            // offset of this tile
+            uint32_t before = 0;
+            for ( uint32_t t = threadIdx.x; t < blockIdx.x; t += kScanThreads )
+                before += tileSums[ blockIdx.y * tiles + t ];
+            uint32_t offsetTotal;
+            block_exclusive_sum( before, offsetTotal, warpSums );
             // coalesced load into a padded tile (index + index / 32 avoids bank conflicts)
 #pragma unroll
             for ( int k = 0; k < kScanItems; k++ )
@@ -120,8 +130,8 @@ namespace sesgb
                 v[ k ]           = tile[ j + j / 32 ];
                 s += v[ k ];
             }
-            uint32_t       total;
-            uint32_t       e   = block_exclusive_sum( s, total, warpSums ) + tileOffsets[ blockIdx.x ];
+            uint32_t total;
+            uint32_t e = block_exclusive_sum( s, total, warpSums ) + offsetTotal;
 #pragma unroll
             for ( int k = 0; k < kScanItems; k++ )
             {
@@ -137,6 +147,12 @@ namespace sesgb
                 const uint64_t i = base + j;
                 if ( i < n )
                     out[ i ] = tile[ j + j / 32 ];
+            }
+            if ( threadIdx.x == 0 && base + kScanTile >= n )
+            {
+                out[ n ] = offsetTotal + total;
+                if ( a.total[ blockIdx.y ] )
+                    *a.total[ blockIdx.y ] = offsetTotal + total;
             }
         }
 
@@ -219,20 +235,34 @@ namespace sesgb
     size_t scan_scratch_bytes( uint64_t n )
     {
         const uint64_t tiles = ( n + kScanTile - 1 ) / kScanTile + 1;
-        return ( tiles * sizeof( uint32_t ) + 255 ) & ~(size_t)255;
+        return ( kScanArrays * tiles * sizeof( uint32_t ) + 255 ) & ~(size_t)255;
     }
-
+    void exclusive_scan_many( const ScanJob * jobs, int count, uint64_t nHost, const uint32_t * nDevice, void * scratch,
+                              cudaStream_t stream )
+    {
+        ScanArrays a = {};
+        for ( int k = 0; k < count && k < kScanArrays; k++ )
+        {
+            a.in[ k ]    = jobs[ k ].in;
+            a.out[ k ]   = jobs[ k ].out;
+            a.total[ k ] = jobs[ k ].total;
+        }
+        const uint32_t tiles = (uint32_t)( ( nHost + kScanTile - 1 ) / kScanTile );
+        const dim3     grid( tiles > 0 ? tiles : 1u, (unsigned)( count < kScanArrays ? count : kScanArrays ) );
+        uint32_t *     tileSums = static_cast<uint32_t *>( scratch );
+        if ( tiles > 1 )
+        {
+            k_tile_sums<<<grid, kScanThreads, 0, stream>>>( a, nHost, nDevice, tileSums, tiles );
+            count_launches( 1 );
+        }
+        k_tile_scan<<<grid, kScanThreads, 0, stream>>>( a, nHost, nDevice, tileSums, tiles );
+        count_launches( 1 );
+    }
     void exclusive_scan( const uint32_t * in, uint32_t * out, uint64_t nHost, const uint32_t * nDevice, uint32_t * total,
                          void * scratch, cudaStream_t stream )
     {
-        const uint32_t tiles    = (uint32_t)( ( nHost + kScanTile - 1 ) / kScanTile );
-        uint32_t *     tileSums = static_cast<uint32_t *>( scratch );
-        if ( tiles > 0 )
-            k_tile_sums<<<tiles, kScanThreads, 0, stream>>>( in, nHost, nDevice, tileSums );
-        k_scan_tile_sums<<<1, 1024, 0, stream>>>( tileSums, tiles, total, out, nHost, nDevice );
-        if ( tiles > 0 )
-            k_tile_scan<<<tiles, kScanThreads, 0, stream>>>( in, out, nHost, nDevice, tileSums );
-        count_launches( tiles > 0 ? 3 : 1 );
+        const ScanJob job = { in, out, total };
+        exclusive_scan_many( &job, 1, nHost, nDevice, scratch, stream );
     }
 
     size_t radix_scratch_bytes( uint32_t n )

@@ -124,6 +124,38 @@ namespace sesgb
                 }
         }
 
+        // Bitonic sort of up to 64 keys held in registers, two per lane: key
+        // index lane + 32 r is held in v[r]; ascending on return.
+        __device__ __forceinline__ void warp_sort64( uint32_t & v0, uint32_t & v1, bool two )
+        {
+            const uint32_t lane = lane_id();
+            const uint32_t top  = two ? 64u : 32u;
+            for ( uint32_t k = 2; k <= top; k <<= 1 )
+                for ( uint32_t j = k >> 1; j > 0; j >>= 1 )
+                {
+                    if ( j == 32 )
+                    {
+                        // partner in the lane's other register; k == 64: ascending
+                        const uint32_t lo = min( v0, v1 ), hi = max( v0, v1 );
+                        v0 = lo;
+                        v1 = hi;
+                        continue;
+                    }
+                    const bool lower = ( lane & j ) == 0;
+                    {
+                        const uint32_t p   = __shfl_xor_sync( 0xffffffffu, v0, j );
+                        const bool     asc = ( lane & k ) == 0;
+                        v0                 = ( lower == asc ) ? min( v0, p ) : max( v0, p );
+                    }
+                    if ( two )
+                    {
+                        const uint32_t p   = __shfl_xor_sync( 0xffffffffu, v1, j );
+                        const bool     asc = ( ( lane + 32u ) & k ) == 0;
+                        v1                 = ( lower == asc ) ? min( v1, p ) : max( v1, p );
+                    }
+                }
+        }
+
         // ------------------------------------------------------------------
         __global__ void k_hash( Build b )
         {
@@ -245,10 +277,24 @@ namespace sesgb
             }
             __syncwarp();
             const uint32_t held = count < kNbrBuf ? count : kNbrBuf;
-            warp_bitonic_sort<uint32_t>( buf[ warp ], held, kNbrBuf, 0xffffffffu );
             const uint32_t kept = held < b.cap ? held : b.cap;
-            for ( uint32_t s = lane; s < kept; s += 32 )
-                b.nbr[ (size_t)i * b.cap + s ] = buf[ warp ][ s ];
+            if ( held <= 64 )
+            {
+                // in registers (the common case)
+                uint32_t v0 = lane < held ? buf[ warp ][ lane ] : 0xffffffffu;
+                uint32_t v1 = lane + 32 < held ? buf[ warp ][ lane + 32 ] : 0xffffffffu;
+                warp_sort64( v0, v1, held > 32 );
+                if ( lane < kept )
+                    b.nbr[ (size_t)i * b.cap + lane ] = v0;
+                if ( lane + 32 < kept )
+                    b.nbr[ (size_t)i * b.cap + lane + 32 ] = v1;
+            }
+            else
+            {
+                warp_bitonic_sort<uint32_t>( buf[ warp ], held, kNbrBuf, 0xffffffffu );
+                for ( uint32_t s = lane; s < kept; s += 32 )
+                    b.nbr[ (size_t)i * b.cap + s ] = buf[ warp ][ s ];
+            }
             for ( int o = 16; o > 0; o >>= 1 )
                 fp64 += __shfl_xor_sync( 0xffffffffu, fp64, o );
             if ( lane == 0 )
