@@ -311,13 +311,12 @@ namespace sesgb
         }
 
         // ---- circle visibility ----------------------------------------------
-        // Warp per atom i. The circles (i, s) are processed kVisCircles at a time,
-        // one group of kVisGroup lanes per circle, each lane testing the k of its
-        // residue class (k = lane in group + kVisGroup u). The neighbourhood is
-        // staged in shared memory as (d_k, K_k, |d_k|^2) relative to atom i; a test
-        // is then sqrt- and division-free: with t the axial offset of the circle
-        // (centre c = t d_j), g = d_j . d_k and p^2 = |d_k|^2 - g^2 / |d_j|^2 (k's
-        // distance from the circle axis, squared)
+        // Warp per atom i, lane per circle (i, s): every lane tests its circle
+        // against the same k in turn. The neighbourhood is staged in shared memory
+        // as (d_k, K_k, |d_k|^2) relative to atom i; a test is then sqrt- and
+        // division-free: with t the axial offset of the circle (centre c = t d_j),
+        // g = d_j . d_k and p^2 = |d_k|^2 - g^2 / |d_j|^2 (k's distance from the
+        // circle axis, squared)
         //     A = R_i^2 + |d_k|^2 - R_k^2 - 1e-4 - 2 t g      (= |c - d_k|^2 + r^2 - R_k^2 - 1e-4)
         //     G = A^2 - 4 r^2 p^2,
         // k holds the whole circle iff A < 0 and G > 0 and touches it iff A < 0
@@ -325,8 +324,6 @@ namespace sesgb
         // operations.cu:164-197). Tests inside the float32 error band go to a
         // queue that k_visibility_band decides in double precision with full
         // warps; k_visibility_final turns the flags into statuses and counts.
-        constexpr int kVisGroup   = 4;              // lanes per circle
-        constexpr int kVisCircles = 32 / kVisGroup; // circles per warp step
         constexpr int kVisQueue   = 128;            // band tests a warp holds before they go to the global queue
         constexpr int kMaskSlots  = 64;             // atoms with at most this many neighbours keep touch masks
 
@@ -343,8 +340,8 @@ namespace sesgb
 
         struct VisSmem
         {
-            float4 *   rel;   // rows + kVisGroup: d_k, R_i^2 + |d_k|^2 - R_k^2 - 1e-4 (padding: never touches)
-            float *    dd;    // rows + kVisGroup: |d_k|^2
+            float4 *   rel;   // rows + 32: d_k, R_i^2 + |d_k|^2 - R_k^2 - 1e-4 (padding: never touches)
+            float *    dd;    // rows + 32: |d_k|^2
             uint8_t *  res;   // rows: kVis* flags
             uint16_t * list;  // rows: circles to evaluate
             uint32_t * queue; // kVisQueue: s | k << 16
@@ -352,13 +349,13 @@ namespace sesgb
 
         __host__ __device__ inline size_t vis_smem_per_warp( uint32_t cap )
         {
-            const size_t r = staged_rows( cap ) + kVisGroup;
+            const size_t r = staged_rows( cap ) + 32;
             return ( ( r * ( 16 + 4 + 1 + 2 ) + 15 ) & ~(size_t)15 ) + kVisQueue * 4;
         }
 
         __device__ inline VisSmem vis_smem( unsigned char * base, uint32_t cap )
         {
-            const size_t r = staged_rows( cap ) + kVisGroup;
+            const size_t r = staged_rows( cap ) + 32;
             VisSmem      m;
             m.rel   = reinterpret_cast<float4 *>( base );
             m.dd    = reinterpret_cast<float *>( base + r * 16 );
@@ -432,13 +429,13 @@ namespace sesgb
             const float4   ai  = b.atoms[ i ];
             const float    Ri  = ai.w + b.rp;
             const size_t   row = (size_t)i * b.cap;
-            const uint32_t U   = ( ni + kVisGroup - 1 ) / kVisGroup; // tests per lane and circle
 
-            // stage the neighbourhood and the list of circles to evaluate (the
-            // exterior build evaluates circles (i, j) with i < j only)
+            // stage the neighbourhood (padded by 32 far slots) and the list of
+            // circles to evaluate (the exterior build evaluates circles (i, j) with
+            // i < j only)
             float    d2max = 0.f, r2max = 0.f;
             uint32_t nc    = 0;
-            for ( uint32_t base = 0; base < U * kVisGroup; base += 32 )
+            for ( uint32_t base = 0; base < ni + 32; base += 32 )
             {
                 const uint32_t s    = base + lane;
                 bool           eval = false;
@@ -456,9 +453,9 @@ namespace sesgb
                     d2max             = fmaxf( d2max, dd );
                     r2max             = fmaxf( r2max, Rk * Rk );
                 }
-                else if ( s < U * kVisGroup )
+                else if ( s < ni + 32 )
                 {
-                    // padding up to a whole number of tests per lane: far away, never undecided
+                    // padding for the rounded-up test loops: far away, never undecided
                     m.rel[ s ] = make_float4( 0.f, 0.f, 0.f, 1e15f );
                     m.dd[ s ]  = 1e15f;
                 }
@@ -476,85 +473,95 @@ namespace sesgb
             const float theta = kRel * ( d2max + 1.f );
             __syncwarp();
 
-            const uint32_t grp = lane / kVisGroup, gl = lane % kVisGroup;
-            const uint32_t gmask = ( ( 1u << kVisGroup ) - 1u ) << ( grp * kVisGroup );
-            uint32_t       nq = 0;
-            // queues the tests of bits w (k = gl + kVisGroup (u0 + bit)) of circle s
-            auto queue_tests = [ & ]( uint32_t w, uint32_t u0, uint32_t s ) {
-                uint32_t tot;
-                uint32_t at = nq + warp_exclusive_sum( (uint32_t)__popc( w ), tot );
-                for ( ; w; w &= w - 1 )
-                {
-                    const uint32_t k = gl + kVisGroup * ( u0 + (uint32_t)( __ffs( w ) - 1 ) );
-                    if ( at < (uint32_t)kVisQueue )
-                        m.queue[ at ] = s | ( k << 16 );
-                    else
-                        band_push( b, i, s | ( k << 16 ) ); // the warp's queue is full
-                    at++;
-                }
-                nq = min( nq + tot, (uint32_t)kVisQueue );
-            };
-            for ( uint32_t c0 = 0; c0 < nc; c0 += kVisCircles )
+            uint32_t nq = 0;
+            // Circles go 32 at a time, one per lane, each lane looping over all k
+            // (the same k in every lane: shared-memory broadcasts). A last step with
+            // fewer circles spreads the k of each circle over a group of G lanes
+            // (k = lane in group + G u).
+            for ( uint32_t c0 = 0; c0 < nc; )
             {
+                const uint32_t rem = nc - c0;
+                uint32_t       G   = 1;
+                if ( rem < 32 )
+                    while ( rem * G * 2 <= 32 )
+                        G <<= 1;
+                const uint32_t grp = lane / G, gl = lane % G;
+                const uint32_t gmask = ( G == 32 ? 0xffffffffu : ( ( 1u << G ) - 1u ) ) << ( grp * G );
                 const uint32_t ci    = c0 + grp;
-                const bool     valid = ci < nc;
-                const uint32_t s     = m.list[ valid ? ci : 0u ];
+                const bool     valid = grp < 32 / G && ci < nc;
+                const uint32_t s     = m.list[ valid ? ci : c0 ];
+                const uint32_t U     = ( ni + G - 1 ) / G; // tests per lane
                 bool           bur = false, tch = false;
-                uint32_t       und = 0; // bit u: the test of k = gl + kVisGroup (u0 + u) is left to double precision
-                uint32_t       tou = 0; // bit u: that k touches the circle or is undecided
-                uint32_t       u0  = 0;
+                uint32_t       und[ 2 ] = { 0, 0 }, tou[ 2 ] = { 0, 0 }; // bit u of word w: k = gl + G (32 w + u)
                 {
                     const VisCircle v = vis_circle( Ri, Mc, theta, m.rel[ s ], m.dd[ s ] );
-                    for ( ;; )
+                    for ( uint32_t u0 = 0; u0 < U; u0 += 32 )
                     {
                         const uint32_t uN = U - u0 < 32 ? U - u0 : 32;
-                        const float4 * qp = m.rel + gl + kVisGroup * u0;
-                        const float *  dp = m.dd + gl + kVisGroup * u0;
-#pragma unroll 3
+                        const float4 * qp = m.rel + gl + G * u0;
+                        const float *  dp = m.dd + gl + G * u0;
+                        uint32_t       uw = 0, tw = 0;
+#pragma unroll 4
                         for ( uint32_t u = 0; u < uN; u++ )
                         {
-                            const float4 q  = qp[ kVisGroup * u ];
-                            const float  dk = dp[ kVisGroup * u ];
+                            const float4 q  = qp[ G * u ];
+                            const float  dk = dp[ G * u ];
                             const float  g  = v.dj.x * q.x + v.dj.y * q.y + v.dj.z * q.z;
                             const float  A  = fmaf( v.m2t, g, q.w );
                             const float  p2 = fmaf( -g * v.inv, g, dk );
-                            const float  G  = fmaf( A, A, -v.r2x4 * p2 );
+                            const float  G2 = fmaf( A, A, -v.r2x4 * p2 );
                             const float  eG = fmaf( v.alpha, fabsf( A ), fmaf( v.beta, p2, v.gamma ) );
                             // false on NaN: the test is then left to double precision
-                            const bool ok  = ( p2 > v.theta ) & ( fabsf( A ) > v.eA ) & ( fabsf( G ) > eG );
+                            const bool ok  = ( p2 > v.theta ) & ( fabsf( A ) > v.eA ) & ( fabsf( G2 ) > eG );
                             const bool neg = A < 0.f;
-                            bur            = bur | ( ok & neg & ( G > 0.f ) );
-                            tch            = tch | ( ok & ( neg | ( G < 0.f ) ) );
-                            und |= (uint32_t)!ok << u;
-                            tou |= (uint32_t)( !ok | neg | ( G < 0.f ) ) << u;
+                            bur            = bur | ( ok & neg & ( G2 > 0.f ) );
+                            tch            = tch | ( ok & ( neg | ( G2 < 0.f ) ) );
+                            uw |= (uint32_t)!ok << u;
+                            tw |= (uint32_t)( !ok | neg | ( G2 < 0.f ) ) << u;
                         }
                         // the circle's own j is always undecided and never tested
-                        const uint32_t us = s / kVisGroup;
-                        if ( gl == s % kVisGroup && us >= u0 && us < u0 + uN )
-                            und &= ~( 1u << ( us - u0 ) );
-                        if ( u0 + 32 >= U )
-                            break;
-                        // more than 32 tests per lane: earlier bits go out now (no buried filter)
+                        const uint32_t us = s / G;
+                        if ( gl == s % G && us >= u0 && us < u0 + uN )
+                            uw &= ~( 1u << ( us - u0 ) );
                         if ( !valid )
-                            und = 0;
-                        if ( __any_sync( 0xffffffffu, und != 0 ) )
-                            queue_tests( und, u0, s );
-                        und = 0;
-                        u0 += 32;
+                            uw = 0;
+                        if ( u0 < 64 )
+                        {
+                            und[ u0 / 32 ] = uw;
+                            tou[ u0 / 32 ] = tw;
+                        }
+                        else if ( __any_sync( 0xffffffffu, uw != 0 ) )
+                        {
+                            // more than 64 tests per lane: these go out now (no buried filter)
+                            uint32_t tot;
+                            uint32_t at = nq + warp_exclusive_sum( (uint32_t)__popc( uw ), tot );
+                            for ( uint32_t w = uw; w; w &= w - 1 )
+                            {
+                                const uint32_t k = gl + G * ( u0 + (uint32_t)( __ffs( w ) - 1 ) );
+                                if ( at < (uint32_t)kVisQueue )
+                                    m.queue[ at ] = s | ( k << 16 );
+                                else
+                                    band_push( b, i, s | ( k << 16 ) );
+                                at++;
+                            }
+                            nq = min( nq + tot, (uint32_t)kVisQueue );
+                        }
                     }
                 }
-                if ( U <= (uint32_t)( kMaskSlots / kVisGroup ) )
+                const bool gb = ( __ballot_sync( 0xffffffffu, bur ) & gmask ) != 0;
+                const bool gt = ( __ballot_sync( 0xffffffffu, tch ) & gmask ) != 0;
+                if ( ni <= (uint32_t)kMaskSlots )
                 {
-                    // touch mask of the circle over slots 0..63 (slot gl + kVisGroup u from lane gl, bit u):
-                    // the atoms that may hold a point of it; k_probes tests only those
-                    uint64_t x = tou & 0xffffu;
-                    x          = ( x | ( x << 24 ) ) & 0x000000FF000000FFull;
-                    x          = ( x | ( x << 12 ) ) & 0x000F000F000F000Full;
-                    x          = ( x | ( x << 6 ) ) & 0x0303030303030303ull;
-                    x          = ( x | ( x << 3 ) ) & 0x1111111111111111ull;
-                    x <<= gl;
-                    x |= __shfl_xor_sync( 0xffffffffu, x, 1 );
-                    x |= __shfl_xor_sync( 0xffffffffu, x, 2 );
+                    // touch mask of the circle over slots 0..63: the atoms that may hold
+                    // a point of it (k_probes tests only those)
+                    uint64_t x = 0;
+                    if ( G == 1 )
+                        x = (uint64_t)tou[ 0 ] | ( (uint64_t)tou[ 1 ] << 32 );
+                    else
+                        for ( uint32_t w = tou[ 0 ]; w; w &= w - 1 )
+                            x |= 1ull << ( gl + G * (uint32_t)( __ffs( w ) - 1 ) );
+                    for ( uint32_t o = 1; o < G; o <<= 1 )
+                        x |= __shfl_xor_sync( 0xffffffffu, x, o );
                     if ( valid && gl == 0 && ( m.res[ s ] & kVisUpper ) )
                     {
                         const uint32_t at = b.pairOff[ i ] + s;
@@ -564,15 +571,29 @@ namespace sesgb
                             atomicOr( &b.counts->overflow, (uint32_t)kOverflowPairs );
                     }
                 }
-                const bool gb = ( __ballot_sync( 0xffffffffu, bur ) & gmask ) != 0;
-                const bool gt = ( __ballot_sync( 0xffffffffu, tch ) & gmask ) != 0;
                 if ( valid && gl == 0 && ( gb || gt ) )
                     atomicOr( reinterpret_cast<uint32_t *>( m.res ) + ( s >> 2 ),
                               (uint32_t)( ( gb ? kVisBuried : 0 ) | ( gt ? kVisTouched : 0 ) ) << ( 8 * ( s & 3 ) ) );
-                if ( !valid || gb )
-                    und = 0;
-                if ( __any_sync( 0xffffffffu, und != 0 ) )
-                    queue_tests( und, u0, s );
+                // queue the undecided tests of circles not buried in float32
+                if ( gb )
+                    und[ 0 ] = und[ 1 ] = 0;
+                if ( __any_sync( 0xffffffffu, ( und[ 0 ] | und[ 1 ] ) != 0 ) )
+                {
+                    uint32_t tot;
+                    uint32_t at = nq + warp_exclusive_sum( (uint32_t)( __popc( und[ 0 ] ) + __popc( und[ 1 ] ) ), tot );
+                    for ( uint32_t h = 0; h < 2; h++ )
+                        for ( uint32_t w = und[ h ]; w; w &= w - 1 )
+                        {
+                            const uint32_t k = gl + G * ( 32 * h + (uint32_t)( __ffs( w ) - 1 ) );
+                            if ( at < (uint32_t)kVisQueue )
+                                m.queue[ at ] = s | ( k << 16 );
+                            else
+                                band_push( b, i, s | ( k << 16 ) ); // the warp's queue is full
+                            at++;
+                        }
+                    nq = min( nq + tot, (uint32_t)kVisQueue );
+                }
+                c0 += 32 / G;
             }
             __syncwarp();
             // hand the band tests of circles not buried in float32 to the double-precision pass
