@@ -140,11 +140,15 @@ def workload(name: str):
     raise ValueError(name)
 
 
-def time_ours(atoms, mode, steps, warmup, flush):
-    """Device-timed builds from atoms resident in HBM; returns per-step ms, launches, context."""
+def time_ours(atoms, mode, steps, warmup, flush, stages=None):
+    """Device-timed builds from atoms resident in HBM; returns per-step ms, launches, context.
+
+    With `stages` (a dict), the builds also record CUDA events between their
+    stages (on the build's stream) and the dict receives the per-stage
+    milliseconds averaged over the timed builds."""
     import torch
     from sesdf_gb300 import SesBuild, api
-    g = SesBuild(atoms, RP, mode)
+    g = SesBuild(atoms, RP, mode, profile=stages is not None)
     d_atoms = torch.from_numpy(atoms).cuda()
     stream = torch.cuda.current_stream()
     for _ in range(max(warmup, 1)):
@@ -161,6 +165,10 @@ def time_ours(atoms, mode, steps, warmup, flush):
         g.build_async(d_atoms.data_ptr(), stream.cuda_stream)
         ends[k].record(stream)
         g.finish()
+        if stages is not None:
+            for name, v in g.stage_times().items():
+                if name:
+                    stages[name] = stages.get(name, 0.0) + v / steps
     torch.cuda.synchronize()
     launches = api.launch_count() - l0
     ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
@@ -189,39 +197,38 @@ def time_e2e(atoms, mode, steps, warmup, flush):
     return ms
 
 
-def stage_profile(atoms, mode, steps):
-    """Per-stage milliseconds (CUDA events between stages), averaged over `steps` builds."""
-    import torch
-    from sesdf_gb300 import SesBuild
-    g = SesBuild(atoms, RP, mode, profile=True)
-    d = torch.from_numpy(atoms).cuda()
-    stream = torch.cuda.current_stream()
-    g.build_async(d.data_ptr(), stream.cuda_stream)
-    g.finish()
-    acc = {}
-    for _ in range(steps):
-        g.build_async(d.data_ptr(), stream.cuda_stream)
-        g.finish()
-        for k, v in g.stage_times().items():
-            acc[k] = acc.get(k, 0.0) + v / steps
-    counts = g.counts()
-    nbr = g.analysis(1, np.uint32)  # neighbour counts
-    g.close()
-    return acc, counts, nbr
+def profiled_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` from its committed ncu summary (profiles/), or None."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles", f"{kernel}_assembly100k.txt")
+    try:
+        with open(path) as f:
+            for line in f:
+                if line.startswith("dram_bytes_per_launch:"):
+                    return int(line.split(":", 1)[1].strip())
+    except OSError:
+        pass
+    return None
 
 
 def roofline(stages, counts, nbr, n_atoms):
-    """Visibility kernel (one launch per build): algorithmic bytes and flops per launch."""
+    """The dominant kernel of the build (k_visibility or k_probes, one launch per build):
+    algorithmic bytes and flops per launch over its CUDA-event time in the timed builds."""
     hbm, sm_max, src = peaks()
-    P = counts["pairs"]
-    pair_tests = float(np.sum(nbr.astype(np.float64) * np.maximum(nbr.astype(np.float64) - 1, 0)))
-    ms = stages["visibility"]
-    bytes_alg = 21.0 * P + 32.0 * n_atoms  # neighbour ids + neighbour atoms + status + per-atom I/O
-    flops_alg = 30.0 * pair_tests           # one circle-vs-atom test
-    achieved = bytes_alg / (ms * 1e-3) / 1e9
+    P, C1, I = counts["pairs"], counts["partial_circles"], counts["probes"]
+    nb = nbr.astype(np.float64)
     fp32_peak = FP32_LANES * 2 * sm_max * 1e6 / 1e12
-    return {"kernel": "k_visibility", "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-            "frac": round(achieved / hbm, 4), "traffic": None, "peak_source": src,
+    if stages.get("probes", 0.0) > stages.get("visibility", 0.0):
+        kernel, ms = "k_probes", stages["probes"]
+        # staged neighbourhood (ids, atoms, statuses, neighbour counts), touch masks, staged probes and jobs
+        bytes_alg = 25.0 * P + 8.0 * C1 + 64.0 * I + 36.0 * n_atoms
+        flops_alg = 180.0 * counts.get("candidates", 0)  # solve, plane occlusion tests, singular test
+    else:
+        kernel, ms = "k_visibility", stages["visibility"]
+        bytes_alg = 21.0 * P + 32.0 * n_atoms  # neighbour ids + neighbour atoms + status + per-atom I/O
+        flops_alg = 30.0 * float(np.sum(nb * np.maximum(nb - 1, 0)))  # one circle-vs-atom test
+    achieved = bytes_alg / (ms * 1e-3) / 1e9
+    return {"kernel": kernel, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
+            "frac": round(achieved / hbm, 4), "traffic": profiled_traffic(kernel), "peak_source": src,
             "ms_per_launch": round(ms, 4), "bytes_per_launch": bytes_alg,
             "alu": {"flops_per_launch": flops_alg, "achieved_tflops": round(flops_alg / (ms * 1e-3) / 1e12, 2),
                     "fp32_nominal_tflops": round(fp32_peak, 1),
@@ -253,13 +260,15 @@ def run_ours(args, rank, world, local):
     torch.cuda.synchronize()
     sampler.start()
     t_wall = time.perf_counter()
-    ms, launches, g = time_ours(atoms, "full", args.steps, args.warmup, flush)
+    stages = {}
+    ms, launches, g = time_ours(atoms, "full", args.steps, args.warmup, flush, stages)
     torch.cuda.synchronize()
     barrier(world)
     wall = time.perf_counter() - t_wall
     clocks = sampler.stop()
     total_ms = max_over_ranks(float(np.sum(ms)), world)
     counts = g.counts()
+    nbr = g.analysis(1, np.uint32)  # neighbour counts
     g.close()
     value = n * args.steps * world / (total_ms * 1e-3)
     if args.kernels_only:
@@ -288,8 +297,7 @@ def run_ours(args, rank, world, local):
             gs.close()
         del shell
 
-    stages, pc, nbr = stage_profile(atoms, "full", 5)
-    roof = roofline(stages, pc, nbr, n)
+    roof = roofline(stages, counts, nbr, n)
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": "atoms/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,

@@ -230,8 +230,8 @@ namespace
         c->graph     = nullptr;
     }
 
-    const char * kStageNames[] = { "grid", "neighbors", "visibility", "circles", "probes",
-                                   "place", "", "segments", "probe_neighbors", "tori" };
+    const char * kStageNames[] = { "grid",       "neighbors", "visibility", "circles",         "probes",
+                                   "probe_jobs", "place",     "segments",   "probe_neighbors", "tori" };
 
     // all launches of one build; no host synchronisation inside
     void enqueue( sesgb_ctx * c, cudaStream_t s, bool profile )
@@ -257,12 +257,13 @@ namespace
         launch_cells( b, b.atoms, n, nullptr, sc, s );
         mark( 1 );
         launch_neighbors( b, s );
+        exclusive_scan( b.nbrCount, b.pairOff, n, nullptr, &d->P, sc, s );
 
         // B, C: visibility, sectors, complete and partial circles
         mark( 2 );
-        exclusive_scan( b.nbrCount, b.pairOff, n, nullptr, &d->P, sc, s );
         launch_visibility( b, s );
         mark( 3 );
+        launch_visibility_resolve( b, s );
         {
             const ScanJob jobs[] = { { b.visCnt, b.visOff, &d->V }, { b.partCnt, b.partOff, &d->C1 }, { b.fullCnt, b.fullOff, &d->F } };
             exclusive_scan_many( jobs, 3, n, nullptr, sc, s );
@@ -272,15 +273,15 @@ namespace
         // D, E: probes
         mark( 4 );
         launch_probes( b, s );
-        launch_probe_jobs( b, s );
         mark( 5 );
+        launch_probe_jobs( b, s );
+        mark( 6 );
         {
             const ScanJob jobs[] = { { b.singCnt, b.singOff, &d->Q }, { b.regCnt, b.regOff, &d->regTotal } };
             exclusive_scan_many( jobs, 2, n, nullptr, sc, s );
         }
         cudaMemsetAsync( b.ccount, 0, sizeof( uint32_t ) * ( b.capC1 + 1ull ), s );
         launch_place( b, s );
-        mark( 6 );
         mark( 7 );
 
         // F: segments

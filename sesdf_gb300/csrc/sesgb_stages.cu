@@ -1925,9 +1925,15 @@ namespace sesgb
         if ( !b.n )
             return;
         k_visibility<<<blocks_for( b.n, kWarpsPerBlock ), 32 * kWarpsPerBlock, visibility_smem( b.cap ), s>>>( b );
+        counted();
+    }
+    void launch_visibility_resolve( const Build & b, cudaStream_t s )
+    {
+        if ( !b.n )
+            return;
         k_visibility_band<<<min( persistent_blocks( 128 ), blocks_for( b.capVisBand, 128 ) + 1 ), 128, 0, s>>>( b );
         k_visibility_final<<<blocks_for( b.n, kWarpsPerBlock ), 32 * kWarpsPerBlock, 0, s>>>( b );
-        counted( 3 );
+        counted( 2 );
     }
     void launch_emit( const Build & b, cudaStream_t s )
     {

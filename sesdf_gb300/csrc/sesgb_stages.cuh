@@ -101,6 +101,7 @@ namespace sesgb
                        cudaStream_t s );
     void launch_neighbors( const Build & b, cudaStream_t s );
     void launch_visibility( const Build & b, cudaStream_t s );
+    void launch_visibility_resolve( const Build & b, cudaStream_t s );
     void launch_emit( const Build & b, cudaStream_t s );
     void launch_probes( const Build & b, cudaStream_t s );
     void launch_probe_jobs( const Build & b, cudaStream_t s );
