@@ -204,6 +204,30 @@ const char * sesgb_stage_name( uint32_t stage );
 int sesgb_sort_atoms_noalloc( const void * device_atoms, uint32_t n, const float * aabb, float probe_radius,
                               void * device_sorted_atoms, uint32_t * device_sorted_to_input, void * stream );
 
+/* Batches (no counterpart in the reference, which builds one molecule per
+ * Sesdf object): `molecules` molecules whose atoms are concatenated in `atoms`
+ * (host, float4), molecule m owning atoms [molecule_start[m],
+ * molecule_start[m + 1]) (molecule_start[0] = 0, non-decreasing). One build
+ * covers all of them with the same fixed launch sequence as a single molecule
+ * (capturable in a CUDA graph with SESGB_FLAG_GRAPH): every molecule keeps the
+ * reference grid of its own construction (getAabb of its atoms), its own
+ * neighbour grid and its own singular-first probe order, so that molecule m's
+ * slice of the batch equals, buffer for buffer and id for id, what
+ * sesgb_create + sesgb_build give for that molecule alone. The analysis buffers
+ * (sesgb_analysis_buffer) stay in batch-wide numbering. */
+int      sesgb_create_batch( const float * atoms, const uint32_t * molecule_start, uint32_t molecules,
+                             float probe_radius, int mode, const sesgb_options * options, sesgb_ctx ** out );
+uint32_t sesgb_batch_molecules( const sesgb_ctx * ctx );
+/* Per-molecule record of the last build, SESGB_MOL_FIELDS values: atoms, sectors,
+ * complete circles, partial circles, probes, singular probes, segments, tori, then
+ * the first index of each of those in the batch buffers (atoms, sectors, complete
+ * circles, partial circles, probes, singular probes, segments, tori). */
+#define SESGB_MOL_FIELDS 16
+int sesgb_molecule_record( const sesgb_ctx * ctx, uint32_t molecule, uint32_t * record );
+/* getData of one molecule of a batch: pointers into the batch buffers, molecule-local ids. */
+int sesgb_get_full_molecule( sesgb_ctx * ctx, uint32_t molecule, sesgb_full_data * out );
+int sesgb_get_exterior_molecule( sesgb_ctx * ctx, uint32_t molecule, sesgb_exterior_data * out );
+
 /* Number of kernels this library has launched in this process (host-side count). */
 uint64_t sesgb_launch_count( void );
 

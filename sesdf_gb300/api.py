@@ -30,7 +30,12 @@ EXPORTS = [
     "sesgb_max_neighbor_per_atom", "sesgb_max_intersections_per_circle", "sesgb_max_intersection_neighbors",
     "sesgb_error_string", "sesgb_last_error", "sesgb_destroy", "sesgb_stage_times", "sesgb_stage_name",
     "sesgb_launch_count", "sesgb_build_async", "sesgb_finish", "sesgb_sort_atoms_noalloc",
+    "sesgb_create_batch", "sesgb_batch_molecules", "sesgb_molecule_record", "sesgb_get_full_molecule",
+    "sesgb_get_exterior_molecule",
 ]
+MOL_FIELDS = ["atoms", "sectors", "full_circles", "partial_circles", "probes", "singular_probes", "segments", "tori",
+              "atom_base", "sector_base", "full_base", "partial_base", "probe_base", "singular_base", "segment_base",
+              "tori_base"]
 NOALLOC_MAX_ATOMS = 262144
 
 
@@ -115,6 +120,12 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         lib.sesgb_finish.argtypes = [P]
         lib.sesgb_launch_count.argtypes = []
         lib.sesgb_launch_count.restype = ctypes.c_uint64
+        lib.sesgb_create_batch.argtypes = [P, P, U32, F32, I32, ctypes.POINTER(Options), ctypes.POINTER(P)]
+        lib.sesgb_batch_molecules.argtypes = [P]
+        lib.sesgb_batch_molecules.restype = U32
+        lib.sesgb_molecule_record.argtypes = [P, U32, P]
+        lib.sesgb_get_full_molecule.argtypes = [P, U32, ctypes.POINTER(FullData)]
+        lib.sesgb_get_exterior_molecule.argtypes = [P, U32, ctypes.POINTER(ExteriorData)]
         _lib = lib
     return _lib
 
@@ -226,12 +237,8 @@ class SesBuild:
     def max_neighbor_per_atom(self) -> int:
         return int(self._lib.sesgb_max_neighbor_per_atom(self._h))
 
-    def fetch(self, analysis: bool = True) -> dict:
-        """Host copies of every output buffer (and the analysis buffers)."""
-        c = self.counts()
-        d = self.data()
-        out = {"counts": c, "atoms": self._copy(d.atoms, d.atomNb, np.float32, 4)}
-        Q = c["singular_probes"]
+    def _fetch_data(self, d, Q: int) -> dict:
+        out = {"atoms": self._copy(d.atoms, d.atomNb, np.float32, 4)}
         out["probe_pos"] = self._copy(d.concavePatchesPosition, d.concavePatchNb, np.float32, 4)
         out["probe_ids"] = self._copy(d.concavePatchesId, d.concavePatchNb, np.int32, 4)
         out["probe_nbrs"] = self._copy(d.concavePatchesNeighbors, 32 * Q, np.float32, 4)
@@ -244,6 +251,14 @@ class SesBuild:
             out["tori_pos"] = self._copy(d.circlePosition, d.circlePatchNb, np.float32, 4)
             out["tori_axis"] = self._copy(d.circleAxis, d.circlePatchNb, np.float32, 4)
             out["tori_vs"] = self._copy(d.circleVs, d.circlePatchNb, np.float32, 4)
+        return out
+
+    def fetch(self, analysis: bool = True) -> dict:
+        """Host copies of every output buffer (and the analysis buffers)."""
+        c = self.counts()
+        d = self.data()
+        out = self._fetch_data(d, c["singular_probes"])
+        out["counts"] = c
         if analysis:
             out["perm"] = self.analysis(BUF_ATOM_INDICES, np.uint32)
             out["nbr_count"] = self.analysis(BUF_NEIGHBOR_COUNT, np.uint32)
@@ -271,3 +286,51 @@ class SesBuild:
 
     def __exit__(self, *exc):
         self.close()
+
+
+class SesBatch(SesBuild):
+    """Many molecules built together (sesgb_create_batch): one launch sequence for
+    the whole batch, molecule m's slice equal to its own SesBuild."""
+
+    def __init__(self, molecules, probe_radius: float = 1.4, mode: str = "full", max_neighbor_per_atom: int = 0,
+                 max_intersections_per_circle: int = 0, graph: bool = False, device: int = -1, profile: bool = False):
+        self._lib = load_library()
+        mols = [np.ascontiguousarray(np.asarray(m, np.float32).reshape(-1, 4)) for m in molecules]
+        self.starts = np.zeros(len(mols) + 1, np.uint32)
+        self.starts[1:] = np.cumsum([m.shape[0] for m in mols])
+        self.atoms = np.ascontiguousarray(np.concatenate(mols) if mols else np.zeros((0, 4), np.float32))
+        self.mode = mode
+        self.probe_radius = float(probe_radius)
+        flags = (FLAG_GRAPH if graph else 0) | (FLAG_PROFILE if profile else 0)
+        opt = Options(max_neighbor_per_atom, max_intersections_per_circle, device, flags)
+        h = ctypes.c_void_p()
+        st = self._lib.sesgb_create_batch(self.atoms.ctypes.data if self.atoms.size else None, self.starts.ctypes.data,
+                                          len(mols), ctypes.c_float(probe_radius),
+                                          MODE_FULL if mode == "full" else MODE_EXTERIOR, ctypes.byref(opt),
+                                          ctypes.byref(h))
+        self._h = h
+        self._check(st, "create_batch")
+
+    @property
+    def molecules(self) -> int:
+        return int(self._lib.sesgb_batch_molecules(self._h))
+
+    def record(self, m: int) -> dict:
+        r = (ctypes.c_uint32 * len(MOL_FIELDS))()
+        self._check(self._lib.sesgb_molecule_record(self._h, m, r), "molecule_record")
+        return {f: int(r[k]) for k, f in enumerate(MOL_FIELDS)}
+
+    def molecule(self, m: int) -> dict:
+        """Host copies of molecule m's output buffers (molecule-local ids)."""
+        if self.mode == "full":
+            d = FullData()
+            self._check(self._lib.sesgb_get_full_molecule(self._h, m, ctypes.byref(d)), "get_full_molecule")
+        else:
+            d = ExteriorData()
+            self._check(self._lib.sesgb_get_exterior_molecule(self._h, m, ctypes.byref(d)), "get_exterior_molecule")
+        rec = self.record(m)
+        out = self._fetch_data(d, rec["singular_probes"])
+        out["record"] = rec
+        perm = self.analysis(BUF_ATOM_INDICES, np.uint32)
+        out["perm"] = perm[self.starts[m]:self.starts[m + 1]]
+        return out

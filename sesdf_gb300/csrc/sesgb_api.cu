@@ -29,7 +29,14 @@ struct sesgb_ctx
     uint32_t      flags  = 0;
     const float * hostAtoms = nullptr;
     float         aabb[ 6 ] {};
-    int           gridBits = 0;
+    int           gridBits = 0; // radix-sort key bits
+
+    // batches (sesgb_create_batch): molecules, their first atoms, per-molecule records
+    uint32_t              nMol = 1;
+    std::vector<uint32_t> molStart;
+    std::vector<GridRef>  molGrid;
+    std::vector<uint32_t> molCells;
+    uint32_t *            hMol = nullptr; // pinned copy of Build::molCounts
 
     Build          b {};
     DeviceCounts * hCounts = nullptr;
@@ -153,8 +160,33 @@ namespace
         b.atoms           = dalloc<float4>( c, L, n, ok );
         b.perm            = dalloc<uint32_t>( c, L, n, ok );
         b.keys            = dalloc<uint32_t>( c, L, n, ok );
-        b.fine            = dalloc<FineGrid>( c, L, 1, ok );
-        b.capCells        = (uint32_t)std::max<size_t>( 1u << 16, 4 * n );
+        b.fine            = dalloc<FineGrid>( c, L, c->nMol, ok );
+        b.nMol            = c->nMol;
+        if ( c->nMol > 1 )
+        {
+            // per-molecule neighbour grids side by side: molecule m owns cells [cellBase[m], cellBase[m + 1])
+            std::vector<uint32_t> cellBase( c->nMol + 1, 0 );
+            for ( uint32_t m = 0; m < c->nMol; m++ )
+                cellBase[ m + 1 ] = cellBase[ m ] + c->molCells[ m ];
+            b.capCells        = cellBase[ c->nMol ];
+            uint32_t * start  = dalloc<uint32_t>( c, L, c->nMol + 1, ok );
+            uint32_t * base   = dalloc<uint32_t>( c, L, c->nMol + 1, ok );
+            GridRef *  grids  = dalloc<GridRef>( c, L, c->nMol, ok );
+            b.molCounts       = dalloc<uint32_t>( c, L, (size_t)c->nMol * kMolFields, ok );
+            if ( ok && !cuda_ok( c, cudaMallocHost( &c->hMol, sizeof( uint32_t ) * c->nMol * kMolFields ), "cudaMallocHost" ) )
+                ok = false;
+            if ( ok )
+            {
+                cudaMemcpy( start, c->molStart.data(), sizeof( uint32_t ) * ( c->nMol + 1 ), cudaMemcpyHostToDevice );
+                cudaMemcpy( base, cellBase.data(), sizeof( uint32_t ) * ( c->nMol + 1 ), cudaMemcpyHostToDevice );
+                cudaMemcpy( grids, c->molGrid.data(), sizeof( GridRef ) * c->nMol, cudaMemcpyHostToDevice );
+            }
+            b.molStart = start;
+            b.cellBase = base;
+            b.gridM    = grids;
+        }
+        else
+            b.capCells = (uint32_t)std::max<size_t>( 1u << 16, 4 * n );
         b.cellCount       = dalloc<uint32_t>( c, L, b.capCells + 1ull, ok );
         b.cellStart       = dalloc<uint32_t>( c, L, b.capCells + 1ull, ok );
         b.cellCursor      = dalloc<uint32_t>( c, L, b.capCells + 1ull, ok );
@@ -198,6 +230,7 @@ namespace
         b.probePos    = dalloc<float4>( c, L, PR, ok );
         b.probeCid    = dalloc<int4>( c, L, PR, ok );
         b.probeNbrs   = dalloc<float4>( c, L, PR * kMaxProbeNbr, ok );
+        b.singList    = c->nMol > 1 ? dalloc<uint32_t>( c, L, PR, ok ) : nullptr;
         b.ccount      = dalloc<uint32_t>( c, L, C1 + 1, ok );
         b.cstart      = dalloc<uint32_t>( c, L, C1 + 1, ok );
         b.ccursor     = dalloc<uint32_t>( c, L, C1 + 1, ok );
@@ -254,7 +287,7 @@ namespace
         radix_sort( b.keys, b.perm, n, c->gridBits, c->radixScratch, s );
         launch_fine_params( b, -1.f, n, s );
         launch_gather( b, s );
-        launch_cells( b, b.atoms, n, nullptr, sc, s );
+        launch_cells( b, 0, n, nullptr, sc, s );
         mark( 1 );
         launch_neighbors( b, s );
         exclusive_scan( b.nbrCount, b.pairOff, n, nullptr, &d->P, sc, s );
@@ -298,7 +331,7 @@ namespace
         // G: neighbours of singular probes
         mark( 8 );
         launch_fine_params( b, 2.f * c->rp + 0.01f, 0, s );
-        launch_cells( b, b.probePos, b.capProbes, &d->Q, sc, s );
+        launch_cells( b, 1, b.capProbes, &d->Q, sc, s );
         launch_probe_neighbors( b, s );
 
         // H: exterior tori
@@ -309,6 +342,8 @@ namespace
             exclusive_scan( b.torCnt, b.torOff, n, nullptr, &d->T, sc, s );
             launch_tori_emit( b, s );
         }
+        // batches: per-molecule records, molecule-local ids
+        launch_batch_finish( b, s );
         mark( 10 );
     }
 
@@ -379,6 +414,8 @@ namespace
                 cudaStreamBeginCapture( cap, cudaStreamCaptureModeThreadLocal );
                 enqueue( c, cap, false );
                 cudaMemcpyAsync( c->hCounts, c->b.counts, sizeof( DeviceCounts ), cudaMemcpyDeviceToHost, cap );
+                if ( c->nMol > 1 )
+                    cudaMemcpyAsync( c->hMol, c->b.molCounts, sizeof( uint32_t ) * c->nMol * kMolFields, cudaMemcpyDeviceToHost, cap );
                 const cudaError_t e = cudaStreamEndCapture( cap, &c->graph );
                 cudaStreamDestroy( cap );
                 if ( !cuda_ok( c, e, "capture" ) )
@@ -398,6 +435,8 @@ namespace
                     cudaEventCreate( &e );
             enqueue( c, s, profile );
             cudaMemcpyAsync( c->hCounts, c->b.counts, sizeof( DeviceCounts ), cudaMemcpyDeviceToHost, s );
+            if ( c->nMol > 1 )
+                cudaMemcpyAsync( c->hMol, c->b.molCounts, sizeof( uint32_t ) * c->nMol * kMolFields, cudaMemcpyDeviceToHost, s );
             c->profiled = profile;
         }
         return cuda_ok( c, cudaGetLastError(), "launch" ) ? SESGB_OK : SESGB_ERR_CUDA;
@@ -745,6 +784,167 @@ extern "C"
             cudaFree( c->g2t );
         if ( c->hCounts )
             cudaFreeHost( c->hCounts );
+        if ( c->hMol )
+            cudaFreeHost( c->hMol );
         delete c;
+    }
+
+    int sesgb_create_batch( const float * atoms, const uint32_t * molecule_start, uint32_t molecules, float probe_radius,
+                            int mode, const sesgb_options * options, sesgb_ctx ** out )
+    {
+        if ( !out || !molecule_start || molecules == 0 || ( mode != SESGB_MODE_FULL && mode != SESGB_MODE_EXTERIOR )
+             || !( probe_radius >= 0.f ) || molecule_start[ 0 ] != 0 )
+            return SESGB_ERR_INVALID;
+        for ( uint32_t m = 0; m < molecules; m++ )
+            if ( molecule_start[ m + 1 ] < molecule_start[ m ] )
+                return SESGB_ERR_INVALID;
+        const uint32_t n = molecule_start[ molecules ];
+        if ( n && !atoms )
+            return SESGB_ERR_INVALID;
+        if ( molecules == 1 )
+            return sesgb_create( atoms, n, nullptr, probe_radius, mode, options, out );
+        *out            = nullptr;
+        sesgb_ctx * c   = new sesgb_ctx();
+        c->mode         = mode;
+        c->n            = n;
+        c->rp           = probe_radius;
+        c->hostAtoms    = atoms;
+        sesgb_options o = options ? *options : sesgb_options {};
+        c->b.cap        = o.max_neighbor_per_atom ? o.max_neighbor_per_atom : 128u;
+        c->b.segCap     = o.max_intersections_per_circle ? o.max_intersections_per_circle : 32u;
+        c->flags        = o.flags;
+        c->b.mode       = mode;
+        c->b.rp         = probe_radius;
+        c->b.n          = n;
+        if ( c->b.cap > 4096 || c->b.segCap > (uint32_t)kSegBuf )
+        {
+            delete c;
+            return SESGB_ERR_INVALID;
+        }
+        if ( o.device >= 0 && !cuda_ok( c, cudaSetDevice( o.device ), "cudaSetDevice" ) )
+        {
+            delete c;
+            return SESGB_ERR_CUDA;
+        }
+        cudaGetDevice( &c->device );
+        // each molecule keeps the reference grid of its own construction (getAabb of its atoms)
+        c->nMol = molecules;
+        c->molStart.assign( molecule_start, molecule_start + molecules + 1 );
+        c->molGrid.resize( molecules );
+        c->molCells.resize( molecules );
+        int molShift = 1;
+        for ( uint32_t m = 0; m < molecules; m++ )
+        {
+            const uint32_t cnt = molecule_start[ m + 1 ] - molecule_start[ m ];
+            float          box[ 6 ];
+            host_aabb( atoms + 4ull * molecule_start[ m ], cnt, box );
+            const uint32_t gs     = next_pow2( floor_log2( cnt ) );
+            const float    maxVdw = 3.48f;
+            for ( int a = 0; a < 3; a++ )
+            {
+                const float origin = ( box[ a ] - maxVdw ) - probe_radius;
+                const float size   = std::fabs( ( ( box[ 3 + a ] + maxVdw ) + probe_radius ) - origin );
+                ( &c->molGrid[ m ].origin.x )[ a ] = origin;
+                ( &c->molGrid[ m ].cell.x )[ a ]   = size / (float)gs;
+            }
+            c->molGrid[ m ].size = (int)gs;
+            molShift             = std::max( molShift, 3 * (int)floor_log2( gs ) );
+            c->molCells[ m ]     = std::max<uint32_t>( 1024u, cnt );
+        }
+        const int molBits = (int)floor_log2( molecules - 1 ) + 1;
+        if ( molShift + molBits > 32 )
+        {
+            delete c;
+            return SESGB_ERR_INVALID;
+        }
+        c->b.molShift = (uint32_t)molShift;
+        c->gridBits   = molShift + molBits;
+        c->b.grid     = c->molGrid[ 0 ];
+        host_aabb( atoms, n, c->aabb );
+
+        Build & b    = c->b;
+        b.capSectors = grow( 40ull * n );
+        b.capFull    = grow( 4ull * n );
+        b.capC1      = grow( 24ull * n );
+        b.capProbes  = grow( 8ull * n );
+        b.capVisBand = grow( std::max<uint64_t>( 1u << 16, n / 2 ) );
+        b.capPairs   = grow( 40ull * n );
+        b.capSeg     = grow( 8ull * n );
+        b.capTori    = grow( 16ull * n );
+        if ( !allocate_fixed( c ) || !allocate_dynamic( c ) || !cuda_ok( c, configure_kernels( c->b ), "configure" ) )
+        {
+            const int st = SESGB_ERR_CUDA;
+            sesgb_destroy( c );
+            return st;
+        }
+        *out = c;
+        return SESGB_OK;
+    }
+
+    uint32_t sesgb_batch_molecules( const sesgb_ctx * c ) { return c ? c->nMol : 0u; }
+
+    int sesgb_molecule_record( const sesgb_ctx * c, uint32_t molecule, uint32_t * record )
+    {
+        if ( !c || !record || molecule >= c->nMol )
+            return SESGB_ERR_INVALID;
+        if ( !c->built )
+            return SESGB_ERR_NOT_BUILT;
+        if ( c->nMol == 1 )
+        {
+            const DeviceCounts & h = *c->hCounts;
+            const uint32_t       r[ kMolFields ] = { c->n, h.V, h.F, h.C1, h.I, h.Q, h.S, h.T, 0, 0, 0, 0, 0, 0, 0, 0 };
+            std::memcpy( record, r, sizeof( r ) );
+            return SESGB_OK;
+        }
+        std::memcpy( record, c->hMol + (size_t)molecule * kMolFields, sizeof( uint32_t ) * kMolFields );
+        return SESGB_OK;
+    }
+
+    int sesgb_get_full_molecule( sesgb_ctx * c, uint32_t molecule, sesgb_full_data * o )
+    {
+        uint32_t r[ kMolFields ];
+        int      st = sesgb_molecule_record( c, molecule, r );
+        if ( st != SESGB_OK )
+            return st;
+        if ( ( st = sesgb_get_full( c, o ) ) != SESGB_OK )
+            return st;
+        const Build & b            = c->b;
+        o->atomNb                  = r[ kMolAtoms ];
+        o->atoms                   = b.atoms + r[ kMolAtomBase ];
+        o->convexPatchNb           = r[ kMolAtoms ];
+        o->convexPatches           = b.convex + r[ kMolAtomBase ];
+        o->sectorNb                = r[ kMolSectors ];
+        o->sectors                 = b.sectors + r[ kMolSectorBase ];
+        o->segmentPatchNb          = r[ kMolSegments ];
+        o->segmentPatches          = b.segments + r[ kMolSegmentBase ];
+        o->circlePatchNb           = r[ kMolFull ];
+        o->circlePatches           = b.fullCircles + r[ kMolFullBase ];
+        o->concavePatchNb          = r[ kMolProbes ];
+        o->concavePatchesPosition  = b.probePos + r[ kMolProbeBase ];
+        o->concavePatchesId        = b.probeIds + r[ kMolProbeBase ];
+        o->concavePatchesNeighbors = b.probeNbrs + (size_t)kMaxProbeNbr * r[ kMolSingularBase ];
+        return SESGB_OK;
+    }
+
+    int sesgb_get_exterior_molecule( sesgb_ctx * c, uint32_t molecule, sesgb_exterior_data * o )
+    {
+        uint32_t r[ kMolFields ];
+        int      st = sesgb_molecule_record( c, molecule, r );
+        if ( st != SESGB_OK )
+            return st;
+        if ( ( st = sesgb_get_exterior( c, o ) ) != SESGB_OK )
+            return st;
+        const Build & b            = c->b;
+        o->atomNb                  = r[ kMolAtoms ];
+        o->atoms                   = b.atoms + r[ kMolAtomBase ];
+        o->circlePatchNb           = r[ kMolTori ];
+        o->circlePosition          = b.torPos + r[ kMolToriBase ];
+        o->circleAxis              = b.torAxis + r[ kMolToriBase ];
+        o->circleVs                = b.torVs + r[ kMolToriBase ];
+        o->concavePatchNb          = r[ kMolProbes ];
+        o->concavePatchesPosition  = b.probePos + r[ kMolProbeBase ];
+        o->concavePatchesId        = b.probeIds + r[ kMolProbeBase ];
+        o->concavePatchesNeighbors = b.probeNbrs + (size_t)kMaxProbeNbr * r[ kMolSingularBase ];
+        return SESGB_OK;
     }
 }

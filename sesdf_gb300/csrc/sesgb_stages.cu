@@ -156,44 +156,76 @@ namespace sesgb
                 }
         }
 
+        // ---- molecules of a batch ---------------------------------------------
+        __device__ __forceinline__ uint32_t mol_of( const Build & b, uint32_t sortedAtom )
+        {
+            return b.nMol > 1 ? b.keys[ sortedAtom ] >> b.molShift : 0u;
+        }
+        __device__ __forceinline__ GridRef grid_of( const Build & b, uint32_t m ) { return b.nMol > 1 ? b.gridM[ m ] : b.grid; }
+        __device__ __forceinline__ uint32_t cell_base( const Build & b, uint32_t m ) { return b.nMol > 1 ? b.cellBase[ m ] : 0u; }
+        // last molecule whose first atom is <= a (empty molecules are skipped)
+        __device__ __forceinline__ uint32_t mol_of_index( const Build & b, uint32_t a )
+        {
+            uint32_t lo = 0, hi = b.nMol;
+            while ( hi - lo > 1 )
+            {
+                const uint32_t mid = ( lo + hi ) >> 1;
+                if ( b.molStart[ mid ] <= a )
+                    lo = mid;
+                else
+                    hi = mid;
+            }
+            return lo;
+        }
+
         // ------------------------------------------------------------------
         __global__ void k_hash( Build b )
         {
             const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
             if ( i >= b.n )
                 return;
-            const float4 a = b.atomsIn[ i ];
-            const int3   p = ref_grid_position( b.grid, a.x, a.y, a.z );
-            if ( p.x < 0 || p.y < 0 || p.z < 0 || p.x >= b.grid.size || p.y >= b.grid.size || p.z >= b.grid.size )
+            const float4   a = b.atomsIn[ i ];
+            const uint32_t m = b.nMol > 1 ? mol_of_index( b, i ) : 0u;
+            const GridRef  g = grid_of( b, m );
+            const int3     p = ref_grid_position( g, a.x, a.y, a.z );
+            if ( p.x < 0 || p.y < 0 || p.z < 0 || p.x >= g.size || p.y >= g.size || p.z >= g.size )
                 atomicAdd( &b.counts->outside, 1u );
-            b.keys[ i ] = ref_grid_hash( b.grid, p );
+            b.keys[ i ] = ( m << b.molShift ) | ref_grid_hash( g, p );
             b.perm[ i ] = i;
             atomicMax( reinterpret_cast<int *>( &b.counts->rmax ), __float_as_int( fmaxf( a.w, 0.f ) ) );
         }
 
-        // one thread: neighbour-grid geometry from the reference grid box
+        // thread per molecule: neighbour-grid geometry from the molecule's reference grid box
         __global__ void k_fine_params( Build b, float cutoff )
         {
             if ( cutoff < 0.f )
                 cutoff = 2.f * ( b.counts->rmax + b.rp ) + 0.01f;
-            const float ex = b.grid.cell.x * b.grid.size, ey = b.grid.cell.y * b.grid.size, ez = b.grid.cell.z * b.grid.size;
-            float       h  = cutoff;
-            int3        d;
-            for ( int it = 0; it < 200; it++ )
+            for ( uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < b.nMol; m += gridDim.x * blockDim.x )
             {
-                d = make_int3( max( 1, (int)ceilf( ex / h ) ), max( 1, (int)ceilf( ey / h ) ), max( 1, (int)ceilf( ez / h ) ) );
-                if ( (uint64_t)d.x * d.y * d.z <= b.capCells )
-                    break;
-                h *= 1.1f;
+                const GridRef  gr  = grid_of( b, m );
+                const uint32_t cap = b.nMol > 1 ? b.cellBase[ m + 1 ] - b.cellBase[ m ] : b.capCells;
+                const float    ex = gr.cell.x * gr.size, ey = gr.cell.y * gr.size, ez = gr.cell.z * gr.size;
+                float          h  = cutoff;
+                int3           d;
+                for ( int it = 0; it < 200; it++ )
+                {
+                    d = make_int3( max( 1, (int)ceilf( ex / h ) ), max( 1, (int)ceilf( ey / h ) ), max( 1, (int)ceilf( ez / h ) ) );
+                    if ( (uint64_t)d.x * d.y * d.z <= cap )
+                        break;
+                    h *= 1.1f;
+                }
+                FineGrid g;
+                g.origin    = gr.origin;
+                g.h         = h;
+                g.dims      = d;
+                g.cells     = (uint32_t)( (uint64_t)d.x * d.y * d.z );
+                b.fine[ m ] = g;
+                if ( m == 0 )
+                {
+                    b.counts->fineCells = g.cells;
+                    b.counts->fineCell  = h;
+                }
             }
-            FineGrid g;
-            g.origin = b.grid.origin;
-            g.h      = h;
-            g.dims   = d;
-            g.cells  = (uint32_t)( (uint64_t)d.x * d.y * d.z );
-            *b.fine  = g;
-            b.counts->fineCells = g.cells;
-            b.counts->fineCell  = h;
         }
 
         __global__ void k_gather( Build b )
@@ -204,25 +236,46 @@ namespace sesgb
             b.atoms[ s ] = b.atomsIn[ b.perm[ s ] ];
         }
 
-        __global__ void k_cell_count( Build b, const float4 * pos, uint32_t nHost, const uint32_t * nDevice )
+        // item q of a cell sort: kind 0 the sorted atom q, kind 1 the singular probe q
+        __device__ __forceinline__ float4 cell_item( const Build & b, int kind, uint32_t q, uint32_t & key )
+        {
+            float4   p;
+            uint32_t m = 0;
+            if ( kind == 0 )
+            {
+                p = b.atoms[ q ];
+                m = mol_of( b, q );
+            }
+            else
+            {
+                const uint32_t pi = b.nMol > 1 ? b.singList[ q ] : q;
+                p                 = b.probePos[ pi ];
+                if ( b.nMol > 1 )
+                    m = mol_of( b, (uint32_t)b.probeIds[ pi ].x );
+            }
+            const FineGrid g = b.fine[ m ];
+            key              = cell_base( b, m ) + fine_key( g, fine_cell( g, p.x, p.y, p.z ) );
+            return p;
+        }
+
+        __global__ void k_cell_count( Build b, int kind, uint32_t nHost, const uint32_t * nDevice )
         {
             const uint32_t n = nDevice ? min( *nDevice, nHost ) : nHost;
-            const FineGrid g = *b.fine;
             for ( uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x )
             {
-                const float4 p = pos[ q ];
-                atomicAdd( &b.cellCount[ fine_key( g, fine_cell( g, p.x, p.y, p.z ) ) ], 1u );
+                uint32_t key;
+                cell_item( b, kind, q, key );
+                atomicAdd( &b.cellCount[ key ], 1u );
             }
         }
 
-        __global__ void k_cell_scatter( Build b, const float4 * pos, uint32_t nHost, const uint32_t * nDevice )
+        __global__ void k_cell_scatter( Build b, int kind, uint32_t nHost, const uint32_t * nDevice )
         {
             const uint32_t n = nDevice ? min( *nDevice, nHost ) : nHost;
-            const FineGrid g = *b.fine;
             for ( uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x )
             {
-                const float4   p   = pos[ q ];
-                const uint32_t key = fine_key( g, fine_cell( g, p.x, p.y, p.z ) );
+                uint32_t       key;
+                const float4   p   = cell_item( b, kind, q, key );
                 const uint32_t idx = b.cellStart[ key ] + atomicAdd( &b.cellCursor[ key ], 1u );
                 b.cellItems[ idx ] = q;
                 b.cellPos[ idx ]   = p;
@@ -237,10 +290,11 @@ namespace sesgb
             const uint32_t      i    = blockIdx.x * kWarpsPerBlock + warp;
             if ( i >= b.n )
                 return;
-            const FineGrid g  = *b.fine;
+            const uint32_t m  = mol_of( b, i );
+            const FineGrid g  = b.fine[ m ];
             const float4   ai = b.atoms[ i ];
             Rows           rows;
-            stencil_rows( g, b.cellStart, fine_cell( g, ai.x, ai.y, ai.z ), rows );
+            stencil_rows( g, b.cellStart + cell_base( b, m ), fine_cell( g, ai.x, ai.y, ai.z ), rows );
             const float Ri    = ai.w + b.rp;
             uint32_t    count = 0, fp64 = 0;
             for ( uint32_t base = 0; base < rows.total; base += 32 )
@@ -1453,6 +1507,16 @@ namespace sesgb
             const uint32_t cnt   = b.chunkLen[ i ];
             const uint32_t chunk = b.chunkStart[ i ];
             uint32_t       so = b.singOff[ i ], ro = Q + b.regOff[ i ];
+            uint32_t       sq = b.singOff[ i ]; // singular index (molecule-major)
+            if ( b.nMol > 1 )
+            {
+                // singular probes first within each molecule of the batch
+                const uint32_t m  = mol_of( b, i );
+                const uint32_t a0 = b.molStart[ m ], a1 = b.molStart[ m + 1 ];
+                const uint32_t s0 = b.singOff[ a0 ], r0 = b.regOff[ a0 ];
+                so                = r0 + b.singOff[ i ];
+                ro                = s0 + ( b.singOff[ a1 ] - s0 ) + b.regOff[ i ];
+            }
             for ( uint32_t m0 = 0; m0 < cnt; m0 += 32 )
             {
                 const uint32_t m     = m0 + lane;
@@ -1465,8 +1529,11 @@ namespace sesgb
                 const uint32_t ms   = __ballot_sync( 0xffffffffu, sing );
                 const uint32_t mr   = __ballot_sync( 0xffffffffu, live && !sing );
                 const uint32_t dst  = sing ? so + __popc( ms & lanemask_lt() ) : ro + __popc( mr & lanemask_lt() );
+                if ( sing && b.nMol > 1 )
+                    b.singList[ sq + __popc( ms & lanemask_lt() ) ] = dst;
                 so += __popc( ms );
                 ro += __popc( mr );
+                sq += __popc( ms );
                 if ( !live )
                     continue;
                 b.probePos[ dst ] = b.stagePos[ chunk + m ];
@@ -1676,15 +1743,18 @@ namespace sesgb
             __shared__ unsigned long long buf[ kWarpsPerBlock ][ kSnbrBuf ];
             const uint32_t                warp = threadIdx.x >> 5, lane = lane_id();
             const uint32_t                Q    = min( b.counts->Q, b.capProbes );
-            const FineGrid                g    = *b.fine;
             const float                   t2   = 2.f * b.rp;
             const double                  t2d  = 2.0 * (double)b.rp;
             uint32_t                      fp64 = 0, trunc = 0;
             for ( uint32_t q = blockIdx.x * kWarpsPerBlock + warp; q < Q; q += gridDim.x * kWarpsPerBlock )
             {
-                const float4 pq = b.probePos[ q ];
-                Rows         rows;
-                stencil_rows( g, b.cellStart, fine_cell( g, pq.x, pq.y, pq.z ), rows );
+                const uint32_t pi = b.nMol > 1 ? b.singList[ q ] : q; // probe index of singular probe q
+                const float4   pq = b.probePos[ pi ];
+                const uint32_t m  = b.nMol > 1 ? mol_of( b, (uint32_t)b.probeIds[ pi ].x ) : 0u;
+                const FineGrid g  = b.fine[ m ];
+                const GridRef  gr = grid_of( b, m );
+                Rows           rows;
+                stencil_rows( g, b.cellStart + cell_base( b, m ), fine_cell( g, pq.x, pq.y, pq.z ), rows );
                 uint32_t count = 0;
                 for ( uint32_t base = 0; base < rows.total; base += 32 )
                 {
@@ -1711,8 +1781,7 @@ namespace sesgb
                                 fp64++;
                             }
                             if ( pass )
-                                key = ( (unsigned long long)ref_grid_hash( b.grid, ref_grid_position( b.grid, pp.x, pp.y, pp.z ) ) << 32 )
-                                      | p;
+                                key = ( (unsigned long long)ref_grid_hash( gr, ref_grid_position( gr, pp.x, pp.y, pp.z ) ) << 32 ) | p;
                         }
                     }
                     const uint32_t mask = __ballot_sync( 0xffffffffu, pass );
@@ -1728,13 +1797,13 @@ namespace sesgb
                 if ( lane < kept )
                 {
                     const uint32_t p  = (uint32_t)( buf[ warp ][ lane ] & 0xffffffffull );
-                    const float4   pp = b.probePos[ p ];
+                    const float4   pp = b.probePos[ b.nMol > 1 ? b.singList[ p ] : p ];
                     const float    wv = b.mode == 0 ? __fmul_rn( __fmul_rn( pq.x, pq.y ), pq.z ) : 0.f;
                     b.probeNbrs[ (size_t)q * kMaxProbeNbr + lane ] = make_float4( pp.x, pp.y, pp.z, wv );
                 }
                 if ( lane == 0 )
                 {
-                    b.probeIds[ q ].w = (int)kept;
+                    b.probeIds[ pi ].w = (int)kept;
                     if ( count > kMaxProbeNbr )
                         trunc++;
                 }
@@ -1757,7 +1826,96 @@ namespace sesgb
         {
             const uint32_t Q = min( b.counts->Q, b.capProbes );
             for ( uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < Q; q += gridDim.x * blockDim.x )
-                b.probePos[ q ].w = (float)(int)( q * kMaxProbeNbr );
+            {
+                uint32_t pi = q, local = q;
+                if ( b.nMol > 1 )
+                {
+                    // index of the neighbour block within the probe's molecule
+                    pi    = b.singList[ q ];
+                    local = q - b.singOff[ b.molStart[ mol_of( b, (uint32_t)b.probeIds[ pi ].x ) ] ];
+                }
+                b.probePos[ pi ].w = (float)(int)( local * kMaxProbeNbr );
+            }
+        }
+
+        // ---- batches: per-molecule counts and molecule-local ids ----------------
+        __global__ void k_mol_counts( Build b )
+        {
+            for ( uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < b.nMol; m += gridDim.x * blockDim.x )
+            {
+                const uint32_t a0 = b.molStart[ m ], a1 = b.molStart[ m + 1 ];
+                uint32_t *     o  = b.molCounts + (size_t)m * kMolFields;
+                const uint32_t q0 = b.singOff[ a0 ], q1 = b.singOff[ a1 ];
+                o[ kMolAtoms ]        = a1 - a0;
+                o[ kMolSingular ]     = q1 - q0;
+                o[ kMolProbes ]       = ( q1 - q0 ) + ( b.regOff[ a1 ] - b.regOff[ a0 ] );
+                o[ kMolAtomBase ]     = a0;
+                o[ kMolProbeBase ]    = q0 + b.regOff[ a0 ];
+                o[ kMolSingularBase ] = q0;
+                o[ kMolC1 ]           = b.partOff[ a1 ] - b.partOff[ a0 ];
+                o[ kMolC1Base ]       = b.partOff[ a0 ];
+                if ( b.mode == 0 )
+                {
+                    o[ kMolSectors ]     = b.visOff[ a1 ] - b.visOff[ a0 ];
+                    o[ kMolSectorBase ]  = b.visOff[ a0 ];
+                    o[ kMolFull ]        = b.fullOff[ a1 ] - b.fullOff[ a0 ];
+                    o[ kMolFullBase ]    = b.fullOff[ a0 ];
+                    o[ kMolSegments ]    = b.segOff[ b.partOff[ a1 ] ] - b.segOff[ b.partOff[ a0 ] ];
+                    o[ kMolSegmentBase ] = b.segOff[ b.partOff[ a0 ] ];
+                    o[ kMolTori ] = o[ kMolToriBase ] = 0;
+                }
+                else
+                {
+                    o[ kMolTori ]     = b.torOff[ a1 ] - b.torOff[ a0 ];
+                    o[ kMolToriBase ] = b.torOff[ a0 ];
+                    o[ kMolSectors ] = o[ kMolSectorBase ] = o[ kMolFull ] = o[ kMolFullBase ] = 0;
+                    o[ kMolSegments ] = o[ kMolSegmentBase ] = 0;
+                }
+            }
+        }
+
+        // Ids in the output buffers become molecule-local, so that each molecule's
+        // slice of a batch reads exactly like the buffers of its own build.
+        __global__ void k_mol_rebase( Build b )
+        {
+            const uint32_t stride = gridDim.x * blockDim.x;
+            const uint32_t t0     = blockIdx.x * blockDim.x + threadIdx.x;
+            for ( uint32_t s = t0; s < b.n; s += stride )
+            {
+                const uint32_t m  = mol_of( b, s );
+                const uint32_t a0 = b.molStart[ m ];
+                b.perm[ s ] -= a0;
+                if ( b.mode == 0 )
+                {
+                    const uint32_t v0 = b.molCounts[ (size_t)m * kMolFields + kMolSectorBase ];
+                    uint2          cv = b.convex[ s ];
+                    b.convex[ s ]     = make_uint2( cv.x - v0, cv.y - v0 );
+                }
+            }
+            const uint32_t I = min( b.counts->I, b.capProbes );
+            for ( uint32_t p = t0; p < I; p += stride )
+            {
+                int4           id = b.probeIds[ p ];
+                const uint32_t a0 = b.molStart[ mol_of( b, (uint32_t)id.x ) ];
+                b.probeIds[ p ]   = make_int4( id.x - (int)a0, id.y - (int)a0, id.z - (int)a0, id.w );
+            }
+            if ( b.mode != 0 )
+                return;
+            const uint32_t F = min( b.counts->F, b.capFull );
+            for ( uint32_t f = t0; f < F; f += stride )
+            {
+                const uint2    c  = b.fullCircles[ f ];
+                const uint32_t a0 = b.molStart[ mol_of( b, c.x ) ];
+                b.fullCircles[ f ] = make_uint2( c.x - a0, c.y - a0 );
+            }
+            const uint32_t S = min( b.counts->S, b.capSeg );
+            for ( uint32_t k = t0; k < S; k += stride )
+            {
+                const uint4    g  = b.segments[ k ];
+                const uint32_t m  = mol_of( b, g.x );
+                const uint32_t a0 = b.molStart[ m ], p0 = b.molCounts[ (size_t)m * kMolFields + kMolProbeBase ];
+                b.segments[ k ]   = make_uint4( g.x - a0, g.y - a0, g.z - p0, g.w - p0 );
+            }
         }
 
         // ---- exterior tori ---------------------------------------------------
@@ -1889,7 +2047,7 @@ namespace sesgb
     }
     void launch_fine_params( const Build & b, float cutoff, uint32_t, cudaStream_t s )
     {
-        k_fine_params<<<1, 1, 0, s>>>( b, cutoff );
+        k_fine_params<<<blocks_for( b.nMol, 128 ), 128, 0, s>>>( b, cutoff );
         counted();
     }
     void launch_gather( const Build & b, cudaStream_t s )
@@ -1899,7 +2057,7 @@ namespace sesgb
         k_gather<<<blocks_for( b.n, 256 ), 256, 0, s>>>( b );
         counted();
     }
-    void launch_cells( const Build & b, const float4 * pos, uint32_t nHost, const uint32_t * nDevice, void * scanScratch,
+    void launch_cells( const Build & b, int kind, uint32_t nHost, const uint32_t * nDevice, void * scanScratch,
                        cudaStream_t s )
     {
         cudaMemsetAsync( b.cellCount, 0, sizeof( uint32_t ) * ( (size_t)b.capCells + 1 ), s );
@@ -1907,10 +2065,23 @@ namespace sesgb
         if ( nHost == 0 )
             return;
         const uint32_t blocks = nDevice ? min( persistent_blocks( 256 ), blocks_for( nHost, 256 ) ) : blocks_for( nHost, 256 );
-        k_cell_count<<<blocks, 256, 0, s>>>( b, pos, nHost, nDevice );
-        const uint32_t * cells = reinterpret_cast<const uint32_t *>( reinterpret_cast<const char *>( b.fine ) + offsetof( FineGrid, cells ) );
-        exclusive_scan( b.cellCount, b.cellStart, b.capCells, cells, nullptr, scanScratch, s );
-        k_cell_scatter<<<blocks, 256, 0, s>>>( b, pos, nHost, nDevice );
+        k_cell_count<<<blocks, 256, 0, s>>>( b, kind, nHost, nDevice );
+        if ( b.nMol > 1 )
+            exclusive_scan( b.cellCount, b.cellStart, b.capCells, nullptr, nullptr, scanScratch, s ); // all molecules' cells
+        else
+        {
+            const uint32_t * cells = reinterpret_cast<const uint32_t *>( reinterpret_cast<const char *>( b.fine ) + offsetof( FineGrid, cells ) );
+            exclusive_scan( b.cellCount, b.cellStart, b.capCells, cells, nullptr, scanScratch, s );
+        }
+        k_cell_scatter<<<blocks, 256, 0, s>>>( b, kind, nHost, nDevice );
+        counted( 2 );
+    }
+    void launch_batch_finish( const Build & b, cudaStream_t s )
+    {
+        if ( b.nMol <= 1 || !b.n )
+            return;
+        k_mol_counts<<<blocks_for( b.nMol, 128 ), 128, 0, s>>>( b );
+        k_mol_rebase<<<persistent_blocks( 256 ), 256, 0, s>>>( b );
         counted( 2 );
     }
     void launch_neighbors( const Build & b, cudaStream_t s )

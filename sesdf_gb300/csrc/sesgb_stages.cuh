@@ -9,6 +9,13 @@ namespace sesgb
     constexpr int kSegBuf        = 64;              // probes per circle the segment stage can hold
     constexpr int kSnbrBuf       = 256;             // per-warp candidate buffer of the singular-probe search
     constexpr uint32_t kMaxProbeNbr = 32;           // MaxIntersectionNeighbors (sesdf.cu:18)
+    // per-molecule record of a batch build (molCounts)
+    enum MolField : uint32_t
+    {
+        kMolAtoms = 0, kMolSectors, kMolFull, kMolC1, kMolProbes, kMolSingular, kMolSegments, kMolTori,
+        kMolAtomBase, kMolSectorBase, kMolFullBase, kMolC1Base, kMolProbeBase, kMolSingularBase, kMolSegmentBase,
+        kMolToriBase, kMolFields
+    };
 
     // Everything a kernel of the build needs, passed by value.
     struct Build
@@ -21,6 +28,17 @@ namespace sesgb
         float    rp;
         GridRef  grid;
 
+        // batches: nMol molecules built together (nMol = 1 for a single molecule). Sort
+        // keys carry the molecule above molShift, so every molecule keeps its own
+        // reference-grid order and atoms stay molecule-major in sorted order.
+        uint32_t         nMol;
+        uint32_t         molShift;
+        const uint32_t * molStart;  // nMol + 1: first atom of each molecule (input and sorted order)
+        const GridRef *  gridM;     // nMol: reference grid of each molecule
+        const uint32_t * cellBase;  // nMol + 1: first cell of each molecule's neighbour grid
+        uint32_t *       singList;  // capProbes: probe index of each singular probe (batches)
+        uint32_t *       molCounts; // nMol * kMolFields: per-molecule counts and bases (batches)
+
         // capacities of the count-dependent buffers
         uint32_t capSectors, capFull, capC1, capProbes, capSeg, capTori, capCells;
 
@@ -30,7 +48,7 @@ namespace sesgb
         uint32_t *     perm;    // sorted id -> input id
         uint32_t *     keys;    // sort keys scratch (n)
 
-        // neighbour grid
+        // neighbour grid (one per molecule)
         FineGrid * fine;
         uint32_t * cellCount; // capCells + 1
         uint32_t * cellStart; // capCells + 1
@@ -97,8 +115,10 @@ namespace sesgb
     void launch_hash( const Build & b, cudaStream_t s );
     void launch_fine_params( const Build & b, float cutoff, uint32_t items, cudaStream_t s );
     void launch_gather( const Build & b, cudaStream_t s );
-    void launch_cells( const Build & b, const float4 * pos, uint32_t nHost, const uint32_t * nDevice, void * scanScratch,
+    // kind 0: the sorted atoms (n); kind 1: the singular probes (count read from *nDevice)
+    void launch_cells( const Build & b, int kind, uint32_t nHost, const uint32_t * nDevice, void * scanScratch,
                        cudaStream_t s );
+    void launch_batch_finish( const Build & b, cudaStream_t s );
     void launch_neighbors( const Build & b, cudaStream_t s );
     void launch_visibility( const Build & b, cudaStream_t s );
     void launch_visibility_resolve( const Build & b, cudaStream_t s );
