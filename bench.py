@@ -197,6 +197,79 @@ def time_e2e(atoms, mode, steps, warmup, flush):
     return ms
 
 
+def time_plain_loop(mols, mode, repeats, flush):
+    """One build per molecule through its own context (created beforehand), in sequence:
+    per-step device ms for the whole loop."""
+    import torch
+    from sesdf_gb300 import SesBuild
+    stream = torch.cuda.current_stream()
+    ctxs = [SesBuild(m, RP, mode) for m in mols]
+    dev = [torch.from_numpy(m).cuda() for m in mols]
+    for g, d in zip(ctxs, dev):
+        g.build_async(d.data_ptr(), stream.cuda_stream)
+        g.finish()
+    out = []
+    for _ in range(repeats):
+        flush.zero_()
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        for g, d in zip(ctxs, dev):
+            g.build_async(d.data_ptr(), stream.cuda_stream)
+            g.finish()
+        t1.record(stream)
+        torch.cuda.synchronize()
+        out.append(t0.elapsed_time(t1))
+    for g in ctxs:
+        g.close()
+    return out
+
+
+def time_batched(mols, mode, repeats, flush, cap, graph):
+    import torch
+    from sesdf_gb300 import SesBatch
+    stream = torch.cuda.current_stream()
+    b = SesBatch(mols, RP, mode, max_neighbor_per_atom=cap, graph=graph)
+    d = torch.from_numpy(b.atoms).cuda()
+    for _ in range(2):
+        b.build_async(d.data_ptr(), stream.cuda_stream)
+        b.finish()
+    out = []
+    for _ in range(repeats):
+        flush.zero_()
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        b.build_async(d.data_ptr(), stream.cuda_stream)
+        t1.record(stream)
+        b.finish()
+        torch.cuda.synchronize()
+        out.append(t0.elapsed_time(t1))
+    c = b.counts()
+    b.close()
+    return out, c
+
+
+def batch_extras(args, flush):
+    """Batched builds (256 molecules of log-uniform size; 64 jittered frames) against the plain loop."""
+    from sesdf_gb300 import synth
+    from sesdf_gb300.autotune import tune_batch
+    res = {}
+    sizes = synth.batch_sizes()
+    sets = {"batch256_mixed": [synth.globule(int(n), 1300 + m) for m, n in enumerate(sizes)],
+            "batch64_frames": synth.frames()}
+    for name, mols in sets.items():
+        tuned = tune_batch(mols, RP, "full")
+        bm, c = time_batched(mols, "full", 5, flush, tuned["max_neighbor_per_atom"], tuned["graph"])
+        pm = time_plain_loop(mols, "full", 3, flush)
+        atoms = int(sum(m.shape[0] for m in mols))
+        res[name] = {"molecules": len(mols), "atoms": atoms, "batched_ms": round(float(np.median(bm)), 3),
+                     "plain_loop_ms": round(float(np.median(pm)), 3),
+                     "speedup": round(float(np.median(pm)) / float(np.median(bm)), 2),
+                     "batched_atoms_per_s": round(atoms / (float(np.median(bm)) * 1e-3), 1),
+                     "tuned": {k: tuned[k] for k in ("max_neighbor_per_atom", "graph", "max_neighbors")},
+                     "probes": c["probes"]}
+    return res
+
+
 def profiled_traffic(kernel: str):
     """DRAM bytes per launch of `kernel` from its committed ncu summary (profiles/), or None."""
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles", f"{kernel}_assembly100k.txt")
@@ -296,6 +369,7 @@ def run_ours(args, rank, world, local):
                                    "probes": c["probes"], "fp64_decisions": c["fp64_decisions"]}
             gs.close()
         del shell
+        extra.update(batch_extras(args, flush))
 
     roof = roofline(stages, counts, nbr, n)
     line = {
