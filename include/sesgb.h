@@ -228,6 +228,27 @@ int sesgb_molecule_record( const sesgb_ctx * ctx, uint32_t molecule, uint32_t * 
 int sesgb_get_full_molecule( sesgb_ctx * ctx, uint32_t molecule, sesgb_full_data * out );
 int sesgb_get_exterior_molecule( sesgb_ctx * ctx, uint32_t molecule, sesgb_exterior_data * out );
 
+/* Signed distance to the SES at query points (no counterpart in the reference).
+ * E = probe-centre positions outside every SAS sphere (radius r_i + rp); with
+ * T = rp + SESGB_SDF_BAND: outside the SAS, sdf(x) = min_i(|x - c_i| - r_i)
+ * clamped to SESGB_SDF_BAND; inside, sdf(x) = rp - min(T, dist(x, dE)), dE
+ * being the SAS surface (accessible sphere patches, visible-circle arcs, probe
+ * positions) of the last full-surface build. Positive outside the molecule.
+ * device_queries: float3[m]; device_sdf: float[m]; device_kind (may be NULL):
+ * int[m], the primitive that decided each value (0 deeper than the band, 1 atom
+ * outside the SAS, 2 beyond the band outside, 3 SAS sphere, 4 circle arc, 5
+ * probe). Needs a built full-surface context of one molecule. */
+#define SESGB_SDF_BAND 3.0f
+int sesgb_sdf( sesgb_ctx * ctx, const float * device_queries, uint32_t m, float * device_sdf, int * device_kind,
+               void * stream );
+/* Adjoint of sesgb_sdf: device_grad_atoms (float4[n], input atom order) receives
+ * sum_q device_grad_sdf[q] * d sdf(q) / d (x, y, z, r) of every atom. The
+ * primitives are searched again (nothing is kept from the forward call); a probe
+ * position is differentiated by the implicit-function rule on its three
+ * sphere constraints, a circle point by the Lagrange rule on its two. */
+int sesgb_sdf_backward( sesgb_ctx * ctx, const float * device_queries, uint32_t m, const float * device_grad_sdf,
+                        float * device_grad_atoms, void * stream );
+
 /* Number of kernels this library has launched in this process (host-side count). */
 uint64_t sesgb_launch_count( void );
 

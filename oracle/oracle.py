@@ -112,3 +112,38 @@ def run(atoms: np.ndarray, probe_radius: float = 1.4, mode: str = "full", box=No
     out["counters"] = dict(zip(COUNTERS, [int(c) for c in out["counters"]]))
     out["Q"] = int(np.sum(np.abs(out["cids"][:, 3]) == 2)) if out["cids"].size else 0
     return out
+
+
+def sdf(built: dict, queries: np.ndarray, band: float = 3.0, gq: np.ndarray | None = None, threads: int = 0):
+    """FP64 signed distance to the SES at float32 query points [m, 3] from the outputs of run()
+    (full mode). Returns (sdf float64 [m], kind int32 [m], grad float64 [n, 4] in sorted atom order or
+    None): grad = sum_q gq[q] d sdf_q / d (x, y, z, r) when gq is given. Test oracle only."""
+    lib = _load()
+    if not getattr(lib, "_sdf_ready", False):
+        P = ctypes.c_void_p
+        lib.ora_sdf.argtypes = [P, ctypes.c_uint32, P, P, P, P, P, ctypes.c_uint32, ctypes.c_float, ctypes.c_float, P,
+                                ctypes.c_uint32, P, P, P, P, ctypes.c_int]
+        lib.ora_sdf.restype = ctypes.c_int
+        lib._sdf_ready = True
+    atoms = np.ascontiguousarray(built["atoms"], np.float32)
+    n = atoms.shape[0]
+    q = np.ascontiguousarray(queries, np.float32).reshape(-1, 3)
+    m = q.shape[0]
+    noff = np.ascontiguousarray(built["noff"], np.uint32)
+    nbr = np.ascontiguousarray(built["nbr"], np.uint32)
+    status = np.ascontiguousarray(built["status"], np.uint8)
+    ids = np.ascontiguousarray(built["ids"], np.int32).reshape(-1, 4)
+    posd = np.ascontiguousarray(built["posd"], np.float64).reshape(-1, 4)
+    out = np.zeros(m, np.float64)
+    kind = np.zeros(m, np.int32)
+    g = np.zeros((n, 4), np.float64) if gq is not None else None
+    gqa = np.ascontiguousarray(gq, np.float64) if gq is not None else None
+
+    def ptr(a):
+        return a.ctypes.data if a is not None and a.size else None
+    st = lib.ora_sdf(ptr(atoms), n, ptr(noff), ptr(nbr), ptr(status), ptr(ids), ptr(posd), ids.shape[0],
+                     ctypes.c_float(float(built["probe_radius"])), ctypes.c_float(band), ptr(q), m, ptr(gqa),
+                     out.ctypes.data, kind.ctypes.data, ptr(g), threads)
+    if st != 0:
+        raise RuntimeError("ora_sdf failed")
+    return out, kind, g

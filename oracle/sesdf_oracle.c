@@ -1250,3 +1250,384 @@ void ora_free( void * h )
     free( o->tori );
     free( o );
 }
+
+/* ---- SDF at query points (test oracle, FP64) ---------------------------------
+ * The project's definition of the signed distance to the SES (no reference
+ * counterpart): E = probe-centre positions outside every SAS sphere
+ * (R_i = r_i + rp); with T = rp + band, outside the SAS sdf = min_i(|x - c_i| -
+ * r_i) clamped to band; inside, sdf = rp - min(T, dist(x, dE)), dE the SAS
+ * surface made of the accessible sphere patches (radial projections of x that
+ * no other SAS sphere strictly contains), the visible circles' arcs (nearest
+ * circle points likewise) and the probe positions. Inputs are the build's
+ * sorted atoms, neighbour lists, statuses and probes (ids, FP64 positions).
+ * kind: 0 clamped inside, 1 atom (outside the SAS), 2 clamped outside, 3 sphere
+ * patch, 4 circle arc, 5 probe. With gq, grad (4n, sorted order) receives
+ * sum_q gq[q] d sdf_q / d (c, r) of the active primitive: the atom or sphere
+ * distance directly, a circle point and a probe by the Lagrange /
+ * implicit-function rule on their sphere constraints |p - c_m|^2 = R_m^2. */
+static double d3len( const double v[ 3 ] ) { return sqrt( v[ 0 ] * v[ 0 ] + v[ 1 ] * v[ 1 ] + v[ 2 ] * v[ 2 ] ); }
+static void   sdf_cross( const double a[ 3 ], const double b[ 3 ], double o[ 3 ] )
+{
+    o[ 0 ] = a[ 1 ] * b[ 2 ] - a[ 2 ] * b[ 1 ];
+    o[ 1 ] = a[ 2 ] * b[ 0 ] - a[ 0 ] * b[ 2 ];
+    o[ 2 ] = a[ 0 ] * b[ 1 ] - a[ 1 ] * b[ 0 ];
+}
+
+static int sdf_hidden( const float * atoms, const uint32_t * row, uint32_t ni, uint32_t skip, double rp, const double q[ 3 ] )
+{
+    for ( uint32_t k = 0; k < ni; k++ )
+    {
+        if ( k == skip )
+            continue;
+        const float * c  = atoms + 4 * (size_t)row[ k ];
+        const double  dx = q[ 0 ] - c[ 0 ], dy = q[ 1 ] - c[ 1 ], dz = q[ 2 ] - c[ 2 ];
+        const double  R  = (double)c[ 3 ] + rp;
+        if ( dx * dx + dy * dy + dz * dz < R * R )
+            return 1;
+    }
+    return 0;
+}
+
+typedef struct
+{
+    int    kind;
+    int    a, b, c;
+    double q[ 3 ];
+    double value;
+} ora_hit_t;
+
+static void sdf_grad( const float * atoms, double rp, const ora_hit_t * h, const double x[ 3 ], double gs, double * grad )
+{
+    if ( h->kind == 1 || h->kind == 3 )
+    {
+        const float * c = atoms + 4 * (size_t)h->a;
+        double        w[ 3 ] = { x[ 0 ] - c[ 0 ], x[ 1 ] - c[ 1 ], x[ 2 ] - c[ 2 ] };
+        const double  L = d3len( w );
+        if ( !( L > 0.0 ) )
+            return;
+        double sgn = -1.0;
+        if ( h->kind == 3 && L > (double)c[ 3 ] + rp )
+            sgn = 1.0;
+        for ( int a = 0; a < 3; a++ )
+            grad[ 4 * (size_t)h->a + a ] += gs * sgn * w[ a ] / L;
+        grad[ 4 * (size_t)h->a + 3 ] += gs * sgn;
+        return;
+    }
+    if ( h->kind != 4 && h->kind != 5 )
+        return;
+    const double u0[ 3 ] = { x[ 0 ] - h->q[ 0 ], x[ 1 ] - h->q[ 1 ], x[ 2 ] - h->q[ 2 ] };
+    const double D       = d3len( u0 );
+    if ( !( D > 0.0 ) )
+        return;
+    const double u[ 3 ] = { u0[ 0 ] / D, u0[ 1 ] / D, u0[ 2 ] / D };
+    const int    m      = h->kind == 4 ? 2 : 3;
+    const int    ids[ 3 ] = { h->a, h->b, h->c };
+    double       A[ 3 ][ 3 ], R[ 3 ], w[ 3 ] = { 0, 0, 0 };
+    for ( int k = 0; k < m; k++ )
+    {
+        const float * c = atoms + 4 * (size_t)ids[ k ];
+        for ( int a = 0; a < 3; a++ )
+            A[ k ][ a ] = 2.0 * ( h->q[ a ] - c[ a ] );
+        R[ k ] = (double)c[ 3 ] + rp;
+    }
+    if ( m == 2 )
+    {
+        double g00 = 0, g01 = 0, g11 = 0, r0 = 0, r1 = 0;
+        for ( int a = 0; a < 3; a++ )
+        {
+            g00 += A[ 0 ][ a ] * A[ 0 ][ a ];
+            g01 += A[ 0 ][ a ] * A[ 1 ][ a ];
+            g11 += A[ 1 ][ a ] * A[ 1 ][ a ];
+            r0 += A[ 0 ][ a ] * u[ a ];
+            r1 += A[ 1 ][ a ] * u[ a ];
+        }
+        const double det = g00 * g11 - g01 * g01;
+        if ( !( fabs( det ) > 0.0 ) )
+            return;
+        w[ 0 ] = ( r0 * g11 - r1 * g01 ) / det;
+        w[ 1 ] = ( r1 * g00 - r0 * g01 ) / det;
+    }
+    else
+    {
+        /* sum_k w_k A_k = u (A_k as columns): Cramer's rule */
+        double c12[ 3 ], cu2[ 3 ], c01[ 3 ];
+        sdf_cross( A[ 1 ], A[ 2 ], c12 );
+        sdf_cross( u, A[ 2 ], cu2 );
+        sdf_cross( A[ 0 ], A[ 1 ], c01 );
+        const double det = A[ 0 ][ 0 ] * c12[ 0 ] + A[ 0 ][ 1 ] * c12[ 1 ] + A[ 0 ][ 2 ] * c12[ 2 ];
+        if ( !( fabs( det ) > 0.0 ) )
+            return;
+        w[ 0 ] = ( u[ 0 ] * c12[ 0 ] + u[ 1 ] * c12[ 1 ] + u[ 2 ] * c12[ 2 ] ) / det;               /* det[u, A1, A2] */
+        w[ 1 ] = ( A[ 0 ][ 0 ] * cu2[ 0 ] + A[ 0 ][ 1 ] * cu2[ 1 ] + A[ 0 ][ 2 ] * cu2[ 2 ] ) / det; /* det[A0, u, A2] */
+        w[ 2 ] = ( c01[ 0 ] * u[ 0 ] + c01[ 1 ] * u[ 1 ] + c01[ 2 ] * u[ 2 ] ) / det;               /* det[A0, A1, u] */
+    }
+    for ( int k = 0; k < m; k++ )
+    {
+        for ( int a = 0; a < 3; a++ )
+            grad[ 4 * (size_t)ids[ k ] + a ] += gs * w[ k ] * A[ k ][ a ];
+        grad[ 4 * (size_t)ids[ k ] + 3 ] += gs * 2.0 * w[ k ] * R[ k ];
+    }
+}
+
+static int cmp_dkey( const void * a, const void * b )
+{
+    const double * x = (const double *)a;
+    const double * y = (const double *)b;
+    if ( x[ 0 ] != y[ 0 ] )
+        return x[ 0 ] < y[ 0 ] ? -1 : 1;
+    return x[ 1 ] < y[ 1 ] ? -1 : ( x[ 1 ] > y[ 1 ] );
+}
+
+int ora_sdf( const float * atoms, uint32_t n, const uint32_t * noff, const uint32_t * nbr, const uint8_t * status,
+             const int32_t * ids, const double * posd, uint32_t I, float rpf, float bandf, const float * queries,
+             uint32_t m, const double * gq, double * sdf, int32_t * kind, double * grad, int threads )
+{
+    const double rp = rpf, band = bandf, T = rp + band;
+    double       lo[ 3 ] = { 1e300, 1e300, 1e300 }, hi[ 3 ] = { -1e300, -1e300, -1e300 }, rmax = 0;
+    if ( n == 0 )
+    {
+        for ( uint32_t q = 0; q < m; q++ )
+        {
+            sdf[ q ] = band;
+            if ( kind )
+                kind[ q ] = 2;
+        }
+        return 0;
+    }
+    for ( uint32_t i = 0; i < n; i++ )
+    {
+        for ( int a = 0; a < 3; a++ )
+        {
+            lo[ a ] = atoms[ 4 * i + a ] < lo[ a ] ? atoms[ 4 * i + a ] : lo[ a ];
+            hi[ a ] = atoms[ 4 * i + a ] > hi[ a ] ? atoms[ 4 * i + a ] : hi[ a ];
+        }
+        rmax = atoms[ 4 * i + 3 ] > rmax ? atoms[ 4 * i + 3 ] : rmax;
+    }
+    /* atom grid with cell >= the reach R + T */
+    const double h = rmax + rp + T + 1e-3;
+    int          dims[ 3 ];
+    for ( int a = 0; a < 3; a++ )
+    {
+        lo[ a ] -= h;
+        dims[ a ] = (int)( ( hi[ a ] + h - lo[ a ] ) / h ) + 1;
+    }
+    const uint64_t cells = (uint64_t)dims[ 0 ] * dims[ 1 ] * dims[ 2 ];
+    uint32_t *     start = (uint32_t *)calloc( cells + 1, sizeof( uint32_t ) );
+    uint32_t *     item  = (uint32_t *)malloc( sizeof( uint32_t ) * n );
+    uint32_t *     cell  = (uint32_t *)malloc( sizeof( uint32_t ) * n );
+    /* probes by their first atom */
+    uint32_t * pstart = (uint32_t *)calloc( n + 1, sizeof( uint32_t ) );
+    uint32_t * pitem  = (uint32_t *)malloc( sizeof( uint32_t ) * ( I ? I : 1 ) );
+    if ( !start || !item || !cell || !pstart || !pitem )
+        return -1;
+    for ( uint32_t i = 0; i < n; i++ )
+    {
+        int c[ 3 ];
+        for ( int a = 0; a < 3; a++ )
+            c[ a ] = (int)( ( atoms[ 4 * i + a ] - lo[ a ] ) / h );
+        cell[ i ] = (uint32_t)( ( (uint64_t)c[ 2 ] * dims[ 1 ] + c[ 1 ] ) * dims[ 0 ] + c[ 0 ] );
+        start[ cell[ i ] + 1 ]++;
+    }
+    for ( uint64_t k = 0; k < cells; k++ )
+        start[ k + 1 ] += start[ k ];
+    {
+        uint32_t * cur = (uint32_t *)malloc( sizeof( uint32_t ) * ( cells + 1 ) );
+        memcpy( cur, start, sizeof( uint32_t ) * ( cells + 1 ) );
+        for ( uint32_t i = 0; i < n; i++ )
+            item[ cur[ cell[ i ] ]++ ] = i;
+        free( cur );
+    }
+    for ( uint32_t p = 0; p < I; p++ )
+        pstart[ ids[ 4 * p ] + 1 ]++;
+    for ( uint32_t i = 0; i < n; i++ )
+        pstart[ i + 1 ] += pstart[ i ];
+    {
+        uint32_t * cur = (uint32_t *)malloc( sizeof( uint32_t ) * ( n + 1 ) );
+        memcpy( cur, pstart, sizeof( uint32_t ) * ( n + 1 ) );
+        for ( uint32_t p = 0; p < I; p++ )
+            pitem[ cur[ ids[ 4 * p ] ]++ ] = p;
+        free( cur );
+    }
+    if ( grad )
+        memset( grad, 0, sizeof( double ) * 4 * n );
+    int nthreads = threads > 0 ? threads : omp_get_max_threads();
+    /* per-thread gradient accumulators, summed at the end (deterministic per thread count) */
+    double * gpriv = grad ? (double *)calloc( (size_t)nthreads * 4 * n, sizeof( double ) ) : NULL;
+#pragma omp parallel num_threads( nthreads )
+    {
+        const int tid  = omp_get_thread_num();
+        double *  gmy  = gpriv ? gpriv + (size_t)tid * 4 * n : NULL;
+        double *  keys = (double *)malloc( sizeof( double ) * 2 * ( n < 4096 ? n : 4096 ) );
+#pragma omp for schedule( dynamic, 256 )
+        for ( uint32_t qi = 0; qi < m; qi++ )
+        {
+            const double x[ 3 ] = { queries[ 3 * (size_t)qi ], queries[ 3 * (size_t)qi + 1 ], queries[ 3 * (size_t)qi + 2 ] };
+            int          c[ 3 ];
+            for ( int a = 0; a < 3; a++ )
+                c[ a ] = (int)( ( x[ a ] - lo[ a ] ) / h );
+            uint32_t  nl = 0;
+            double    smin = 1e300, vmin = 1e300;
+            int       vatom = -1;
+            for ( int dz = -1; dz <= 1; dz++ )
+                for ( int dy = -1; dy <= 1; dy++ )
+                    for ( int dx = -1; dx <= 1; dx++ )
+                    {
+                        const int cx = c[ 0 ] + dx, cy = c[ 1 ] + dy, cz = c[ 2 ] + dz;
+                        if ( cx < 0 || cy < 0 || cz < 0 || cx >= dims[ 0 ] || cy >= dims[ 1 ] || cz >= dims[ 2 ] )
+                            continue;
+                        const uint64_t k = ( (uint64_t)cz * dims[ 1 ] + cy ) * dims[ 0 ] + cx;
+                        for ( uint32_t e = start[ k ]; e < start[ k + 1 ]; e++ )
+                        {
+                            const uint32_t i  = item[ e ];
+                            const double   w[ 3 ] = { x[ 0 ] - atoms[ 4 * i ], x[ 1 ] - atoms[ 4 * i + 1 ], x[ 2 ] - atoms[ 4 * i + 2 ] };
+                            const double   L  = d3len( w );
+                            const double   R  = (double)atoms[ 4 * i + 3 ] + rp;
+                            if ( !( L <= R + T ) )
+                                continue;
+                            smin           = L - R < smin ? L - R : smin;
+                            const double v = L - atoms[ 4 * i + 3 ];
+                            if ( v < vmin || ( v == vmin && (int)i < vatom ) )
+                            {
+                                vmin  = v;
+                                vatom = (int)i;
+                            }
+                            if ( nl < 4096 )
+                            {
+                                keys[ 2 * nl ]     = fabs( L - R );
+                                keys[ 2 * nl + 1 ] = (double)i;
+                                nl++;
+                            }
+                        }
+                    }
+            ora_hit_t hit;
+            hit.a = hit.b = hit.c = -1;
+            hit.q[ 0 ] = x[ 0 ], hit.q[ 1 ] = x[ 1 ], hit.q[ 2 ] = x[ 2 ];
+            if ( !( smin < 0.0 ) )
+            {
+                if ( vatom >= 0 && vmin <= band )
+                {
+                    hit.kind  = 1;
+                    hit.a     = vatom;
+                    hit.value = vmin;
+                }
+                else
+                {
+                    hit.kind  = 2;
+                    hit.value = band;
+                }
+            }
+            else
+            {
+                qsort( keys, nl, 2 * sizeof( double ), cmp_dkey );
+                double best = T;
+                hit.kind    = 0;
+                for ( uint32_t t = 0; t < nl; t++ )
+                {
+                    const double   dl = keys[ 2 * t ];
+                    const uint32_t i  = (uint32_t)keys[ 2 * t + 1 ];
+                    if ( !( dl < best ) )
+                        break;
+                    const float *    ci  = atoms + 4 * (size_t)i;
+                    const double     Ri  = (double)ci[ 3 ] + rp;
+                    const uint32_t * row = nbr + noff[ i ];
+                    const uint32_t   ni  = noff[ i + 1 ] - noff[ i ];
+                    /* sphere patch */
+                    {
+                        double       w[ 3 ] = { x[ 0 ] - ci[ 0 ], x[ 1 ] - ci[ 1 ], x[ 2 ] - ci[ 2 ] };
+                        const double L      = d3len( w );
+                        if ( L > 0.0 )
+                        {
+                            const double q[ 3 ] = { ci[ 0 ] + w[ 0 ] * ( Ri / L ), ci[ 1 ] + w[ 1 ] * ( Ri / L ), ci[ 2 ] + w[ 2 ] * ( Ri / L ) };
+                            if ( !sdf_hidden( atoms, row, ni, 0xffffffffu, rp, q ) && dl < best )
+                            {
+                                best     = dl;
+                                hit.kind = 3;
+                                hit.a    = (int)i;
+                                memcpy( hit.q, q, sizeof( q ) );
+                            }
+                        }
+                    }
+                    /* visible circles */
+                    for ( uint32_t s = 0; s < ni; s++ )
+                    {
+                        if ( status[ noff[ i ] + s ] == 0 )
+                            continue;
+                        const float * cj = atoms + 4 * (size_t)row[ s ];
+                        const double  Rj = (double)cj[ 3 ] + rp;
+                        const double  d[ 3 ] = { (double)cj[ 0 ] - ci[ 0 ], (double)cj[ 1 ] - ci[ 1 ], (double)cj[ 2 ] - ci[ 2 ] };
+                        const double  dd = d[ 0 ] * d[ 0 ] + d[ 1 ] * d[ 1 ] + d[ 2 ] * d[ 2 ];
+                        const double  tt = ( Ri * Ri - Rj * Rj + dd ) / ( 2.0 * dd );
+                        const double  r2 = Ri * Ri - tt * tt * dd;
+                        if ( !( r2 > 0.0 ) )
+                            continue;
+                        const double r    = sqrt( r2 );
+                        const double dl2  = sqrt( dd );
+                        const double nn[ 3 ] = { d[ 0 ] / dl2, d[ 1 ] / dl2, d[ 2 ] / dl2 };
+                        const double cc[ 3 ] = { ci[ 0 ] + d[ 0 ] * tt, ci[ 1 ] + d[ 1 ] * tt, ci[ 2 ] + d[ 2 ] * tt };
+                        const double w[ 3 ]  = { x[ 0 ] - cc[ 0 ], x[ 1 ] - cc[ 1 ], x[ 2 ] - cc[ 2 ] };
+                        const double hh      = w[ 0 ] * nn[ 0 ] + w[ 1 ] * nn[ 1 ] + w[ 2 ] * nn[ 2 ];
+                        const double v[ 3 ]  = { w[ 0 ] - hh * nn[ 0 ], w[ 1 ] - hh * nn[ 1 ], w[ 2 ] - hh * nn[ 2 ] };
+                        const double rho     = d3len( v );
+                        double       dist, q[ 3 ] = { cc[ 0 ], cc[ 1 ], cc[ 2 ] };
+                        if ( rho > 1e-6 )
+                        {
+                            for ( int a = 0; a < 3; a++ )
+                                q[ a ] = cc[ a ] + v[ a ] * ( r / rho );
+                            dist = sqrt( hh * hh + ( rho - r ) * ( rho - r ) );
+                            if ( !( dist < best ) || sdf_hidden( atoms, row, ni, s, rp, q ) )
+                                continue;
+                        }
+                        else
+                        {
+                            dist = sqrt( hh * hh + r2 );
+                            if ( !( dist < best ) )
+                                continue;
+                        }
+                        best     = dist;
+                        hit.kind = 4;
+                        hit.a    = (int)i;
+                        hit.b    = (int)row[ s ];
+                        memcpy( hit.q, q, sizeof( q ) );
+                    }
+                    /* probes whose first atom is i */
+                    for ( uint32_t e = pstart[ i ]; e < pstart[ i + 1 ]; e++ )
+                    {
+                        const uint32_t p    = pitem[ e ];
+                        const double * pp   = posd + 4 * (size_t)p;
+                        const double   w[ 3 ] = { x[ 0 ] - pp[ 0 ], x[ 1 ] - pp[ 1 ], x[ 2 ] - pp[ 2 ] };
+                        const double   dist = d3len( w );
+                        if ( dist < best )
+                        {
+                            best     = dist;
+                            hit.kind = 5;
+                            hit.a    = ids[ 4 * p ];
+                            hit.b    = ids[ 4 * p + 1 ];
+                            hit.c    = ids[ 4 * p + 2 ];
+                            memcpy( hit.q, pp, 3 * sizeof( double ) );
+                        }
+                    }
+                }
+                hit.value = rp - best;
+            }
+            sdf[ qi ] = hit.value;
+            if ( kind )
+                kind[ qi ] = hit.kind;
+            if ( gmy && gq )
+                sdf_grad( atoms, rp, &hit, x, gq[ qi ], gmy );
+        }
+        free( keys );
+    }
+    if ( grad )
+    {
+        for ( int t = 0; t < nthreads; t++ )
+            for ( size_t k = 0; k < 4 * (size_t)n; k++ )
+                grad[ k ] += gpriv[ (size_t)t * 4 * n + k ];
+        free( gpriv );
+    }
+    free( start );
+    free( item );
+    free( cell );
+    free( pstart );
+    free( pitem );
+    return 0;
+}

@@ -31,8 +31,9 @@ EXPORTS = [
     "sesgb_error_string", "sesgb_last_error", "sesgb_destroy", "sesgb_stage_times", "sesgb_stage_name",
     "sesgb_launch_count", "sesgb_build_async", "sesgb_finish", "sesgb_sort_atoms_noalloc",
     "sesgb_create_batch", "sesgb_batch_molecules", "sesgb_molecule_record", "sesgb_get_full_molecule",
-    "sesgb_get_exterior_molecule",
+    "sesgb_get_exterior_molecule", "sesgb_sdf", "sesgb_sdf_backward",
 ]
+SDF_BAND = 3.0
 MOL_FIELDS = ["atoms", "sectors", "full_circles", "partial_circles", "probes", "singular_probes", "segments", "tori",
               "atom_base", "sector_base", "full_base", "partial_base", "probe_base", "singular_base", "segment_base",
               "tori_base"]
@@ -126,6 +127,8 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         lib.sesgb_molecule_record.argtypes = [P, U32, P]
         lib.sesgb_get_full_molecule.argtypes = [P, U32, ctypes.POINTER(FullData)]
         lib.sesgb_get_exterior_molecule.argtypes = [P, U32, ctypes.POINTER(ExteriorData)]
+        lib.sesgb_sdf.argtypes = [P, P, U32, P, P, P]
+        lib.sesgb_sdf_backward.argtypes = [P, P, U32, P, P, P]
         _lib = lib
     return _lib
 
@@ -232,6 +235,15 @@ class SesBuild:
         n = ctypes.c_uint32()
         self._check(self._lib.sesgb_stage_times(self._h, ms, 16, ctypes.byref(n)), "stage_times")
         return {self._lib.sesgb_stage_name(k).decode(): float(ms[k]) for k in range(n.value)}
+
+    def sdf(self, queries_ptr: int, m: int, out_ptr: int, kind_ptr: int | None = None, stream: int | None = None):
+        """Signed distance to the SES at m float3 query points (device pointers); enqueued on `stream`."""
+        self._check(self._lib.sesgb_sdf(self._h, queries_ptr, m, out_ptr, kind_ptr, stream), "sdf")
+
+    def sdf_backward(self, queries_ptr: int, m: int, grad_sdf_ptr: int, grad_atoms_ptr: int, stream: int | None = None):
+        """grad_atoms (float4[n], input order) = sum_q grad_sdf[q] d sdf_q / d (x, y, z, r)."""
+        self._check(self._lib.sesgb_sdf_backward(self._h, queries_ptr, m, grad_sdf_ptr, grad_atoms_ptr, stream),
+                    "sdf_backward")
 
     @property
     def max_neighbor_per_atom(self) -> int:

@@ -38,6 +38,9 @@ struct sesgb_ctx
     std::vector<uint32_t> molCells;
     uint32_t *            hMol = nullptr; // pinned copy of Build::molCounts
 
+    // SDF queries: gradient scratch in sorted atom order
+    float * gradSorted = nullptr;
+
     Build          b {};
     DeviceCounts * hCounts = nullptr;
     void *         scanScratch = nullptr;
@@ -786,7 +789,52 @@ extern "C"
             cudaFreeHost( c->hCounts );
         if ( c->hMol )
             cudaFreeHost( c->hMol );
+        if ( c->gradSorted )
+            cudaFree( c->gradSorted );
         delete c;
+    }
+
+    // ---- signed distance at query points ---------------------------------------
+    static int sdf_prepare( sesgb_ctx * c, cudaStream_t s )
+    {
+        if ( !c->built )
+            return SESGB_ERR_NOT_BUILT;
+        if ( c->mode != SESGB_MODE_FULL || c->nMol != 1 )
+        {
+            c->err = "the SDF needs a full-surface build of one molecule";
+            return SESGB_ERR_MODE;
+        }
+        const float reach = c->hCounts->rmax + 2.f * c->rp + SESGB_SDF_BAND;
+        launch_fine_params( c->b, reach, c->n, s );
+        launch_cells( c->b, 0, c->n, nullptr, c->scanScratch, s );
+        return cuda_ok( c, cudaGetLastError(), "sdf grid" ) ? SESGB_OK : SESGB_ERR_CUDA;
+    }
+
+    int sesgb_sdf( sesgb_ctx * c, const float * device_queries, uint32_t m, float * device_sdf, int * device_kind, void * stream )
+    {
+        if ( !c || ( m && ( !device_queries || !device_sdf ) ) )
+            return SESGB_ERR_INVALID;
+        cudaStream_t s  = static_cast<cudaStream_t>( stream );
+        int          st = sdf_prepare( c, s );
+        if ( st != SESGB_OK )
+            return st;
+        launch_sdf( c->b, device_queries, m, SESGB_SDF_BAND, device_sdf, device_kind, s );
+        return cuda_ok( c, cudaGetLastError(), "sdf" ) ? SESGB_OK : SESGB_ERR_CUDA;
+    }
+
+    int sesgb_sdf_backward( sesgb_ctx * c, const float * device_queries, uint32_t m, const float * device_grad_sdf,
+                            float * device_grad_atoms, void * stream )
+    {
+        if ( !c || !device_grad_atoms || ( m && ( !device_queries || !device_grad_sdf ) ) )
+            return SESGB_ERR_INVALID;
+        cudaStream_t s  = static_cast<cudaStream_t>( stream );
+        int          st = sdf_prepare( c, s );
+        if ( st != SESGB_OK )
+            return st;
+        if ( !c->gradSorted && !cuda_ok( c, cudaMalloc( &c->gradSorted, sizeof( float ) * 4 * std::max<size_t>( c->n, 1 ) ), "cudaMalloc" ) )
+            return SESGB_ERR_CUDA;
+        launch_sdf_backward( c->b, device_queries, m, SESGB_SDF_BAND, device_grad_sdf, c->gradSorted, device_grad_atoms, s );
+        return cuda_ok( c, cudaGetLastError(), "sdf backward" ) ? SESGB_OK : SESGB_ERR_CUDA;
     }
 
     int sesgb_create_batch( const float * atoms, const uint32_t * molecule_start, uint32_t molecules, float probe_radius,

@@ -53,6 +53,7 @@ namespace sesgb
         kOverflowAtomProbes = 1u << 10, // an atom owns more probes than one warp holds (128)
         kOverflowVisBand    = 1u << 11, // more visibility tests in the float32 band than the queue holds
         kOverflowPairs      = 1u << 12, // more neighbour pairs than the touch-mask buffer holds
+        kOverflowSdfList    = 1u << 13, // a query point had more atoms within reach than the SDF search holds
     };
 
     enum Fp64Stage : uint32_t

@@ -2190,3 +2190,430 @@ namespace sesgb
         counted();
     }
 } // namespace sesgb
+
+// ---- signed distance to the SES at query points -----------------------------
+//
+// Definition (project-written; the reference has no SDF). E is the set of
+// probe-centre positions that overlap no atom: outside every SAS sphere
+// (radius R_i = r_i + rp). With T = rp + kSdfBand:
+//   x outside the SAS:  sdf = min_i (|x - c_i| - r_i), clamped to kSdfBand;
+//   x inside the SAS:   sdf = rp - min(T, dist(x, dE)).
+// dE is the SAS surface: the accessible parts of the SAS spheres, the arcs of
+// the visible circles and the probe positions. The nearest point of dE is the
+// radial projection of x on a sphere, the nearest point of a circle, or a
+// probe, whichever is nearest among those that lie on dE (not strictly inside
+// another SAS sphere); only atoms with |x - c_i| <= R_i + T can carry one.
+// The gradient with respect to the atoms follows the active primitive: the
+// sphere or atom distance directly, a circle point and a probe by the
+// Lagrange / implicit-function rule for points constrained to |p - c_m| = R_m.
+namespace sesgb
+{
+    namespace
+    {
+        constexpr int   kSdfWarps = 4;   // warps per block (one query per warp)
+        constexpr int   kSdfList  = 256; // atoms within reach held per query
+
+        enum SdfKind : int
+        {
+            kSdfClampInside = 0, // deeper than T below dE
+            kSdfAtom        = 1, // outside the SAS: nearest vdW sphere
+            kSdfClampOutside = 2,
+            kSdfSphere      = 3, // radial projection on an accessible SAS sphere patch
+            kSdfCircle      = 4, // nearest point of an accessible arc
+            kSdfProbe       = 5, // probe position (vertex of dE)
+        };
+
+        struct SdfHit
+        {
+            int    kind;
+            int    a, b, c; // sorted atom ids
+            float3 q;       // point of dE (or of the vdW sphere)
+            float  value;
+        };
+
+        struct SdfSmem
+        {
+            unsigned long long key[ kSdfList ]; // (delta bits << 32) | atom
+            float4             nb[ 520 ];       // neighbourhood of the atom being examined: (c_k, R_k)
+        };
+
+        __device__ __forceinline__ void warp_min_hit( float & best, int & owner )
+        {
+            // smallest candidate distance, lowest lane on ties
+            for ( int o = 16; o > 0; o >>= 1 )
+            {
+                const float ob = __shfl_xor_sync( 0xffffffffu, best, o );
+                const int   oo = __shfl_xor_sync( 0xffffffffu, owner, o );
+                if ( ob < best || ( ob == best && oo < owner ) )
+                {
+                    best  = ob;
+                    owner = oo;
+                }
+            }
+        }
+
+        // one query, the whole warp; the hit is valid in every lane
+        __device__ SdfHit sdf_query( const Build & b, float3 x, SdfSmem & sm, float band, uint32_t & overflow )
+        {
+            const uint32_t lane = lane_id();
+            const float    T    = b.rp + band;
+            const FineGrid g    = b.fine[ 0 ];
+            Rows           rows;
+            stencil_rows( g, b.cellStart, fine_cell( g, x.x, x.y, x.z ), rows );
+            // atoms within reach; minima of |x - c| - R (SAS) and |x - c| - r (vdW)
+            uint32_t nl = 0;
+            float    smin = 3.4e38f, vmin = 3.4e38f;
+            int      vatom = 0x7fffffff;
+            for ( uint32_t base = 0; base < rows.total; base += 32 )
+            {
+                const uint32_t f    = base + lane;
+                bool           keep = false;
+                uint32_t       i    = 0;
+                float          dl   = 0.f;
+                if ( f < rows.total )
+                {
+                    const uint32_t idx = row_item( rows, f );
+                    i                  = b.cellItems[ idx ];
+                    const float4 c     = b.cellPos[ idx ];
+                    const float  L     = sqrtf( ( x.x - c.x ) * ( x.x - c.x ) + ( x.y - c.y ) * ( x.y - c.y ) + ( x.z - c.z ) * ( x.z - c.z ) );
+                    const float  R     = c.w + b.rp;
+                    keep               = L <= R + T;
+                    if ( keep )
+                    {
+                        smin = fminf( smin, L - R );
+                        const float v = L - c.w;
+                        if ( v < vmin || ( v == vmin && (int)i < vatom ) )
+                        {
+                            vmin  = v;
+                            vatom = (int)i;
+                        }
+                        dl = fabsf( L - R );
+                    }
+                }
+                const uint32_t mk = __ballot_sync( 0xffffffffu, keep );
+                const uint32_t at = nl + __popc( mk & lanemask_lt() );
+                if ( keep && at < (uint32_t)kSdfList )
+                    sm.key[ at ] = ( (unsigned long long)__float_as_uint( dl ) << 32 ) | i;
+                nl += __popc( mk );
+            }
+            if ( nl > (uint32_t)kSdfList )
+            {
+                overflow = 1;
+                nl       = kSdfList;
+            }
+            for ( int o = 16; o > 0; o >>= 1 )
+            {
+                smin          = fminf( smin, __shfl_xor_sync( 0xffffffffu, smin, o ) );
+                const float v = __shfl_xor_sync( 0xffffffffu, vmin, o );
+                const int   a = __shfl_xor_sync( 0xffffffffu, vatom, o );
+                if ( v < vmin || ( v == vmin && a < vatom ) )
+                {
+                    vmin  = v;
+                    vatom = a;
+                }
+            }
+            SdfHit hit;
+            hit.a = hit.b = hit.c = -1;
+            hit.q                 = x;
+            if ( !( smin < 0.f ) )
+            {
+                // outside the SAS (or nothing within reach)
+                if ( vatom != 0x7fffffff && vmin <= band )
+                {
+                    hit.kind  = kSdfAtom;
+                    hit.a     = vatom;
+                    hit.value = vmin;
+                }
+                else
+                {
+                    hit.kind  = kSdfClampOutside;
+                    hit.value = band;
+                }
+                return hit;
+            }
+            __syncwarp();
+            warp_bitonic_sort<unsigned long long>( sm.key, nl, kSdfList, ~0ull );
+            float best  = T;
+            hit.kind    = kSdfClampInside;
+            for ( uint32_t t = 0; t < nl; t++ )
+            {
+                const unsigned long long key = sm.key[ t ];
+                const float              dl  = __uint_as_float( (uint32_t)( key >> 32 ) );
+                if ( !( dl < best ) )
+                    break; // every candidate of this and later atoms is at least dl away
+                const uint32_t i   = (uint32_t)key;
+                const float4   ci  = b.atoms[ i ];
+                const float    Ri  = ci.w + b.rp;
+                const uint32_t ni  = b.nbrCount[ i ];
+                const size_t   row = (size_t)i * b.cap;
+                for ( uint32_t s = lane; s < ni; s += 32 )
+                {
+                    const float4 ck = b.atoms[ b.nbr[ row + s ] ];
+                    sm.nb[ s ]      = make_float4( ck.x, ck.y, ck.z, ck.w + b.rp );
+                }
+                __syncwarp();
+                // candidates of this atom, one per lane at most, reduced at the end
+                float  cand = 3.4e38f;
+                int    ck = 0, cb = -1, cc = -1;
+                float3 cq = x;
+                // radial projection on sphere i
+                {
+                    const float3 w = make_float3( x.x - ci.x, x.y - ci.y, x.z - ci.z );
+                    const float  L = sqrtf( w.x * w.x + w.y * w.y + w.z * w.z );
+                    if ( L > 0.f )
+                    {
+                        const float3 q = make_float3( ci.x + w.x * ( Ri / L ), ci.y + w.y * ( Ri / L ), ci.z + w.z * ( Ri / L ) );
+                        bool         hidden = false;
+                        for ( uint32_t s = lane; s < ni; s += 32 )
+                        {
+                            const float4 nk = sm.nb[ s ];
+                            const float  dx = q.x - nk.x, dy = q.y - nk.y, dz = q.z - nk.z;
+                            hidden          = hidden || ( dx * dx + dy * dy + dz * dz < nk.w * nk.w );
+                        }
+                        if ( !__any_sync( 0xffffffffu, hidden ) && lane == 0 )
+                        {
+                            cand = dl;
+                            ck   = kSdfSphere;
+                            cq   = q;
+                        }
+                    }
+                }
+                // nearest points of the visible circles of i
+                for ( uint32_t s0 = 0; s0 < ni; s0 += 32 )
+                {
+                    const uint32_t s = s0 + lane;
+                    if ( s >= ni || b.status[ row + s ] == 0 )
+                        continue;
+                    const float4 nj = sm.nb[ s ];
+                    const float3 d  = make_float3( nj.x - ci.x, nj.y - ci.y, nj.z - ci.z );
+                    const float  dd = d.x * d.x + d.y * d.y + d.z * d.z;
+                    const float  tt = ( Ri * Ri - nj.w * nj.w + dd ) / ( 2.f * dd );
+                    const float  r2 = Ri * Ri - tt * tt * dd;
+                    if ( !( r2 > 0.f ) )
+                        continue;
+                    const float  r   = sqrtf( r2 );
+                    const float  inv = rsqrtf( dd );
+                    const float3 n   = make_float3( d.x * inv, d.y * inv, d.z * inv );
+                    const float3 c   = make_float3( ci.x + d.x * tt, ci.y + d.y * tt, ci.z + d.z * tt );
+                    const float3 w   = make_float3( x.x - c.x, x.y - c.y, x.z - c.z );
+                    const float  h   = w.x * n.x + w.y * n.y + w.z * n.z;
+                    const float3 v   = make_float3( w.x - h * n.x, w.y - h * n.y, w.z - h * n.z );
+                    const float  rho = sqrtf( v.x * v.x + v.y * v.y + v.z * v.z );
+                    float        dist;
+                    float3       q = c;
+                    if ( rho > 1e-6f )
+                    {
+                        q    = make_float3( c.x + v.x * ( r / rho ), c.y + v.y * ( r / rho ), c.z + v.z * ( r / rho ) );
+                        dist = sqrtf( h * h + ( rho - r ) * ( rho - r ) );
+                        if ( !( dist < cand ) || !( dist < best ) )
+                            continue;
+                        bool hidden = false;
+                        for ( uint32_t k = 0; k < ni && !hidden; k++ )
+                        {
+                            if ( k == s )
+                                continue;
+                            const float4 nk = sm.nb[ k ];
+                            const float  dx = q.x - nk.x, dy = q.y - nk.y, dz = q.z - nk.z;
+                            hidden          = dx * dx + dy * dy + dz * dz < nk.w * nk.w;
+                        }
+                        if ( hidden )
+                            continue;
+                    }
+                    else
+                    {
+                        // x on the axis: every point of the circle is as near; a visible
+                        // circle has an accessible arc
+                        dist = sqrtf( h * h + r2 );
+                        if ( !( dist < cand ) || !( dist < best ) )
+                            continue;
+                    }
+                    cand = dist;
+                    ck   = kSdfCircle;
+                    cb   = (int)b.nbr[ row + s ];
+                    cq   = q;
+                }
+                // probes owned by i (the smallest atom of their triplet)
+                {
+                    const uint32_t chunk = b.chunkStart[ i ], len = b.chunkLen[ i ];
+                    for ( uint32_t e = lane; e < len; e += 32 )
+                    {
+                        const int4 cid = b.stageCid[ chunk + e ];
+                        if ( cid.w == 0 )
+                            continue;
+                        const float4 p    = b.stagePos[ chunk + e ];
+                        const float  dist = sqrtf( ( x.x - p.x ) * ( x.x - p.x ) + ( x.y - p.y ) * ( x.y - p.y ) + ( x.z - p.z ) * ( x.z - p.z ) );
+                        if ( dist < cand )
+                        {
+                            const int4 ids = b.stageIds[ chunk + e ];
+                            cand           = dist;
+                            ck             = kSdfProbe;
+                            cb             = ids.y;
+                            cc             = ids.z;
+                            cq             = make_float3( p.x, p.y, p.z );
+                        }
+                    }
+                }
+                float wbest = cand;
+                int   owner = (int)lane;
+                warp_min_hit( wbest, owner );
+                if ( wbest < best )
+                {
+                    best     = wbest;
+                    hit.kind = __shfl_sync( 0xffffffffu, ck, owner );
+                    hit.a    = (int)i;
+                    hit.b    = __shfl_sync( 0xffffffffu, cb, owner );
+                    hit.c    = __shfl_sync( 0xffffffffu, cc, owner );
+                    hit.q.x  = __shfl_sync( 0xffffffffu, cq.x, owner );
+                    hit.q.y  = __shfl_sync( 0xffffffffu, cq.y, owner );
+                    hit.q.z  = __shfl_sync( 0xffffffffu, cq.z, owner );
+                }
+                __syncwarp();
+            }
+            hit.value = b.rp - best;
+            return hit;
+        }
+
+        __device__ __forceinline__ void add_grad( float * g, uint32_t atom, float gx, float gy, float gz, float gr )
+        {
+            atomicAdd( g + 4 * atom + 0, gx );
+            atomicAdd( g + 4 * atom + 1, gy );
+            atomicAdd( g + 4 * atom + 2, gz );
+            atomicAdd( g + 4 * atom + 3, gr );
+        }
+
+        // d sdf / d (c, r) of the active primitive, scaled by gs, into g (sorted order)
+        __device__ void sdf_gradient( const Build & b, const SdfHit & h, float3 x, float gs, float * g )
+        {
+            if ( h.kind == kSdfAtom || h.kind == kSdfSphere )
+            {
+                // sdf = |x - c_a| - r_a (outside the SAS, or x inside sphere a); the
+                // opposite sign when x lies outside sphere a but inside another
+                const float4 c = b.atoms[ h.a ];
+                const float3 w = make_float3( x.x - c.x, x.y - c.y, x.z - c.z );
+                const float  L = sqrtf( w.x * w.x + w.y * w.y + w.z * w.z );
+                if ( !( L > 0.f ) )
+                    return;
+                float sgn = -1.f;
+                if ( h.kind == kSdfSphere && L > c.w + b.rp )
+                    sgn = 1.f;
+                add_grad( g, (uint32_t)h.a, gs * sgn * w.x / L, gs * sgn * w.y / L, gs * sgn * w.z / L, gs * sgn );
+                return;
+            }
+            if ( h.kind != kSdfCircle && h.kind != kSdfProbe )
+                return;
+            const float3 p = h.q;
+            const float  dx = x.x - p.x, dy = x.y - p.y, dz = x.z - p.z;
+            const float  D  = sqrtf( dx * dx + dy * dy + dz * dz );
+            if ( !( D > 0.f ) )
+                return;
+            const float3 u = make_float3( dx / D, dy / D, dz / D );
+            const int    m = h.kind == kSdfCircle ? 2 : 3;
+            const int    ids[ 3 ] = { h.a, h.b, h.c };
+            float3       a[ 3 ];
+            float        R[ 3 ];
+            for ( int k = 0; k < m; k++ )
+            {
+                const float4 c = b.atoms[ ids[ k ] ];
+                a[ k ]         = make_float3( 2.f * ( p.x - c.x ), 2.f * ( p.y - c.y ), 2.f * ( p.z - c.z ) );
+                R[ k ]         = c.w + b.rp;
+            }
+            // multipliers w: sum_k w_k a_k = u (least squares for the circle, exact for the probe)
+            float w[ 3 ] = { 0.f, 0.f, 0.f };
+            if ( m == 2 )
+            {
+                const float g00 = a[ 0 ].x * a[ 0 ].x + a[ 0 ].y * a[ 0 ].y + a[ 0 ].z * a[ 0 ].z;
+                const float g01 = a[ 0 ].x * a[ 1 ].x + a[ 0 ].y * a[ 1 ].y + a[ 0 ].z * a[ 1 ].z;
+                const float g11 = a[ 1 ].x * a[ 1 ].x + a[ 1 ].y * a[ 1 ].y + a[ 1 ].z * a[ 1 ].z;
+                const float r0  = a[ 0 ].x * u.x + a[ 0 ].y * u.y + a[ 0 ].z * u.z;
+                const float r1  = a[ 1 ].x * u.x + a[ 1 ].y * u.y + a[ 1 ].z * u.z;
+                const float det = g00 * g11 - g01 * g01;
+                if ( !( fabsf( det ) > 0.f ) )
+                    return;
+                w[ 0 ] = ( r0 * g11 - r1 * g01 ) / det;
+                w[ 1 ] = ( r1 * g00 - r0 * g01 ) / det;
+            }
+            else
+            {
+                // columns a_0, a_1, a_2: Cramer's rule
+                const float3 c01 = make_float3( a[ 1 ].y * a[ 2 ].z - a[ 1 ].z * a[ 2 ].y, a[ 1 ].z * a[ 2 ].x - a[ 1 ].x * a[ 2 ].z,
+                                                a[ 1 ].x * a[ 2 ].y - a[ 1 ].y * a[ 2 ].x );
+                const float det = a[ 0 ].x * c01.x + a[ 0 ].y * c01.y + a[ 0 ].z * c01.z;
+                if ( !( fabsf( det ) > 0.f ) )
+                    return;
+                const float3 cu1 = make_float3( u.y * a[ 2 ].z - u.z * a[ 2 ].y, u.z * a[ 2 ].x - u.x * a[ 2 ].z, u.x * a[ 2 ].y - u.y * a[ 2 ].x );
+                const float3 c0v = make_float3( a[ 0 ].y * a[ 1 ].z - a[ 0 ].z * a[ 1 ].y, a[ 0 ].z * a[ 1 ].x - a[ 0 ].x * a[ 1 ].z,
+                                                a[ 0 ].x * a[ 1 ].y - a[ 0 ].y * a[ 1 ].x );
+                w[ 0 ] = ( u.x * c01.x + u.y * c01.y + u.z * c01.z ) / det;                 // det[u, a1, a2]
+                w[ 1 ] = ( a[ 0 ].x * cu1.x + a[ 0 ].y * cu1.y + a[ 0 ].z * cu1.z ) / det;  // det[a0, u, a2]
+                w[ 2 ] = ( c0v.x * u.x + c0v.y * u.y + c0v.z * u.z ) / det;                 // det[a0, a1, u]
+            }
+            // sdf = rp - D: d sdf / d c_k = w_k a_k, d sdf / d r_k = 2 w_k R_k
+            for ( int k = 0; k < m; k++ )
+                add_grad( g, (uint32_t)ids[ k ], gs * w[ k ] * a[ k ].x, gs * w[ k ] * a[ k ].y, gs * w[ k ] * a[ k ].z,
+                          gs * 2.f * w[ k ] * R[ k ] );
+        }
+
+        template<bool kBackward>
+        __global__ void __launch_bounds__( 32 * kSdfWarps ) k_sdf( Build b, const float * queries, uint32_t m, float band,
+                                                                   float * sdf, const float * gradSdf, float * gradSorted,
+                                                                   int * kind )
+        {
+            __shared__ SdfSmem smem[ kSdfWarps ];
+            const uint32_t     warp = threadIdx.x >> 5, lane = lane_id();
+            uint32_t           overflow = 0;
+            for ( uint32_t qi = blockIdx.x * kSdfWarps + warp; qi < m; qi += gridDim.x * kSdfWarps )
+            {
+                const float3 x = make_float3( queries[ 3 * (size_t)qi ], queries[ 3 * (size_t)qi + 1 ], queries[ 3 * (size_t)qi + 2 ] );
+                const SdfHit h = sdf_query( b, x, smem[ warp ], band, overflow );
+                if ( lane == 0 )
+                {
+                    if ( kBackward )
+                        sdf_gradient( b, h, x, gradSdf[ qi ], gradSorted );
+                    else
+                    {
+                        sdf[ qi ] = h.value;
+                        if ( kind )
+                            kind[ qi ] = h.kind;
+                    }
+                }
+            }
+            if ( lane == 0 && overflow )
+                atomicOr( &b.counts->overflow, (uint32_t)kOverflowSdfList );
+        }
+
+        __global__ void k_sdf_unsort( Build b, const float * gradSorted, float * gradInput )
+        {
+            for ( uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < b.n; s += gridDim.x * blockDim.x )
+            {
+                const uint32_t i = b.perm[ s ];
+                for ( int k = 0; k < 4; k++ )
+                    gradInput[ 4 * (size_t)i + k ] = gradSorted[ 4 * (size_t)s + k ];
+            }
+        }
+    } // namespace
+
+    void launch_sdf( const Build & b, const float * queries, uint32_t m, float band, float * sdf, int * kind, cudaStream_t s )
+    {
+        if ( !m )
+            return;
+        const uint32_t blocks = min( persistent_blocks( 32 * kSdfWarps ) * 2, ( m + kSdfWarps - 1 ) / kSdfWarps );
+        k_sdf<false><<<blocks, 32 * kSdfWarps, 0, s>>>( b, queries, m, band, sdf, nullptr, nullptr, kind );
+        counted();
+    }
+    void launch_sdf_backward( const Build & b, const float * queries, uint32_t m, float band, const float * gradSdf,
+                              float * gradSorted, float * gradInput, cudaStream_t s )
+    {
+        cudaMemsetAsync( gradSorted, 0, sizeof( float ) * 4 * (size_t)b.n, s );
+        if ( m )
+        {
+            const uint32_t blocks = min( persistent_blocks( 32 * kSdfWarps ) * 2, ( m + kSdfWarps - 1 ) / kSdfWarps );
+            k_sdf<true><<<blocks, 32 * kSdfWarps, 0, s>>>( b, queries, m, band, nullptr, gradSdf, gradSorted, nullptr );
+            counted();
+        }
+        if ( b.n )
+        {
+            k_sdf_unsort<<<blocks_for( b.n, 256 ), 256, 0, s>>>( b, gradSorted, gradInput );
+            counted();
+        }
+    }
+} // namespace sesgb

@@ -498,3 +498,104 @@ void sesgb_synth_uniform( uint64_t seed, uint32_t count, double * out )
     for ( uint32_t i = 0; i < count; i++ )
         out[ i ] = rng_uniform( &rng );
 }
+
+/* Query points for the SDF: uniform in the atoms' bounding box (getAabb:
+ * min(c - r), max(c + r)), kept when |min_i(|x - c_i| - r_i)| <= band. Draws
+ * until m points are kept (at most 10000 m draws); returns the number kept. */
+uint32_t sesgb_synth_queries( const float * atoms, uint32_t n, uint32_t m, uint64_t seed, float band, float * out )
+{
+    if ( n == 0 || m == 0 )
+        return 0;
+    double lo[ 3 ] = { 1e300, 1e300, 1e300 }, hi[ 3 ] = { -1e300, -1e300, -1e300 }, rmax = 0.0;
+    for ( uint32_t i = 0; i < n; i++ )
+        for ( int a = 0; a < 3; a++ )
+        {
+            const double c = atoms[ 4 * i + a ], r = atoms[ 4 * i + 3 ];
+            lo[ a ]        = c - r < lo[ a ] ? c - r : lo[ a ];
+            hi[ a ]        = c + r > hi[ a ] ? c + r : hi[ a ];
+            rmax           = r > rmax ? r : rmax;
+        }
+    /* cell grid over the box, cell >= band + rmax: the 27 cells around x hold every atom within band of its surface */
+    const double h = (double)band + rmax + 1e-3;
+    int          dims[ 3 ];
+    for ( int a = 0; a < 3; a++ )
+    {
+        dims[ a ] = (int)( ( hi[ a ] - lo[ a ] ) / h ) + 1;
+        if ( dims[ a ] < 1 )
+            dims[ a ] = 1;
+    }
+    const uint64_t cells = (uint64_t)dims[ 0 ] * dims[ 1 ] * dims[ 2 ];
+    uint32_t *     start = (uint32_t *)calloc( cells + 1, sizeof( uint32_t ) );
+    uint32_t *     item  = (uint32_t *)malloc( sizeof( uint32_t ) * n );
+    uint32_t *     cell  = (uint32_t *)malloc( sizeof( uint32_t ) * n );
+    if ( !start || !item || !cell )
+    {
+        free( start );
+        free( item );
+        free( cell );
+        return 0;
+    }
+    for ( uint32_t i = 0; i < n; i++ )
+    {
+        int c[ 3 ];
+        for ( int a = 0; a < 3; a++ )
+        {
+            c[ a ] = (int)( ( atoms[ 4 * i + a ] - lo[ a ] ) / h );
+            c[ a ] = c[ a ] < 0 ? 0 : ( c[ a ] >= dims[ a ] ? dims[ a ] - 1 : c[ a ] );
+        }
+        cell[ i ] = (uint32_t)( ( (uint64_t)c[ 2 ] * dims[ 1 ] + c[ 1 ] ) * dims[ 0 ] + c[ 0 ] );
+        start[ cell[ i ] + 1 ]++;
+    }
+    for ( uint64_t k = 0; k < cells; k++ )
+        start[ k + 1 ] += start[ k ];
+    {
+        uint32_t * cur = (uint32_t *)malloc( sizeof( uint32_t ) * ( cells + 1 ) );
+        memcpy( cur, start, sizeof( uint32_t ) * ( cells + 1 ) );
+        for ( uint32_t i = 0; i < n; i++ )
+            item[ cur[ cell[ i ] ]++ ] = i;
+        free( cur );
+    }
+    rng_t    r;
+    uint32_t kept = 0;
+    rng_seed( &r, seed );
+    for ( uint64_t draw = 0; kept < m && draw < 10000ull * m; draw++ )
+    {
+        float x[ 3 ];
+        int   c[ 3 ];
+        for ( int a = 0; a < 3; a++ )
+        {
+            x[ a ] = (float)( lo[ a ] + ( hi[ a ] - lo[ a ] ) * rng_uniform( &r ) );
+            c[ a ] = (int)( ( x[ a ] - lo[ a ] ) / h );
+            c[ a ] = c[ a ] < 0 ? 0 : ( c[ a ] >= dims[ a ] ? dims[ a ] - 1 : c[ a ] );
+        }
+        double best = 1e300;
+        for ( int dz = -1; dz <= 1; dz++ )
+            for ( int dy = -1; dy <= 1; dy++ )
+                for ( int dx = -1; dx <= 1; dx++ )
+                {
+                    const int cx = c[ 0 ] + dx, cy = c[ 1 ] + dy, cz = c[ 2 ] + dz;
+                    if ( cx < 0 || cy < 0 || cz < 0 || cx >= dims[ 0 ] || cy >= dims[ 1 ] || cz >= dims[ 2 ] )
+                        continue;
+                    const uint64_t k = ( (uint64_t)cz * dims[ 1 ] + cy ) * dims[ 0 ] + cx;
+                    for ( uint32_t e = start[ k ]; e < start[ k + 1 ]; e++ )
+                    {
+                        const uint32_t i  = item[ e ];
+                        const double   ex = (double)x[ 0 ] - atoms[ 4 * i ], ey = (double)x[ 1 ] - atoms[ 4 * i + 1 ],
+                                     ez = (double)x[ 2 ] - atoms[ 4 * i + 2 ];
+                        const double d = sqrt( ex * ex + ey * ey + ez * ez ) - atoms[ 4 * i + 3 ];
+                        best           = d < best ? d : best;
+                    }
+                }
+        if ( best <= (double)band && best >= -(double)band )
+        {
+            out[ 3 * kept + 0 ] = x[ 0 ];
+            out[ 3 * kept + 1 ] = x[ 1 ];
+            out[ 3 * kept + 2 ] = x[ 2 ];
+            kept++;
+        }
+    }
+    free( start );
+    free( item );
+    free( cell );
+    return kept;
+}

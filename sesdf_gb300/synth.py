@@ -30,6 +30,9 @@ def _load():
         lib = ctypes.CDLL(path)
         lib.sesgb_synth_globule.argtypes = [ctypes.c_uint32, ctypes.c_uint64, ctypes.c_void_p]
         lib.sesgb_synth_globule.restype = ctypes.c_int
+        lib.sesgb_synth_queries.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64,
+                                            ctypes.c_float, ctypes.c_void_p]
+        lib.sesgb_synth_queries.restype = ctypes.c_uint32
         lib.sesgb_synth_assembly.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_uint64,
                                              ctypes.c_void_p]
         lib.sesgb_synth_shell.argtypes = [ctypes.c_uint32, ctypes.c_uint32, ctypes.c_uint64, ctypes.c_double,
@@ -83,6 +86,21 @@ def jitter(atoms: np.ndarray, sigma: float, seed: int) -> np.ndarray:
 def frames(count: int = 64, n: int = 20000, seed: int = 1400, sigma: float = 0.3):
     base = globule(n, seed)
     return [jitter(base, sigma, seed + f) for f in range(count)]
+
+
+def queries(atoms: np.ndarray, m: int, seed: int, band: float = 3.0) -> np.ndarray:
+    """m query points uniform in the atoms' bounding box, kept within `band` of the vdW surface (float32 [m, 3])."""
+    lib = _load()
+    a = np.ascontiguousarray(atoms, np.float32).reshape(-1, 4)
+    out = np.zeros((m, 3), np.float32)
+    got = lib.sesgb_synth_queries(a.ctypes.data, a.shape[0], m, seed, ctypes.c_float(band), out.ctypes.data)
+    return out[:got]
+
+
+def sdf_workload():
+    """20,000-atom globule (seed 1500) and 1,000,000 query points within 3 A of its vdW surface (seed 1501)."""
+    atoms = globule(20000, 1500)
+    return atoms, queries(atoms, 1_000_000, 1501)
 
 
 WORKLOADS = {
