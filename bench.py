@@ -270,6 +270,43 @@ def batch_extras(args, flush):
     return res
 
 
+def sdf_extra(flush):
+    """SDF forward and adjoint: 20,000-atom globule, 1M query points within 3 A of its vdW surface."""
+    import torch
+    from sesdf_gb300 import SesBuild, synth
+    atoms, q = synth.sdf_workload()
+    m = q.shape[0]
+    stream = torch.cuda.current_stream()
+    g = SesBuild(atoms, RP, "full")
+    g.build()
+    dq = torch.from_numpy(q).cuda()
+    out = torch.empty(m, dtype=torch.float32, device="cuda")
+    gs = torch.ones(m, dtype=torch.float32, device="cuda")
+    ga = torch.empty((atoms.shape[0], 4), dtype=torch.float32, device="cuda")
+    res = {}
+    for name, fn in (("forward", lambda: g.sdf(dq.data_ptr(), m, out.data_ptr(), None, stream.cuda_stream)),
+                     ("backward", lambda: g.sdf_backward(dq.data_ptr(), m, gs.data_ptr(), ga.data_ptr(),
+                                                         stream.cuda_stream))):
+        for _ in range(3):
+            fn()
+        ms = []
+        for _ in range(10):
+            flush.zero_()
+            t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            t0.record(stream)
+            fn()
+            t1.record(stream)
+            torch.cuda.synchronize()
+            ms.append(t0.elapsed_time(t1))
+        res[f"{name}_ms"] = round(float(np.median(ms)), 4)
+        res[f"{name}_queries_per_s"] = round(m / (float(np.median(ms)) * 1e-3), 1)
+    res["queries"] = int(m)
+    res["atoms"] = int(atoms.shape[0])
+    res["band_A"] = 3.0
+    g.close()
+    return res
+
+
 def profiled_traffic(kernel: str):
     """DRAM bytes per launch of `kernel` from its committed ncu summary (profiles/), or None."""
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles", f"{kernel}_assembly100k.txt")
@@ -370,6 +407,7 @@ def run_ours(args, rank, world, local):
             gs.close()
         del shell
         extra.update(batch_extras(args, flush))
+        extra["sdf_20k_1m"] = sdf_extra(flush)
 
     roof = roofline(stages, counts, nbr, n)
     line = {

@@ -38,8 +38,10 @@ struct sesgb_ctx
     std::vector<uint32_t> molCells;
     uint32_t *            hMol = nullptr; // pinned copy of Build::molCounts
 
-    // SDF queries: gradient scratch in sorted atom order
+    // SDF queries: gradient scratch in sorted atom order, query-order scratch (grow-only)
     float * gradSorted = nullptr;
+    void *  sdfScratch = nullptr;
+    size_t  sdfScratchBytes = 0;
 
     Build          b {};
     DeviceCounts * hCounts = nullptr;
@@ -791,14 +793,32 @@ extern "C"
             cudaFreeHost( c->hMol );
         if ( c->gradSorted )
             cudaFree( c->gradSorted );
+        if ( c->sdfScratch )
+            cudaFree( c->sdfScratch );
         delete c;
     }
 
     // ---- signed distance at query points ---------------------------------------
-    static int sdf_prepare( sesgb_ctx * c, cudaStream_t s )
+    static int sdf_prepare( sesgb_ctx * c, uint32_t m, cudaStream_t s )
     {
         if ( !c->built )
             return SESGB_ERR_NOT_BUILT;
+        const size_t need = sdf_scratch_bytes( m );
+        if ( need > c->sdfScratchBytes )
+        {
+            if ( c->sdfScratch )
+            {
+                cudaStreamSynchronize( s );
+                cudaFree( c->sdfScratch );
+                c->sdfScratch = nullptr;
+            }
+            if ( !cuda_ok( c, cudaMalloc( &c->sdfScratch, need ), "cudaMalloc" ) )
+            {
+                c->sdfScratchBytes = 0;
+                return SESGB_ERR_CUDA;
+            }
+            c->sdfScratchBytes = need;
+        }
         if ( c->mode != SESGB_MODE_FULL || c->nMol != 1 )
         {
             c->err = "the SDF needs a full-surface build of one molecule";
@@ -815,10 +835,10 @@ extern "C"
         if ( !c || ( m && ( !device_queries || !device_sdf ) ) )
             return SESGB_ERR_INVALID;
         cudaStream_t s  = static_cast<cudaStream_t>( stream );
-        int          st = sdf_prepare( c, s );
+        int          st = sdf_prepare( c, m, s );
         if ( st != SESGB_OK )
             return st;
-        launch_sdf( c->b, device_queries, m, SESGB_SDF_BAND, device_sdf, device_kind, s );
+        launch_sdf( c->b, device_queries, m, SESGB_SDF_BAND, device_sdf, device_kind, c->sdfScratch, s );
         return cuda_ok( c, cudaGetLastError(), "sdf" ) ? SESGB_OK : SESGB_ERR_CUDA;
     }
 
@@ -828,12 +848,13 @@ extern "C"
         if ( !c || !device_grad_atoms || ( m && ( !device_queries || !device_grad_sdf ) ) )
             return SESGB_ERR_INVALID;
         cudaStream_t s  = static_cast<cudaStream_t>( stream );
-        int          st = sdf_prepare( c, s );
+        int          st = sdf_prepare( c, m, s );
         if ( st != SESGB_OK )
             return st;
         if ( !c->gradSorted && !cuda_ok( c, cudaMalloc( &c->gradSorted, sizeof( float ) * 4 * std::max<size_t>( c->n, 1 ) ), "cudaMalloc" ) )
             return SESGB_ERR_CUDA;
-        launch_sdf_backward( c->b, device_queries, m, SESGB_SDF_BAND, device_grad_sdf, c->gradSorted, device_grad_atoms, s );
+        launch_sdf_backward( c->b, device_queries, m, SESGB_SDF_BAND, device_grad_sdf, c->gradSorted, device_grad_atoms,
+                             c->sdfScratch, s );
         return cuda_ok( c, cudaGetLastError(), "sdf backward" ) ? SESGB_OK : SESGB_ERR_CUDA;
     }
 

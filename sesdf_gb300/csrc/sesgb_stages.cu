@@ -2332,15 +2332,85 @@ namespace sesgb
                 return hit;
             }
             __syncwarp();
-            warp_bitonic_sort<unsigned long long>( sm.key, nl, kSdfList, ~0ull );
             float best  = T;
             hit.kind    = kSdfClampInside;
+            // x lies in a SAS sphere with R - |x - c| = -smin: every point of dE is at least that far
+            const float floorD = -smin;
+            if ( !( floorD < T ) )
+            {
+                hit.value = b.rp - T;
+                return hit;
+            }
+            // probes (vertices of dE, never hidden) first: an early upper bound for the search
+            {
+                float  cand = 3.4e38f;
+                int    pa = -1, pb = -1, pc = -1;
+                float3 pq = x;
+                for ( uint32_t e0 = 0; e0 < nl; e0++ )
+                {
+                    const uint32_t i     = (uint32_t)sm.key[ e0 ];
+                    const uint32_t chunk = b.chunkStart[ i ], len = b.chunkLen[ i ];
+                    for ( uint32_t e = lane; e < len; e += 32 )
+                    {
+                        const int4 cid = b.stageCid[ chunk + e ];
+                        if ( cid.w == 0 )
+                            continue;
+                        const float4 p    = b.stagePos[ chunk + e ];
+                        const float  dist = sqrtf( ( x.x - p.x ) * ( x.x - p.x ) + ( x.y - p.y ) * ( x.y - p.y ) + ( x.z - p.z ) * ( x.z - p.z ) );
+                        if ( dist < cand )
+                        {
+                            const int4 ids = b.stageIds[ chunk + e ];
+                            cand           = dist;
+                            pa             = ids.x;
+                            pb             = ids.y;
+                            pc             = ids.z;
+                            pq             = make_float3( p.x, p.y, p.z );
+                        }
+                    }
+                }
+                float wbest = cand;
+                int   owner = (int)lane;
+                warp_min_hit( wbest, owner );
+                if ( wbest < best )
+                {
+                    best     = wbest;
+                    hit.kind = kSdfProbe;
+                    hit.a    = __shfl_sync( 0xffffffffu, pa, owner );
+                    hit.b    = __shfl_sync( 0xffffffffu, pb, owner );
+                    hit.c    = __shfl_sync( 0xffffffffu, pc, owner );
+                    hit.q.x  = __shfl_sync( 0xffffffffu, pq.x, owner );
+                    hit.q.y  = __shfl_sync( 0xffffffffu, pq.y, owner );
+                    hit.q.z  = __shfl_sync( 0xffffffffu, pq.z, owner );
+                }
+            }
+            // atoms in ascending |x - c| - R order (the lower bound of all their candidates),
+            // each picked by a warp minimum over the ones left, until the bound reaches best
             for ( uint32_t t = 0; t < nl; t++ )
             {
-                const unsigned long long key = sm.key[ t ];
-                const float              dl  = __uint_as_float( (uint32_t)( key >> 32 ) );
-                if ( !( dl < best ) )
-                    break; // every candidate of this and later atoms is at least dl away
+                unsigned long long key = ~0ull;
+                uint32_t           at  = 0;
+                for ( uint32_t e = lane; e < nl; e += 32 )
+                    if ( sm.key[ e ] < key )
+                    {
+                        key = sm.key[ e ];
+                        at  = e;
+                    }
+                for ( int o = 16; o > 0; o >>= 1 )
+                {
+                    const unsigned long long ok = __shfl_xor_sync( 0xffffffffu, key, o );
+                    const uint32_t           oa = __shfl_xor_sync( 0xffffffffu, at, o );
+                    if ( ok < key )
+                    {
+                        key = ok;
+                        at  = oa;
+                    }
+                }
+                const float dl = __uint_as_float( (uint32_t)( key >> 32 ) );
+                if ( !( dl < best ) || !( floorD < best ) )
+                    break; // every candidate of this and the remaining atoms is at least dl away
+                __syncwarp();
+                if ( lane == 0 )
+                    sm.key[ at ] = ~0ull; // taken
                 const uint32_t i   = (uint32_t)key;
                 const float4   ci  = b.atoms[ i ];
                 const float    Ri  = ci.w + b.rp;
@@ -2431,27 +2501,6 @@ namespace sesgb
                     ck   = kSdfCircle;
                     cb   = (int)b.nbr[ row + s ];
                     cq   = q;
-                }
-                // probes owned by i (the smallest atom of their triplet)
-                {
-                    const uint32_t chunk = b.chunkStart[ i ], len = b.chunkLen[ i ];
-                    for ( uint32_t e = lane; e < len; e += 32 )
-                    {
-                        const int4 cid = b.stageCid[ chunk + e ];
-                        if ( cid.w == 0 )
-                            continue;
-                        const float4 p    = b.stagePos[ chunk + e ];
-                        const float  dist = sqrtf( ( x.x - p.x ) * ( x.x - p.x ) + ( x.y - p.y ) * ( x.y - p.y ) + ( x.z - p.z ) * ( x.z - p.z ) );
-                        if ( dist < cand )
-                        {
-                            const int4 ids = b.stageIds[ chunk + e ];
-                            cand           = dist;
-                            ck             = kSdfProbe;
-                            cb             = ids.y;
-                            cc             = ids.z;
-                            cq             = make_float3( p.x, p.y, p.z );
-                        }
-                    }
                 }
                 float wbest = cand;
                 int   owner = (int)lane;
@@ -2553,16 +2602,29 @@ namespace sesgb
                           gs * 2.f * w[ k ] * R[ k ] );
         }
 
+        // grid cell of each query (sort key) and its index
+        __global__ void k_sdf_keys( Build b, const float * queries, uint32_t m, uint32_t * keys, uint32_t * order )
+        {
+            const FineGrid g = b.fine[ 0 ];
+            for ( uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < m; q += gridDim.x * blockDim.x )
+            {
+                keys[ q ]  = fine_key( g, fine_cell( g, queries[ 3 * (size_t)q ], queries[ 3 * (size_t)q + 1 ], queries[ 3 * (size_t)q + 2 ] ) );
+                order[ q ] = q;
+            }
+        }
+
         template<bool kBackward>
         __global__ void __launch_bounds__( 32 * kSdfWarps ) k_sdf( Build b, const float * queries, uint32_t m, float band,
                                                                    float * sdf, const float * gradSdf, float * gradSorted,
-                                                                   int * kind )
+                                                                   int * kind, const uint32_t * order )
         {
             __shared__ SdfSmem smem[ kSdfWarps ];
             const uint32_t     warp = threadIdx.x >> 5, lane = lane_id();
             uint32_t           overflow = 0;
-            for ( uint32_t qi = blockIdx.x * kSdfWarps + warp; qi < m; qi += gridDim.x * kSdfWarps )
+            // queries in grid-cell order: neighbouring warps read the same atoms
+            for ( uint32_t qs = blockIdx.x * kSdfWarps + warp; qs < m; qs += gridDim.x * kSdfWarps )
             {
+                const uint32_t qi = order[ qs ];
                 const float3 x = make_float3( queries[ 3 * (size_t)qi ], queries[ 3 * (size_t)qi + 1 ], queries[ 3 * (size_t)qi + 2 ] );
                 const SdfHit h = sdf_query( b, x, smem[ warp ], band, overflow );
                 if ( lane == 0 )
@@ -2592,22 +2654,40 @@ namespace sesgb
         }
     } // namespace
 
-    void launch_sdf( const Build & b, const float * queries, uint32_t m, float band, float * sdf, int * kind, cudaStream_t s )
+    size_t sdf_scratch_bytes( uint32_t m ) { return 2 * ( ( (size_t)m * 4 + 255 ) & ~(size_t)255 ) + radix_scratch_bytes( m ); }
+
+    // queries sorted by grid cell into `order` (scratch: sdf_scratch_bytes)
+    static const uint32_t * sdf_order( const Build & b, const float * queries, uint32_t m, void * scratch, cudaStream_t s )
+    {
+        char *     p     = static_cast<char *>( scratch );
+        uint32_t * keys  = reinterpret_cast<uint32_t *>( p );
+        uint32_t * order = reinterpret_cast<uint32_t *>( p + ( ( (size_t)m * 4 + 255 ) & ~(size_t)255 ) );
+        void *     rad   = p + 2 * ( ( (size_t)m * 4 + 255 ) & ~(size_t)255 );
+        k_sdf_keys<<<min( persistent_blocks( 256 ), blocks_for( m, 256 ) ), 256, 0, s>>>( b, queries, m, keys, order );
+        counted();
+        radix_sort( keys, order, m, 32, rad, s );
+        return order;
+    }
+
+    void launch_sdf( const Build & b, const float * queries, uint32_t m, float band, float * sdf, int * kind, void * scratch,
+                     cudaStream_t s )
     {
         if ( !m )
             return;
-        const uint32_t blocks = min( persistent_blocks( 32 * kSdfWarps ) * 2, ( m + kSdfWarps - 1 ) / kSdfWarps );
-        k_sdf<false><<<blocks, 32 * kSdfWarps, 0, s>>>( b, queries, m, band, sdf, nullptr, nullptr, kind );
+        const uint32_t * order  = sdf_order( b, queries, m, scratch, s );
+        const uint32_t   blocks = min( persistent_blocks( 32 * kSdfWarps ) * 2, ( m + kSdfWarps - 1 ) / kSdfWarps );
+        k_sdf<false><<<blocks, 32 * kSdfWarps, 0, s>>>( b, queries, m, band, sdf, nullptr, nullptr, kind, order );
         counted();
     }
     void launch_sdf_backward( const Build & b, const float * queries, uint32_t m, float band, const float * gradSdf,
-                              float * gradSorted, float * gradInput, cudaStream_t s )
+                              float * gradSorted, float * gradInput, void * scratch, cudaStream_t s )
     {
         cudaMemsetAsync( gradSorted, 0, sizeof( float ) * 4 * (size_t)b.n, s );
         if ( m )
         {
-            const uint32_t blocks = min( persistent_blocks( 32 * kSdfWarps ) * 2, ( m + kSdfWarps - 1 ) / kSdfWarps );
-            k_sdf<true><<<blocks, 32 * kSdfWarps, 0, s>>>( b, queries, m, band, nullptr, gradSdf, gradSorted, nullptr );
+            const uint32_t * order  = sdf_order( b, queries, m, scratch, s );
+            const uint32_t   blocks = min( persistent_blocks( 32 * kSdfWarps ) * 2, ( m + kSdfWarps - 1 ) / kSdfWarps );
+            k_sdf<true><<<blocks, 32 * kSdfWarps, 0, s>>>( b, queries, m, band, nullptr, gradSdf, gradSorted, nullptr, order );
             counted();
         }
         if ( b.n )

@@ -121,9 +121,11 @@ namespace sesgb
     void launch_batch_finish( const Build & b, cudaStream_t s );
     // signed distance to the SES at float3 query points (needs the atom grid of reach
     // rmax + 2 rp + band built by launch_fine_params + launch_cells first)
-    void launch_sdf( const Build & b, const float * queries, uint32_t m, float band, float * sdf, int * kind, cudaStream_t s );
-    void launch_sdf_backward( const Build & b, const float * queries, uint32_t m, float band, const float * gradSdf,
-                              float * gradSorted, float * gradInput, cudaStream_t s );
+    size_t sdf_scratch_bytes( uint32_t m );
+    void   launch_sdf( const Build & b, const float * queries, uint32_t m, float band, float * sdf, int * kind, void * scratch,
+                       cudaStream_t s );
+    void   launch_sdf_backward( const Build & b, const float * queries, uint32_t m, float band, const float * gradSdf,
+                                float * gradSorted, float * gradInput, void * scratch, cudaStream_t s );
     void launch_neighbors( const Build & b, cudaStream_t s );
     void launch_visibility( const Build & b, cudaStream_t s );
     void launch_visibility_resolve( const Build & b, cudaStream_t s );
