@@ -2211,7 +2211,8 @@ namespace sesgb
     namespace
     {
         constexpr int   kSdfWarps = 4;   // warps per block (one query per warp)
-        constexpr int   kSdfList  = 256; // atoms within reach held per query
+        constexpr int   kSdfList   = 256; // atoms within reach held per query
+        constexpr int   kSdfStaged = 128; // neighbour slots staged in shared memory
 
         enum SdfKind : int
         {
@@ -2233,9 +2234,20 @@ namespace sesgb
 
         struct SdfSmem
         {
-            unsigned long long key[ kSdfList ]; // (delta bits << 32) | atom
-            float4             nb[ 520 ];       // neighbourhood of the atom being examined: (c_k, R_k)
+            unsigned long long key[ kSdfList ];   // (delta bits << 32) | atom
+            float4             nb[ kSdfStaged ];   // neighbourhood of the atom being examined: (c_k, R_k)
+            uint16_t           near[ kNbrBuf ];    // its slots whose SAS sphere comes within the current best of x
+            uint8_t            vis[ kNbrBuf ];     // status of its circles
         };
+
+        // neighbour slot s of atom i as (c_k, R_k): staged slots from shared memory
+        __device__ __forceinline__ float4 sdf_nb( const Build & b, const SdfSmem & sm, size_t row, uint32_t s )
+        {
+            if ( s < (uint32_t)kSdfStaged )
+                return sm.nb[ s ];
+            const float4 c = b.atoms[ b.nbr[ row + s ] ];
+            return make_float4( c.x, c.y, c.z, c.w + b.rp );
+        }
 
         __device__ __forceinline__ void warp_min_hit( float & best, int & owner )
         {
@@ -2346,11 +2358,12 @@ namespace sesgb
                 float  cand = 3.4e38f;
                 int    pa = -1, pb = -1, pc = -1;
                 float3 pq = x;
-                for ( uint32_t e0 = 0; e0 < nl; e0++ )
+                // lane per atom: its probe chunk
+                for ( uint32_t e0 = lane; e0 < nl; e0 += 32 )
                 {
                     const uint32_t i     = (uint32_t)sm.key[ e0 ];
                     const uint32_t chunk = b.chunkStart[ i ], len = b.chunkLen[ i ];
-                    for ( uint32_t e = lane; e < len; e += 32 )
+                    for ( uint32_t e = 0; e < len; e++ )
                     {
                         const int4 cid = b.stageCid[ chunk + e ];
                         if ( cid.w == 0 )
@@ -2416,10 +2429,27 @@ namespace sesgb
                 const float    Ri  = ci.w + b.rp;
                 const uint32_t ni  = b.nbrCount[ i ];
                 const size_t   row = (size_t)i * b.cap;
-                for ( uint32_t s = lane; s < ni; s += 32 )
+                // stage N(i); a point q with |x - q| < best can only lie inside the SAS
+                // sphere of a neighbour k with |x - c_k| - R_k < best: those are the "near" ones
+                uint32_t nn = 0;
+                for ( uint32_t s0 = 0; s0 < ni; s0 += 32 )
                 {
-                    const float4 ck = b.atoms[ b.nbr[ row + s ] ];
-                    sm.nb[ s ]      = make_float4( ck.x, ck.y, ck.z, ck.w + b.rp );
+                    const uint32_t s    = s0 + lane;
+                    bool           near = false;
+                    if ( s < ni )
+                    {
+                        sm.vis[ s ]     = b.status[ row + s ];
+                        const float4 ck = b.atoms[ b.nbr[ row + s ] ];
+                        const float  Rk = ck.w + b.rp;
+                        if ( s < (uint32_t)kSdfStaged )
+                            sm.nb[ s ] = make_float4( ck.x, ck.y, ck.z, Rk );
+                        const float Lk  = sqrtf( ( x.x - ck.x ) * ( x.x - ck.x ) + ( x.y - ck.y ) * ( x.y - ck.y ) + ( x.z - ck.z ) * ( x.z - ck.z ) );
+                        near            = Lk - Rk < best;
+                    }
+                    const uint32_t mk = __ballot_sync( 0xffffffffu, near );
+                    if ( near )
+                        sm.near[ nn + __popc( mk & lanemask_lt() ) ] = (uint16_t)s;
+                    nn += __popc( mk );
                 }
                 __syncwarp();
                 // candidates of this atom, one per lane at most, reduced at the end
@@ -2434,9 +2464,9 @@ namespace sesgb
                     {
                         const float3 q = make_float3( ci.x + w.x * ( Ri / L ), ci.y + w.y * ( Ri / L ), ci.z + w.z * ( Ri / L ) );
                         bool         hidden = false;
-                        for ( uint32_t s = lane; s < ni; s += 32 )
+                        for ( uint32_t e = lane; e < nn; e += 32 )
                         {
-                            const float4 nk = sm.nb[ s ];
+                            const float4 nk = sdf_nb( b, sm, row, sm.near[ e ] );
                             const float  dx = q.x - nk.x, dy = q.y - nk.y, dz = q.z - nk.z;
                             hidden          = hidden || ( dx * dx + dy * dy + dz * dz < nk.w * nk.w );
                         }
@@ -2452,9 +2482,15 @@ namespace sesgb
                 for ( uint32_t s0 = 0; s0 < ni; s0 += 32 )
                 {
                     const uint32_t s = s0 + lane;
-                    if ( s >= ni || b.status[ row + s ] == 0 )
+                    if ( s >= ni || sm.vis[ s ] == 0 )
                         continue;
-                    const float4 nj = sm.nb[ s ];
+                    const float4 nj = sdf_nb( b, sm, row, s );
+                    {
+                        // every point of circle (i, j) is on sphere j too: |x - c_j| - R_j bounds it
+                        const float Lj = sqrtf( ( x.x - nj.x ) * ( x.x - nj.x ) + ( x.y - nj.y ) * ( x.y - nj.y ) + ( x.z - nj.z ) * ( x.z - nj.z ) );
+                        if ( !( fabsf( Lj - nj.w ) < best ) )
+                            continue;
+                    }
                     const float3 d  = make_float3( nj.x - ci.x, nj.y - ci.y, nj.z - ci.z );
                     const float  dd = d.x * d.x + d.y * d.y + d.z * d.z;
                     const float  tt = ( Ri * Ri - nj.w * nj.w + dd ) / ( 2.f * dd );
@@ -2478,11 +2514,12 @@ namespace sesgb
                         if ( !( dist < cand ) || !( dist < best ) )
                             continue;
                         bool hidden = false;
-                        for ( uint32_t k = 0; k < ni && !hidden; k++ )
+                        for ( uint32_t e = 0; e < nn && !hidden; e++ )
                         {
+                            const uint32_t k = sm.near[ e ];
                             if ( k == s )
                                 continue;
-                            const float4 nk = sm.nb[ k ];
+                            const float4 nk = sdf_nb( b, sm, row, k );
                             const float  dx = q.x - nk.x, dy = q.y - nk.y, dz = q.z - nk.z;
                             hidden          = dx * dx + dy * dy + dz * dz < nk.w * nk.w;
                         }
@@ -2614,7 +2651,7 @@ namespace sesgb
         }
 
         template<bool kBackward>
-        __global__ void __launch_bounds__( 32 * kSdfWarps ) k_sdf( Build b, const float * queries, uint32_t m, float band,
+        __global__ void __launch_bounds__( 32 * kSdfWarps, 8 ) k_sdf( Build b, const float * queries, uint32_t m, float band,
                                                                    float * sdf, const float * gradSdf, float * gradSorted,
                                                                    int * kind, const uint32_t * order )
         {
