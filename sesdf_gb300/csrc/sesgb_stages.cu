@@ -1050,22 +1050,26 @@ namespace sesgb
         {
             const float4 qj = m.rel[ sj ], qk = m.rel[ sk ];
             const f3     dj = F3( qj.x, qj.y, qj.z ), dk = F3( qk.x, qk.y, qk.z );
+            // approximate reciprocals and roots (a few ulps) are well inside the kSolve error scale
             const float  dJ = dot( dj, dj ), dK = dot( dk, dk );
-            const f3     cJ = dj * ( qj.w / dJ ); // (R_i^2 - R_j^2 + |d_j|^2) / (2 |d_j|^2) = K_j / |d_j|^2
-            const f3     cK = dk * ( qk.w / dK );
-            const f3     nJ = dj * rsqrtf( dJ );
-            const f3     nK = dk * rsqrtf( dK );
+            const float  rJ = rsqrtf( dJ ), rK = rsqrtf( dK );
+            const f3     cJ = dj * ( qj.w * rJ * rJ ); // (R_i^2 - R_j^2 + |d_j|^2) / (2 |d_j|^2) = K_j / |d_j|^2
+            const f3     cK = dk * ( qk.w * rK * rK );
+            const f3     nJ = dj * rJ;
+            const f3     nK = dk * rK;
             const f3     u  = nK - nJ * dot( nK, nJ );
             const float  den = dot( u, nK ); // sin^2 of the angle between the circle axes
             w[ 0 ] = w[ 1 ] = 0;
             band            = !( den > 1e-3f );
             if ( band )
                 return;
-            const f3    xc = cJ + u * ( dot( cK - cJ, nK ) / den );
-            const float xn = sqrtf( dot( xc, xc ) );
-            const float ex = kSolve * ( Ri + xn ) * ( 1.f + 1.f / den );
-            const float tt = Ri * Ri - xn * xn;
-            const float et = 2.f * ( xn + ex ) * ex + kSolve * Ri * Ri;
+            const float iden = __fdividef( 1.f, den );
+            const f3    xc   = cJ + u * ( dot( cK - cJ, nK ) * iden );
+            const float x2   = dot( xc, xc );
+            const float xn   = x2 > 0.f ? x2 * rsqrtf( x2 ) : 0.f;
+            const float ex   = kSolve * ( Ri + xn ) * ( 1.f + iden );
+            const float tt   = Ri * Ri - x2;
+            const float et   = 2.f * ( xn + ex ) * ex + kSolve * Ri * Ri;
             if ( tt < -et )
                 return; // no point
             if ( !( tt > et ) )
@@ -1073,9 +1077,10 @@ namespace sesgb
                 band = true;
                 return;
             }
-            const float root = sqrtf( tt );
+            const float rt   = rsqrtf( tt );
+            const float root = tt * rt;
             const f3    nn   = normalize( cross( nJ, nK ) );
-            const float ep   = ex + et / ( 2.f * root ) + root * kSolve / sqrtf( den );
+            const float ep   = ex + 0.5f * et * rt + root * kSolve * rsqrtf( den );
             // x1,2 = xc +- root nn lie within ep of the exact points: a plane test
             // moves by at most ep |d_l|, rounding by at most eK
             const float eh = ep * pb.dmax + pb.eK;
@@ -1365,6 +1370,37 @@ namespace sesgb
                 fillHere += __popc( __ballot_sync( 0xffffffffu, fill ) );
                 bandHere += __popc( __ballot_sync( 0xffffffffu, band ) );
             }
+            // slot of k in N(j) for every kept entry, found by the whole warp (one coalesced
+            // pass over the row instead of a binary search per lane)
+            uint16_t * sjkS = reinterpret_cast<uint16_t *>( m.cand ); // free after the screening (2 kCandBuf slots)
+            for ( uint32_t e = 0; e < kept && fits; e++ )
+            {
+                const uint32_t ex = m.ent[ e ].x;
+                if ( e > 0 && m.ent[ e - 1 ].x == ex )
+                {
+                    if ( lane == 0 )
+                        sjkS[ e ] = sjkS[ e - 1 ]; // second side of the same candidate
+                    __syncwarp();
+                    continue;
+                }
+                const uint32_t j = m.nid[ ex & 0xffffu ], k = m.nid[ ex >> 16 ];
+                const uint32_t nj = b.nbrCount[ j ];
+                uint32_t       pos = 0;
+                for ( uint32_t base = 0; base < nj; base += 32 )
+                {
+                    const uint32_t s  = base + lane;
+                    const uint32_t mk = __ballot_sync( 0xffffffffu, s < nj && b.nbr[ (size_t)j * b.cap + s ] == k );
+                    if ( mk )
+                    {
+                        pos = base + (uint32_t)( __ffs( mk ) - 1 );
+                        break;
+                    }
+                }
+                if ( lane == 0 )
+                    sjkS[ e ] = (uint16_t)pos;
+                __syncwarp();
+            }
+            __syncwarp();
             uint32_t jbase = 0, gbase = 0;
             if ( lane == 0 && fillHere )
                 jbase = atomicAdd( &b.counts->jobs, fillHere );
@@ -1384,7 +1420,7 @@ namespace sesgb
                     const uint32_t side = en.y & 1u, kind = ( en.y >> 1 ) & 1u;
                     const int      wv   = (int)( en.y >> 2 ) - 4;
                     const uint32_t j = m.nid[ sj ], k = m.nid[ sk ];
-                    const uint32_t sjk  = (uint32_t)find_in_row( b.nbr + (size_t)j * b.cap, b.nbrCount[ j ], k );
+                    const uint32_t sjk  = sjkS[ q ];
                     int4           cid;
                     if ( b.mode == 0 )
                         cid = make_int4( (int)b.slotTrim[ row + sj ], (int)b.slotTrim[ (size_t)j * b.cap + sjk ],
