@@ -248,25 +248,31 @@ def time_batched(mols, mode, repeats, flush, cap, graph):
     return out, c
 
 
-def batch_extras(args, flush):
-    """Batched builds (256 molecules of log-uniform size; 64 jittered frames) against the plain loop."""
+def batch_extras(args, flush, rank=0, world=1):
+    """Batched builds (256 molecules of log-uniform size; 64 jittered frames) against the plain loop.
+    With several ranks each builds its contiguous share of the molecules (balanced by atoms); the
+    slowest rank sets the time."""
     from sesdf_gb300 import synth
     from sesdf_gb300.autotune import tune_batch
+    from sesdf_gb300.partition import split_by_atoms
     res = {}
     sizes = synth.batch_sizes()
     sets = {"batch256_mixed": [synth.globule(int(n), 1300 + m) for m, n in enumerate(sizes)],
             "batch64_frames": synth.frames()}
-    for name, mols in sets.items():
+    for name, all_mols in sets.items():
+        a, b = split_by_atoms([m.shape[0] for m in all_mols], world)[rank]
+        mols = all_mols[a:b] if b > a else all_mols[:1]
         tuned = tune_batch(mols, RP, "full")
         bm, c = time_batched(mols, "full", 5, flush, tuned["max_neighbor_per_atom"], tuned["graph"])
         pm = time_plain_loop(mols, "full", 3, flush)
-        atoms = int(sum(m.shape[0] for m in mols))
-        res[name] = {"molecules": len(mols), "atoms": atoms, "batched_ms": round(float(np.median(bm)), 3),
-                     "plain_loop_ms": round(float(np.median(pm)), 3),
-                     "speedup": round(float(np.median(pm)) / float(np.median(bm)), 2),
-                     "batched_atoms_per_s": round(atoms / (float(np.median(bm)) * 1e-3), 1),
+        bmed = max_over_ranks(float(np.median(bm)), world)
+        pmed = max_over_ranks(float(np.median(pm)), world)
+        atoms = int(sum(m.shape[0] for m in all_mols))
+        res[name] = {"molecules": len(all_mols), "atoms": atoms, "batched_ms": round(bmed, 3),
+                     "plain_loop_ms": round(pmed, 3), "speedup": round(pmed / bmed, 2),
+                     "batched_atoms_per_s": round(atoms / (bmed * 1e-3), 1),
                      "tuned": {k: tuned[k] for k in ("max_neighbor_per_atom", "graph", "max_neighbors")},
-                     "probes": c["probes"]}
+                     "probes_rank0": c["probes"], "split": "molecules by atoms over ranks" if world > 1 else None}
     return res
 
 
@@ -406,7 +412,7 @@ def run_ours(args, rank, world, local):
                                    "probes": c["probes"], "fp64_decisions": c["fp64_decisions"]}
             gs.close()
         del shell
-        extra.update(batch_extras(args, flush))
+        extra.update(batch_extras(args, flush, rank, world))
         extra["sdf_20k_1m"] = sdf_extra(flush)
 
     roof = roofline(stages, counts, nbr, n)
