@@ -149,10 +149,14 @@ def aabb(atoms: np.ndarray) -> np.ndarray:
 
 
 class SesBuild:
-    """One SES build context (bcs::Sesdf for mode "full", bcs::Ssesdf for "exterior")."""
+    """One SES build context (bcs::Sesdf for mode "full", bcs::Ssesdf for "exterior").
+
+    graph=True (default) captures the build's fixed launch sequence in a CUDA graph after
+    the first build and replays it (SESGB_FLAG_GRAPH); profile=True records per-stage
+    events, also inside the graph."""
 
     def __init__(self, atoms: np.ndarray, probe_radius: float = 1.4, mode: str = "full", box=None,
-                 max_neighbor_per_atom: int = 0, max_intersections_per_circle: int = 0, graph: bool = False,
+                 max_neighbor_per_atom: int = 0, max_intersections_per_circle: int = 0, graph: bool = True,
                  device: int = -1, profile: bool = False):
         self._lib = load_library()
         self.atoms = np.ascontiguousarray(np.asarray(atoms, np.float32).reshape(-1, 4))
@@ -305,7 +309,7 @@ class SesBatch(SesBuild):
     the whole batch, molecule m's slice equal to its own SesBuild."""
 
     def __init__(self, molecules, probe_radius: float = 1.4, mode: str = "full", max_neighbor_per_atom: int = 0,
-                 max_intersections_per_circle: int = 0, graph: bool = False, device: int = -1, profile: bool = False):
+                 max_intersections_per_circle: int = 0, graph: bool = True, device: int = -1, profile: bool = False):
         self._lib = load_library()
         mols = [np.ascontiguousarray(np.asarray(m, np.float32).reshape(-1, 4)) for m in molecules]
         self.starts = np.zeros(len(mols) + 1, np.uint32)

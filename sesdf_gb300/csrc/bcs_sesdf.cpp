@@ -44,6 +44,7 @@ namespace bcs
             box( aabb, b );
             o.max_neighbor_per_atom = cap;
             o.device                = -1;
+            o.flags                 = SESGB_FLAG_GRAPH; // rebuilds replay the captured launch sequence
             status = sesgb_create( reinterpret_cast<const float *>( molecule.ptr ), (uint32_t)molecule.size, b, probeRadius, mode,
                                    &o, &ctx );
             return ctx;

@@ -64,6 +64,7 @@ struct sesgb_ctx
     // graph replay
     cudaGraph_t     graph = nullptr;
     cudaGraphExec_t graphExec = nullptr;
+    uint32_t        graphKernels = 0; // kernel launches in one replay
     bool            lastUsedGraph = false;
 
     // build in flight (sesgb_build_async .. sesgb_finish)
@@ -272,15 +273,16 @@ namespace
                                    "probe_jobs", "place",     "segments",   "probe_neighbors", "tori" };
 
     // all launches of one build; no host synchronisation inside
-    void enqueue( sesgb_ctx * c, cudaStream_t s, bool profile )
+    void enqueue( sesgb_ctx * c, cudaStream_t s, bool profile, bool capturing = false )
     {
         Build &     b    = c->b;
         const auto  n    = c->n;
         void *      sc   = c->scanScratch;
         DeviceCounts * d = b.counts;
         auto mark = [ & ]( int k ) {
+            // in a capture, an external record node keeps the event observable after replays
             if ( profile )
-                cudaEventRecord( c->ev[ k ], s );
+                cudaEventRecordWithFlags( c->ev[ k ], s, capturing ? cudaEventRecordExternal : cudaEventRecordDefault );
         };
         cudaMemsetAsync( d, 0, sizeof( DeviceCounts ), s );
         if ( n == 0 )
@@ -408,16 +410,23 @@ namespace
         c->pendingUpload = upload;
         c->pendingAtoms  = deviceAtoms;
         const bool useGraph = ( c->flags & SESGB_FLAG_GRAPH ) && c->built;
-        c->lastUsedGraph    = useGraph;
+        const bool profile  = ( c->flags & SESGB_FLAG_PROFILE ) && c->n;
+        if ( profile && !c->ev[ 0 ] )
+            for ( auto & e : c->ev )
+                cudaEventCreate( &e );
+        c->lastUsedGraph = useGraph;
         if ( useGraph )
         {
+            bool replayed = true;
             if ( !c->graphExec )
             {
+                replayed = false; // the capture counted this build's kernels already
+                const uint64_t l0 = launch_count();
                 cudaStream_t cap;
                 if ( !cuda_ok( c, cudaStreamCreateWithFlags( &cap, cudaStreamNonBlocking ), "stream" ) )
                     return SESGB_ERR_CUDA;
                 cudaStreamBeginCapture( cap, cudaStreamCaptureModeThreadLocal );
-                enqueue( c, cap, false );
+                enqueue( c, cap, profile, true ); // stage events become event-record nodes of the graph
                 cudaMemcpyAsync( c->hCounts, c->b.counts, sizeof( DeviceCounts ), cudaMemcpyDeviceToHost, cap );
                 if ( c->nMol > 1 )
                     cudaMemcpyAsync( c->hMol, c->b.molCounts, sizeof( uint32_t ) * c->nMol * kMolFields, cudaMemcpyDeviceToHost, cap );
@@ -427,17 +436,16 @@ namespace
                     return SESGB_ERR_CUDA;
                 if ( !cuda_ok( c, cudaGraphInstantiate( &c->graphExec, c->graph, 0 ), "instantiate" ) )
                     return SESGB_ERR_CUDA;
+                c->graphKernels = (uint32_t)( launch_count() - l0 );
             }
+            if ( replayed )
+                count_launches( c->graphKernels );
             if ( !cuda_ok( c, cudaGraphLaunch( c->graphExec, s ), "graph launch" ) )
                 return SESGB_ERR_CUDA;
-            c->profiled = false;
+            c->profiled = profile;
         }
         else
         {
-            const bool profile = ( c->flags & SESGB_FLAG_PROFILE ) && c->n;
-            if ( profile && !c->ev[ 0 ] )
-                for ( auto & e : c->ev )
-                    cudaEventCreate( &e );
             enqueue( c, s, profile );
             cudaMemcpyAsync( c->hCounts, c->b.counts, sizeof( DeviceCounts ), cudaMemcpyDeviceToHost, s );
             if ( c->nMol > 1 )

@@ -158,3 +158,23 @@ def test_set_atoms_moves_surface():
         out = g.fetch()
     o = oracle.run(moved, RP, "full", box=g.box)
     compare(moved, out, o, "full")
+
+
+def test_profiled_graph_stage_times():
+    # stage events recorded inside the replayed graph add up to the build
+    import torch
+    atoms = synth.globule(5000, 79)
+    with SesBuild(atoms, RP, "full", graph=True, profile=True) as g:
+        d = torch.from_numpy(atoms).cuda()
+        s = torch.cuda.current_stream()
+        for _ in range(3):
+            t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            t0.record(s)
+            g.build_async(d.data_ptr(), s.cuda_stream)
+            t1.record(s)
+            g.finish()
+        torch.cuda.synchronize()
+        st = g.stage_times()
+        total = t0.elapsed_time(t1)
+    assert all(v >= 0 for v in st.values())
+    assert 0.5 * total <= sum(st.values()) <= 1.01 * total + 0.05
