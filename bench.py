@@ -313,17 +313,23 @@ def sdf_extra(flush):
     return res
 
 
-def profiled_traffic(kernel: str):
-    """DRAM bytes per launch of `kernel` from its committed ncu summary (profiles/), or None."""
+def profiled(kernel: str) -> dict:
+    """From the kernel's committed ncu summary (profiles/<kernel>_assembly100k.txt): DRAM bytes per launch
+    and the issue-slot, ALU-pipe and FMA-pipe utilisations of the same capture (fractions)."""
     path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles", f"{kernel}_assembly100k.txt")
+    out = {}
+    keys = {"dram_bytes_per_launch:": "traffic", "issue active %": "issue_active", "ALU pipe %": "alu_pipe",
+            "FMA pipe %": "fma_pipe", "threads per instruction": "threads_per_instruction"}
     try:
         with open(path) as f:
             for line in f:
-                if line.startswith("dram_bytes_per_launch:"):
-                    return int(line.split(":", 1)[1].strip())
-    except OSError:
+                for k, name in keys.items():
+                    if line.startswith(k):
+                        v = float(line[len(k):].split()[0])
+                        out[name] = int(v) if name == "traffic" else (round(v / 100, 3) if "%" in k else v)
+    except (OSError, ValueError):
         pass
-    return None
+    return out
 
 
 def roofline(stages, counts, nbr, n_atoms):
@@ -343,8 +349,10 @@ def roofline(stages, counts, nbr, n_atoms):
         bytes_alg = 21.0 * P + 32.0 * n_atoms  # neighbour ids + neighbour atoms + status + per-atom I/O
         flops_alg = 30.0 * float(np.sum(nb * np.maximum(nb - 1, 0)))  # one circle-vs-atom test
     achieved = bytes_alg / (ms * 1e-3) / 1e9
+    prof = profiled(kernel)
     return {"kernel": kernel, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-            "frac": round(achieved / hbm, 4), "traffic": profiled_traffic(kernel), "peak_source": src,
+            "frac": round(achieved / hbm, 4), "traffic": prof.get("traffic"), "peak_source": src,
+            "issue": {k: v for k, v in prof.items() if k != "traffic"},
             "ms_per_launch": round(ms, 4), "bytes_per_launch": bytes_alg,
             "alu": {"flops_per_launch": flops_alg, "achieved_tflops": round(flops_alg / (ms * 1e-3) / 1e12, 2),
                     "fp32_nominal_tflops": round(fp32_peak, 1),
