@@ -708,17 +708,17 @@ namespace sesgb
         }
 
         // statuses (0 buried, 1 partial, 2 complete; circles not evaluated 0) and
-        // the per-atom counts, warp per atom
+        // the per-atom counts; four atoms per warp, eight lanes per atom
         __global__ void __launch_bounds__( 32 * kWarpsPerBlock ) k_visibility_final( Build b )
         {
             const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
-            const uint32_t i    = blockIdx.x * kWarpsPerBlock + warp;
-            if ( i >= b.n )
-                return;
-            const uint32_t ni  = b.nbrCount[ i ];
-            const size_t   row = (size_t)i * b.cap;
+            const uint32_t grp = lane / 8, gl = lane % 8;
+            const uint32_t i    = ( blockIdx.x * kWarpsPerBlock + warp ) * 4 + grp;
+            const bool     live = i < b.n;
+            const uint32_t ni   = live ? b.nbrCount[ i ] : 0u;
+            const size_t   row  = (size_t)i * b.cap;
             uint32_t       vis = 0, part = 0, full = 0;
-            for ( uint32_t s = lane; s < ni; s += 32 )
+            for ( uint32_t s = gl; s < ni; s += 8 )
             {
                 const uint32_t j  = b.nbr[ row + s ];
                 const uint32_t r  = b.status[ row + s ];
@@ -728,13 +728,13 @@ namespace sesgb
                 part += ( st == 1 && i < j );
                 full += ( st == 2 && i < j );
             }
-            for ( int o = 16; o > 0; o >>= 1 )
+            for ( int o = 4; o > 0; o >>= 1 )
             {
                 vis += __shfl_xor_sync( 0xffffffffu, vis, o );
                 part += __shfl_xor_sync( 0xffffffffu, part, o );
                 full += __shfl_xor_sync( 0xffffffffu, full, o );
             }
-            if ( lane == 0 )
+            if ( live && gl == 0 )
             {
                 b.visCnt[ i ]  = vis;
                 b.partCnt[ i ] = part;
@@ -767,21 +767,29 @@ namespace sesgb
             return make_float4( cicj.x, cicj.y, cicj.z, acosf( c ) );
         }
 
+        // four atoms per warp, eight lanes per atom (neighbour rows of ~35 slots fill the lanes)
+        constexpr uint32_t kEmitGroup = 8;
+
         __global__ void __launch_bounds__( 32 * kWarpsPerBlock ) k_emit( Build b )
         {
             const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
-            const uint32_t i    = blockIdx.x * kWarpsPerBlock + warp;
-            if ( i >= b.n )
-                return;
-            const uint32_t ni       = b.nbrCount[ i ];
-            const float4   ai       = b.atoms[ i ];
-            uint32_t       visBase  = b.visOff[ i ];
-            uint32_t       partBase = b.partOff[ i ];
-            uint32_t       fullBase = b.fullOff[ i ];
-            uint32_t       ovf      = 0;
-            for ( uint32_t base = 0; base < ni; base += 32 )
+            const uint32_t grp = lane / kEmitGroup, gl = lane % kEmitGroup;
+            const uint32_t gmask = ( ( 1u << kEmitGroup ) - 1u ) << ( grp * kEmitGroup );
+            const uint32_t i     = ( blockIdx.x * kWarpsPerBlock + warp ) * ( 32 / kEmitGroup ) + grp;
+            const bool     live  = i < b.n;
+            const uint32_t ni    = live ? b.nbrCount[ i ] : 0u;
+            const float4   ai    = live ? b.atoms[ i ] : make_float4( 0.f, 0.f, 0.f, 0.f );
+            uint32_t       visBase  = live ? b.visOff[ i ] : 0u;
+            uint32_t       partBase = live ? b.partOff[ i ] : 0u;
+            uint32_t       fullBase = live ? b.fullOff[ i ] : 0u;
+            uint32_t       most     = ni;
+            for ( int o = 16; o > 0; o >>= 1 )
+                most = max( most, __shfl_xor_sync( 0xffffffffu, most, o ) );
+            uint32_t       ovf = 0;
+            const uint32_t lt  = lanemask_lt() & gmask;
+            for ( uint32_t base = 0; base < most; base += kEmitGroup )
             {
-                const uint32_t s     = base + lane;
+                const uint32_t s     = base + gl;
                 const bool     valid = s < ni;
                 const size_t   slot  = (size_t)i * b.cap + s;
                 uint32_t       j     = 0;
@@ -794,10 +802,9 @@ namespace sesgb
                 const bool     vis  = valid && st != 0;
                 const bool     part = valid && st == 1 && i < j;
                 const bool     full = valid && st == 2 && i < j;
-                const uint32_t mv   = __ballot_sync( 0xffffffffu, vis );
-                const uint32_t mp   = __ballot_sync( 0xffffffffu, part );
-                const uint32_t mf   = __ballot_sync( 0xffffffffu, full );
-                const uint32_t lt   = lanemask_lt();
+                const uint32_t mv   = __ballot_sync( 0xffffffffu, vis ) & gmask;
+                const uint32_t mp   = __ballot_sync( 0xffffffffu, part ) & gmask;
+                const uint32_t mf   = __ballot_sync( 0xffffffffu, full ) & gmask;
                 if ( valid )
                     b.slotTrim[ slot ] = partBase + __popc( mp & lt );
                 if ( vis && b.mode == 0 )
@@ -828,7 +835,7 @@ namespace sesgb
                 partBase += __popc( mp );
                 fullBase += __popc( mf );
             }
-            if ( lane == 0 && b.mode == 0 )
+            if ( live && gl == 0 && b.mode == 0 )
                 b.convex[ i ] = make_uint2( b.visOff[ i ], b.visOff[ i ] + b.visCnt[ i ] );
             if ( ovf )
                 atomicOr( &b.counts->overflow, ovf );
@@ -2139,14 +2146,14 @@ namespace sesgb
         if ( !b.n )
             return;
         k_visibility_band<<<min( persistent_blocks( 128 ), blocks_for( b.capVisBand, 128 ) + 1 ), 128, 0, s>>>( b );
-        k_visibility_final<<<blocks_for( b.n, kWarpsPerBlock ), 32 * kWarpsPerBlock, 0, s>>>( b );
+        k_visibility_final<<<blocks_for( b.n, kWarpsPerBlock * 4 ), 32 * kWarpsPerBlock, 0, s>>>( b );
         counted( 2 );
     }
     void launch_emit( const Build & b, cudaStream_t s )
     {
         if ( !b.n )
             return;
-        k_emit<<<blocks_for( b.n, kWarpsPerBlock ), 32 * kWarpsPerBlock, 0, s>>>( b );
+        k_emit<<<blocks_for( b.n, kWarpsPerBlock * ( 32 / kEmitGroup ) ), 32 * kWarpsPerBlock, 0, s>>>( b );
         counted();
     }
     void launch_probes( const Build & b, cudaStream_t s )
