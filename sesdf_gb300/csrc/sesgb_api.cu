@@ -834,7 +834,7 @@ extern "C"
         }
         const float reach = c->hCounts->rmax + 2.f * c->rp + SESGB_SDF_BAND;
         launch_fine_params( c->b, reach, c->n, s );
-        launch_cells( c->b, 0, c->n, nullptr, c->scanScratch, s );
+        launch_cells( c->b, 2, c->n, nullptr, c->scanScratch, s );
         return cuda_ok( c, cudaGetLastError(), "sdf grid" ) ? SESGB_OK : SESGB_ERR_CUDA;
     }
 

@@ -241,10 +241,14 @@ namespace sesgb
         {
             float4   p;
             uint32_t m = 0;
-            if ( kind == 0 )
+            if ( kind == 0 || kind == 2 )
             {
                 p = b.atoms[ q ];
                 m = mol_of( b, q );
+                // kind 2 (SDF queries): the sign of the radius marks an atom without any
+                // accessible surface (neighbours present, every circle buried)
+                if ( kind == 2 && b.visCnt[ q ] == 0 && b.nbrCount[ q ] > 0 )
+                    p.w = -p.w;
             }
             else
             {
@@ -2330,19 +2334,21 @@ namespace sesgb
                     const uint32_t idx = row_item( rows, f );
                     i                  = b.cellItems[ idx ];
                     const float4 c     = b.cellPos[ idx ];
+                    const float  ra    = fabsf( c.w );
                     const float  L     = sqrtf( ( x.x - c.x ) * ( x.x - c.x ) + ( x.y - c.y ) * ( x.y - c.y ) + ( x.z - c.z ) * ( x.z - c.z ) );
-                    const float  R     = c.w + b.rp;
-                    keep               = L <= R + T;
-                    if ( keep )
+                    const float  R     = ra + b.rp;
+                    if ( L <= R + T )
                     {
                         smin = fminf( smin, L - R );
-                        const float v = L - c.w;
+                        const float v = L - ra;
                         if ( v < vmin || ( v == vmin && (int)i < vatom ) )
                         {
                             vmin  = v;
                             vatom = (int)i;
                         }
                         dl = fabsf( L - R );
+                        // fully buried atoms carry no point of dE: only the bounds above use them
+                        keep = !signbit( c.w );
                     }
                 }
                 const uint32_t mk = __ballot_sync( 0xffffffffu, keep );
