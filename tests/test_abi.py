@@ -51,3 +51,28 @@ def test_cpp_dropin_symbols(lib):
     for sym in ("_ZN3bcs5Sesdf5buildEv", "_ZN3bcs6Ssesdf5buildEv", "_ZN3bcs5Sesdf7getDataEv",
                 "_ZN3bcs6Ssesdf7getDataEv", "_ZN3bcs5Sesdf14getAtomIndicesEv"):
         assert hasattr(lib, sym), sym
+
+
+def test_batch_and_sdf_arguments_are_rejected_without_a_gpu(lib):
+    import numpy as np
+    h = ctypes.c_void_p()
+    atoms = np.zeros((4, 4), np.float32)
+    # molecule starts must begin at 0 and never decrease
+    bad = np.array([1, 2, 4], np.uint32)
+    assert lib.sesgb_create_batch(atoms.ctypes.data, bad.ctypes.data, 2, ctypes.c_float(1.4), 0, None,
+                                  ctypes.byref(h)) == -1
+    dec = np.array([0, 3, 2, 4], np.uint32)
+    assert lib.sesgb_create_batch(atoms.ctypes.data, dec.ctypes.data, 3, ctypes.c_float(1.4), 0, None,
+                                  ctypes.byref(h)) == -1
+    ok = np.array([0, 2, 4], np.uint32)
+    assert lib.sesgb_create_batch(atoms.ctypes.data, ok.ctypes.data, 0, ctypes.c_float(1.4), 0, None,
+                                  ctypes.byref(h)) == -1  # no molecules
+    assert lib.sesgb_create_batch(atoms.ctypes.data, ok.ctypes.data, 2, ctypes.c_float(1.4), 9, None,
+                                  ctypes.byref(h)) == -1  # bad mode
+    assert lib.sesgb_batch_molecules(None) == 0
+    rec = (ctypes.c_uint32 * len(api.MOL_FIELDS))()
+    assert lib.sesgb_molecule_record(None, 0, rec) == -1
+    assert lib.sesgb_get_full_molecule(None, 0, None) == -1
+    assert lib.sesgb_sdf(None, None, 0, None, None, None) == -1
+    assert lib.sesgb_sdf_backward(None, None, 0, None, None, None) == -1
+    assert len(api.MOL_FIELDS) == 16
