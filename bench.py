@@ -498,6 +498,22 @@ def run_reference(args, rank, world, local):
             rs.close()
             extra[f"{mode}_1m"] = {"ms_per_step": round(float(np.mean(sm)), 4),
                                    "atoms_per_s": round(shell.shape[0] / (np.mean(sm) * 1e-3), 1)}
+        del shell
+        # the reference's per-molecule loop over the same 256-molecule batch (context for the batched build)
+        from sesdf_gb300 import synth
+        mols = [synth.globule(int(nm), 1300 + k) for k, nm in enumerate(synth.batch_sizes())]
+        refs = [refharness.RefBuild(m, RP, "full") for m in mols]
+        for rr in refs:
+            rr.build()
+        loops = []
+        for _ in range(2):
+            flush.zero_()
+            torch.cuda.synchronize()
+            loops.append(float(sum(float(rr.time(1)[0]) for rr in refs)))
+        for rr in refs:
+            rr.close()
+        extra["batch256_mixed_loop"] = {"molecules": len(mols), "atoms": int(sum(m.shape[0] for m in mols)),
+                                        "loop_ms": round(float(np.median(loops)), 3)}
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": "atoms/s", "n_gpus": 1, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(total / args.steps, 4), "higher_is_better": True,
