@@ -679,8 +679,12 @@ static void circle_intersections( const ora_t * o, uint32_t t, probe_vec_t * out
     const v3       ci    = atom_pos( o, i );
     const double   ri    = atom_r( o, i );
     const v3       cj    = atom_pos( o, j );
-    const double   Ri2   = ( ri + rp ) * ( ri + rp );
-    const circle_t cij   = circle_geometry( ci, ri, cj, atom_r( o, j ), rp );
+    const double   Ri    = ri + rp;
+    const double   Rj    = atom_r( o, j ) + rp;
+    const double   Ri2   = Ri * Ri;
+    const v3       a     = sub( cj, ci );
+    const double   aa    = dot( a, a );
+    const double   p     = ( aa + Ri2 - Rj * Rj ) * 0.5;
     for ( uint32_t sk = 0; sk < ni; sk++ )
     {
         const uint32_t k = o->nbr[ base + sk ];
@@ -691,12 +695,23 @@ static void circle_intersections( const ora_t * o, uint32_t t, probe_vec_t * out
         const int32_t sjk = find_slot( o, j, k );
         if ( sjk < 0 )
             continue;
+        /* The points at distance R_i, R_j, R_k from the centres, in closed form
+         * (the reference intersects the circles (i, j), (i, k) for the same
+         * points, operations.inl:384-398): with a = c_j - c_i, b = c_k - c_i and
+         * n = a x b, x = c_i + y0 +- n sqrt(tt / |n|^2), where
+         * y0 = (p (b x n) + q (n x a)) / |n|^2 lies in the plane of the centres
+         * (a . y0 = p = (|a|^2 + R_i^2 - R_j^2) / 2, b . y0 = q likewise) and
+         * tt = R_i^2 - |y0|^2 is the squared height of the points over that plane. */
         const v3       ck  = atom_pos( o, k );
-        const circle_t cik = circle_geometry( ci, ri, ck, atom_r( o, k ), rp );
-        const v3       u   = sub( cik.normal, mul( cij.normal, dot( cik.normal, cij.normal ) ) );
-        const double   den = dot( u, cik.normal );
-        const v3       xc  = add( cij.center, mul( u, dot( sub( cik.center, cij.center ), cik.normal ) / den ) );
-        const double   tt  = -dot( sub( xc, ci ), sub( xc, ci ) ) + Ri2;
+        const double   Rk  = atom_r( o, k ) + rp;
+        const v3       b   = sub( ck, ci );
+        const v3       n   = cross( a, b );
+        const double   bb  = dot( b, b );
+        const double   q   = ( bb + Ri2 - Rk * Rk ) * 0.5;
+        const double   inv = 1.0 / dot( n, n );
+        const v3       y0  = mul( add( mul( cross( b, n ), p ), mul( cross( n, a ), q ) ), inv );
+        const double   tt  = Ri2 - dot( y0, y0 );
+        const double   den = dot( n, n ) / ( aa * bb ); /* sin^2 of the angle at c_i (diagnostics) */
         const double   cond = 1.0 / fabs( den ) + ( tt > 0.0 ? sqrt( Ri2 ) / sqrt( tt ) : 1e30 );
         if ( fabs( tt ) < kBand * kEps32 * Ri2 * ( 1.0 / fabs( den ) ) )
             counters[ BAND_PROBE_T ]++;
@@ -704,10 +719,10 @@ static void circle_intersections( const ora_t * o, uint32_t t, probe_vec_t * out
             continue;
         if ( cond > 1e3 )
             counters[ ILL_CONDITIONED ]++;
-        const v3     nn   = nrm( cross( cij.normal, cik.normal ) );
-        const double root = sqrt( tt );
-        const v3     x1   = add( xc, mul( nn, root ) );
-        const v3     x2   = sub( xc, mul( nn, root ) );
+        const double s    = sqrt( tt * inv );
+        const v3     xc   = add( ci, y0 );
+        const v3     x1   = add( xc, mul( n, s ) );
+        const v3     x2   = sub( xc, mul( n, s ) );
         int          vis1 = 1, vis2 = 1;
         for ( uint32_t sl = 0; sl < ni && ( vis1 || vis2 ); sl++ )
         {
@@ -728,9 +743,8 @@ static void circle_intersections( const ora_t * o, uint32_t t, probe_vec_t * out
         }
         if ( !vis1 && !vis2 )
             continue;
-        const v3 p2p3 = nrm( sub( cj, ci ) );
-        const v3 p4p3 = nrm( sub( cj, ck ) );
-        const v3 pn   = nrm( cross( p2p3, p4p3 ) );
+        /* singular (operations.inl:441-451): d^2 - rp^2 < -1e-4 with d the
+         * distance of the point from the plane of the centres, d^2 = tt */
         for ( int side = 0; side < 2; side++ )
         {
             if ( side == 0 && !vis1 )
@@ -738,11 +752,10 @@ static void circle_intersections( const ora_t * o, uint32_t t, probe_vec_t * out
             if ( side == 1 && !vis2 )
                 continue;
             const v3     x  = side == 0 ? x1 : x2;
-            const double d  = dot( sub( ci, x ), pn );
-            const double ms = d * d - (double)rp * rp - ( -(double)1e-4f );
-            if ( fabs( ms ) < kBand * kEps32 * ( d * d + (double)rp * rp ) * cond )
+            const double ms = tt - (double)rp * rp - ( -(double)1e-4f );
+            if ( fabs( ms ) < kBand * kEps32 * ( tt + (double)rp * rp ) * cond )
                 counters[ BAND_SINGULAR ]++;
-            const int singular = d * d - (double)rp * rp < -(double)1e-4f;
+            const int singular = tt - (double)rp * rp < -(double)1e-4f;
             probe_t   p;
             p.t      = t;
             p.slotJK = o->noff[ j ] + (uint32_t)sjk;

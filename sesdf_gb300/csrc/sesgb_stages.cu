@@ -861,36 +861,43 @@ namespace sesgb
         }
 
         // ---- probe solve -----------------------------------------------------
-        // Double-precision solve of findIntersectionsBetweenCircles
-        // (operations.inl:384-398): the two points at distance R_i, R_j, R_k
-        // from the centres. Returns false when t < 0 (no point).
-        __device__ __forceinline__ bool solve_d( d3 ci, double ri, d3 cj, double rj, d3 ck, double rk, double rp, d3 & x1, d3 & x2 )
+        // Double-precision triplet point in closed form. With a = c_j - c_i,
+        // b = c_k - c_i and n = a x b, the points at distance R_i, R_j, R_k from
+        // the three centres are c_i + y0 +- n sqrt(h2 / |n|^2), where
+        // y0 = (p (b x n) + q (n x a)) / |n|^2 lies in the plane of the centres
+        // (a . y0 = p = (|a|^2 + R_i^2 - R_j^2) / 2, b . y0 = q likewise) and
+        // h2 = R_i^2 - |y0|^2. The reference intersects the circles (i, j) and
+        // (i, k) for the same points (findIntersectionsBetweenCircles,
+        // operations.inl:384-398); the closed form takes one division and one
+        // root instead of six and four. h is also the distance of the points
+        // from the plane of the centres, the quantity of the singular test.
+        // Returns false when h2 < 0 (no point), as the reference's t < 0.
+        __device__ __forceinline__ bool solve_d( d3 ci, double ri, d3 cj, double rj, d3 ck, double rk, double rp, d3 & x1, d3 & x2,
+                                                 double & h2 )
         {
-            const dcircle cij = dcircle_geometry( ci, ri, cj, rj, rp );
-            const dcircle cik = dcircle_geometry( ci, ri, ck, rk, rp );
-            const d3      u   = dsub( cik.normal, dmul( cij.normal, ddot( cik.normal, cij.normal ) ) );
-            const double  den = ddot( u, cik.normal );
-            const d3 xc = dadd( cij.center, dmul( u, __ddiv_rn( ddot( dsub( cik.center, cij.center ), cik.normal ), den ) ) );
-            const d3     xci = dsub( xc, ci );
-            const double Ri  = __dadd_rn( ri, rp );
-            const double tt  = __dadd_rn( -ddot( xci, xci ), __dmul_rn( Ri, Ri ) );
-            if ( !( tt >= 0.0 ) )
+            const d3     a  = dsub( cj, ci ), bv = dsub( ck, ci );
+            const d3     n  = dcross( a, bv );
+            const double Ri = __dadd_rn( ri, rp ), Rj = __dadd_rn( rj, rp ), Rk = __dadd_rn( rk, rp );
+            const double Ri2 = __dmul_rn( Ri, Ri );
+            const double p   = __dmul_rn( __dsub_rn( __dadd_rn( ddot( a, a ), Ri2 ), __dmul_rn( Rj, Rj ) ), 0.5 );
+            const double q   = __dmul_rn( __dsub_rn( __dadd_rn( ddot( bv, bv ), Ri2 ), __dmul_rn( Rk, Rk ) ), 0.5 );
+            const double inv = __ddiv_rn( 1.0, ddot( n, n ) );
+            const d3     y0  = dmul( dadd( dmul( dcross( bv, n ), p ), dmul( dcross( n, a ), q ) ), inv );
+            h2               = __dsub_rn( Ri2, ddot( y0, y0 ) );
+            if ( !( h2 >= 0.0 ) )
                 return false;
-            const d3     nn   = dnrm( dcross( cij.normal, cik.normal ) );
-            const double root = __dsqrt_rn( tt );
-            x1                = dadd( xc, dmul( nn, root ) );
-            x2                = dsub( xc, dmul( nn, root ) );
+            const double s  = __dsqrt_rn( __dmul_rn( h2, inv ) );
+            const d3     xc = dadd( ci, y0 );
+            x1              = dadd( xc, dmul( n, s ) );
+            x2              = dsub( xc, dmul( n, s ) );
             return true;
         }
 
-        // singular flag (operations.inl:441-451): probe closer than rp to the plane of the centres
-        __device__ __forceinline__ bool singular_d( d3 ci, d3 cj, d3 ck, d3 x, double rp )
+        // singular flag (operations.inl:441-451): the point closer than rp to the
+        // plane of the centres, d^2 - rp^2 < -1e-4 with d^2 = h2
+        __device__ __forceinline__ bool singular_d( double h2, double rp )
         {
-            const d3     p2p3 = dnrm( dsub( cj, ci ) );
-            const d3     p4p3 = dnrm( dsub( cj, ck ) );
-            const d3     pn   = dnrm( dcross( p2p3, p4p3 ) );
-            const double dd   = ddot( dsub( ci, x ), pn );
-            return __dsub_rn( __dmul_rn( dd, dd ), __dmul_rn( rp, rp ) ) < -(double)1e-4f;
+            return __dsub_rn( h2, __dmul_rn( rp, rp ) ) < -(double)1e-4f;
         }
 
         // Occlusion of the double-precision points by N(i) \ {j, k} (operations.inl:401-430):
@@ -1490,20 +1497,22 @@ namespace sesgb
                 const float4   ai = b.atoms[ i ], aj = b.atoms[ b.nbr[ row + sj ] ], ak = b.atoms[ b.nbr[ row + sk ] ];
                 const d3       ci = D3( ai ), cj = D3( aj ), ck = D3( ak );
                 d3             x[ 2 ];
-                const bool     ok = solve_d( ci, (double)ai.w, cj, (double)aj.w, ck, (double)ak.w, rp, x[ 0 ], x[ 1 ] );
+                double         h2 = 0.0;
+                const bool     ok = solve_d( ci, (double)ai.w, cj, (double)aj.w, ck, (double)ak.w, rp, x[ 0 ], x[ 1 ], h2 );
                 if ( kind == kJobFill )
                 {
                     int4 cid = b.stageCid[ ent ];
                     int  aw  = cid.w < 0 ? -cid.w : cid.w;
                     if ( aw == 3 )
                     {
-                        aw    = singular_d( ci, cj, ck, x[ side ], rp ) ? 2 : 1;
+                        aw    = singular_d( h2, rp ) ? 2 : 1;
                         cid.w = cid.w < 0 ? -aw : aw;
                         b.stageCid[ ent ] = cid;
                         atomicAdd( aw == 2 ? &b.singCnt[ i ] : &b.regCnt[ i ], 1u );
                     }
-                    b.stagePos[ ent ] = make_float4( __double2float_rn( x[ side ].x ), __double2float_rn( x[ side ].y ),
-                                                     __double2float_rn( x[ side ].z ), (float)cid.w );
+                    const d3 xs       = side ? x[ 1 ] : x[ 0 ];
+                    b.stagePos[ ent ] = make_float4( __double2float_rn( xs.x ), __double2float_rn( xs.y ),
+                                                     __double2float_rn( xs.z ), (float)cid.w );
                     continue;
                 }
                 // band candidate: entries ent (x1) and ent + 1 (x2)
@@ -1517,7 +1526,7 @@ namespace sesgb
                     if ( !vis[ e ] )
                         continue;
                     int4      cid = b.stageCid[ ent + e ];
-                    const int aw  = singular_d( ci, cj, ck, x[ e ], rp ) ? 2 : 1;
+                    const int aw  = singular_d( h2, rp ) ? 2 : 1;
                     cid.w         = e == 0 ? aw : -aw;
                     b.stageCid[ ent + e ] = cid;
                     b.stagePos[ ent + e ] = make_float4( __double2float_rn( x[ e ].x ), __double2float_rn( x[ e ].y ),
@@ -1542,20 +1551,24 @@ namespace sesgb
         // Stable placement, singular probes first (the reference partitions with an
         // unstable sort, operations.inl:128-135), and the fill of
         // fillIntersections (operations.cu:206-269; exterior ssesdf/operations.cu:287-329).
+        // eight atoms per warp, four lanes per atom (an atom keeps ~2 probes)
+        constexpr uint32_t kPlaceGroup = 4;
+
         __global__ void __launch_bounds__( 32 * kWarpsPerBlock ) k_place( Build b )
         {
             const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
-            const uint32_t i    = blockIdx.x * kWarpsPerBlock + warp;
-            if ( i == 0 && lane == 0 )
+            const uint32_t grp = lane / kPlaceGroup, gl = lane % kPlaceGroup;
+            const uint32_t gmask = ( ( 1u << kPlaceGroup ) - 1u ) << ( grp * kPlaceGroup );
+            const uint32_t i     = ( blockIdx.x * kWarpsPerBlock + warp ) * ( 32 / kPlaceGroup ) + grp;
+            if ( i == 0 && gl == 0 )
                 b.counts->I = b.counts->Q + b.counts->regTotal;
-            if ( i >= b.n )
-                return;
+            const bool     atom  = i < b.n;
             const uint32_t Q     = b.counts->Q;
-            const uint32_t cnt   = b.chunkLen[ i ];
-            const uint32_t chunk = b.chunkStart[ i ];
-            uint32_t       so = b.singOff[ i ], ro = Q + b.regOff[ i ];
-            uint32_t       sq = b.singOff[ i ]; // singular index (molecule-major)
-            if ( b.nMol > 1 )
+            const uint32_t cnt   = atom ? b.chunkLen[ i ] : 0u;
+            const uint32_t chunk = atom ? b.chunkStart[ i ] : 0u;
+            uint32_t       so = atom ? b.singOff[ i ] : 0u, ro = atom ? Q + b.regOff[ i ] : 0u;
+            uint32_t       sq = so; // singular index (molecule-major)
+            if ( atom && b.nMol > 1 )
             {
                 // singular probes first within each molecule of the batch
                 const uint32_t m  = mol_of( b, i );
@@ -1564,20 +1577,24 @@ namespace sesgb
                 so                = r0 + b.singOff[ i ];
                 ro                = s0 + ( b.singOff[ a1 ] - s0 ) + b.regOff[ i ];
             }
-            for ( uint32_t m0 = 0; m0 < cnt; m0 += 32 )
+            uint32_t most = cnt;
+            for ( int o = 16; o > 0; o >>= 1 )
+                most = max( most, __shfl_xor_sync( 0xffffffffu, most, o ) );
+            const uint32_t lt = lanemask_lt() & gmask;
+            for ( uint32_t m0 = 0; m0 < most; m0 += kPlaceGroup )
             {
-                const uint32_t m     = m0 + lane;
+                const uint32_t m     = m0 + gl;
                 const bool     valid = m < cnt;
                 int4           cid   = make_int4( 0, 0, 0, 0 );
                 if ( valid )
                     cid = b.stageCid[ chunk + m ];
                 const bool     live = valid && cid.w != 0; // band entries without a point are holes
                 const bool     sing = live && ( cid.w == 2 || cid.w == -2 );
-                const uint32_t ms   = __ballot_sync( 0xffffffffu, sing );
-                const uint32_t mr   = __ballot_sync( 0xffffffffu, live && !sing );
-                const uint32_t dst  = sing ? so + __popc( ms & lanemask_lt() ) : ro + __popc( mr & lanemask_lt() );
+                const uint32_t ms   = __ballot_sync( 0xffffffffu, sing ) & gmask;
+                const uint32_t mr   = __ballot_sync( 0xffffffffu, live && !sing ) & gmask;
+                const uint32_t dst  = sing ? so + __popc( ms & lt ) : ro + __popc( mr & lt );
                 if ( sing && b.nMol > 1 )
-                    b.singList[ sq + __popc( ms & lanemask_lt() ) ] = dst;
+                    b.singList[ sq + __popc( ms & lt ) ] = dst;
                 so += __popc( ms );
                 ro += __popc( mr );
                 sq += __popc( ms );
@@ -2177,7 +2194,7 @@ namespace sesgb
     {
         if ( !b.n )
             return;
-        k_place<<<blocks_for( b.n, kWarpsPerBlock ), 32 * kWarpsPerBlock, 0, s>>>( b );
+        k_place<<<blocks_for( b.n, kWarpsPerBlock * ( 32 / kPlaceGroup ) ), 32 * kWarpsPerBlock, 0, s>>>( b );
         counted();
     }
     void launch_lists( const Build & b, cudaStream_t s )
