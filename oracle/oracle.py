@@ -17,6 +17,7 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 SRC = os.path.join(HERE, "sesdf_oracle.c")
+SRCS = [SRC, os.path.join(HERE, "area_oracle.c")]
 LIB = os.path.join(HERE, "_lib", "liboracle.so")
 
 COUNTERS = [
@@ -32,9 +33,9 @@ _lib = None
 def build(force: bool = False) -> str:
     """Compile the oracle with IEEE double arithmetic (no contraction) and OpenMP."""
     os.makedirs(os.path.dirname(LIB), exist_ok=True)
-    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
+    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < max(os.path.getmtime(s) for s in SRCS):
         cmd = ["gcc", "-O2", "-ffp-contract=off", "-fno-fast-math", "-fopenmp", "-fPIC", "-shared",
-               "-o", LIB + ".tmp", SRC, "-lm"]
+               "-o", LIB + ".tmp"] + SRCS + ["-lm"]
         subprocess.run(cmd, check=True)
         os.replace(LIB + ".tmp", LIB)
     return LIB
@@ -64,7 +65,7 @@ _DTYPES = {
     "status": np.uint8, "status0": np.uint8, "convex": np.uint32, "sectors": np.float64,
     "full": np.uint32, "slot_trim": np.uint32, "trim_slot": np.uint32, "ids": np.int32, "cids": np.int32,
     "posf": np.float32, "posd": np.float64, "ccount": np.uint32, "cstart": np.uint32, "clist": np.uint32,
-    "segments": np.uint32, "snbr": np.float32, "tori": np.float64, "counters": np.uint64,
+    "segments": np.uint32, "snbr": np.float32, "snbr_idx": np.uint32, "tori": np.float64, "counters": np.uint64,
 }
 _SHAPES = {"atoms": 4, "convex": 2, "sectors": 4, "full": 2, "ids": 4, "cids": 4, "posf": 4, "posd": 4,
            "segments": 4, "snbr": 4, "tori": 12}
@@ -147,3 +148,54 @@ def sdf(built: dict, queries: np.ndarray, band: float = 3.0, gq: np.ndarray | No
     if st != 0:
         raise RuntimeError("ora_sdf failed")
     return out, kind, g
+
+
+def area(built: dict, g_area=None, threads: int = 0):
+    """FP64 SES area of the primitives of a full-surface run(): returns (parts float64 [3] = convex,
+    toroidal, concave; per-atom area float64 [n] (sorted order); grad float64 [n, 4] (sorted order) =
+    d (g . parts) / d (x, y, z, r) with g = g_area (a scalar weighs the three alike), or None).
+    Test oracle only."""
+    lib = _load()
+    if not getattr(lib, "_area_ready", False):
+        P = ctypes.c_void_p
+        lib.ora_area.argtypes = [P, ctypes.c_uint32, P, P, P, P, ctypes.c_uint32, ctypes.c_uint32, P, ctypes.c_float,
+                                 P, P, P, P, ctypes.c_int]
+        lib.ora_area.restype = ctypes.c_int
+        lib.ora_region_area.argtypes = [P, ctypes.c_int, P]
+        lib.ora_region_area.restype = ctypes.c_double
+        lib._area_ready = True
+    atoms = np.ascontiguousarray(built["atoms"], np.float32)
+    n = atoms.shape[0]
+    noff = np.ascontiguousarray(built["noff"], np.uint32)
+    nbr = np.ascontiguousarray(built["nbr"], np.uint32)
+    ids = np.ascontiguousarray(built["ids"], np.int32).reshape(-1, 4)
+    posd = np.ascontiguousarray(built["posd"], np.float64).reshape(-1, 4)
+    sidx = np.ascontiguousarray(built["snbr_idx"], np.uint32)
+    parts = np.zeros(3, np.float64)
+    per_atom = np.zeros(n, np.float64)
+    g = np.zeros((n, 4), np.float64) if g_area is not None else None
+    gw = np.broadcast_to(np.asarray(g_area if g_area is not None else 0.0, np.float64), (3,)).copy()
+
+    def ptr(a):
+        return a.ctypes.data if a is not None and a.size else None
+    ov = lib.ora_area(ptr(atoms), n, ptr(noff), ptr(nbr), ptr(ids), ptr(posd), ids.shape[0], int(built["Q"]),
+                      ptr(sidx), ctypes.c_float(float(built["probe_radius"])),
+                      gw.ctypes.data, parts.ctypes.data,
+                      per_atom.ctypes.data, ptr(g), threads)
+    if ov:
+        raise RuntimeError(f"ora_area: {ov} region(s) exceeded the arc capacity")
+    return parts, per_atom, g
+
+
+def region_area(cons: np.ndarray):
+    """Area of {y on the unit sphere : y . w_m <= c_m} for cons [M, 4] = (w, c); returns
+    (area, sums [M, 4] = (boundary angle, integral of y over it)). Test oracle only."""
+    lib = _load()
+    if not getattr(lib, "_area_ready", False):
+        P = ctypes.c_void_p
+        lib.ora_region_area.argtypes = [P, ctypes.c_int, P]
+        lib.ora_region_area.restype = ctypes.c_double
+    c = np.ascontiguousarray(cons, np.float64).reshape(-1, 4)
+    s = np.zeros_like(c)
+    a = lib.ora_region_area(c.ctypes.data if c.size else None, c.shape[0], s.ctypes.data if s.size else None)
+    return a, s

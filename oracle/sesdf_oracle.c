@@ -157,7 +157,8 @@ typedef struct
     uint32_t * seg; /* 4S */
 
     /* singular probe neighbours */
-    float * snbr; /* 32 * 4 * Q */
+    float *    snbr;    /* 32 * 4 * Q */
+    uint32_t * snbrIdx; /* 32 * Q: singular index of each listed neighbour */
 
     /* exterior tori */
     uint64_t T;
@@ -1010,6 +1011,7 @@ static void stage_singular( ora_t * o )
     const uint32_t maxN = 32;
     const double   twoRp = 2.0 * (double)o->rp;
     o->snbr              = (float *)calloc( 4 * maxN * ( o->Q ? o->Q : 1 ), sizeof( float ) );
+    o->snbrIdx           = (uint32_t *)calloc( maxN * ( o->Q ? o->Q : 1 ), sizeof( uint32_t ) );
     if ( o->Q == 0 )
         return;
     fine_grid_t g;
@@ -1069,6 +1071,7 @@ static void stage_singular( ora_t * o )
             {
                 const float * pp  = o->posf + 4 * buf[ m ].idx;
                 float *       dst = o->snbr + 4 * ( maxN * q + m );
+                o->snbrIdx[ maxN * q + m ] = buf[ m ].idx;
                 dst[ 0 ]          = pp[ 0 ];
                 dst[ 1 ]          = pp[ 1 ];
                 dst[ 2 ]          = pp[ 2 ];
@@ -1219,6 +1222,7 @@ int ora_array( void * h, const char * name, void ** ptr, uint64_t * count )
     ORA_ARR( "clist", o->clist, o->clist ? 3ull * o->I : 0 )
     ORA_ARR( "segments", o->seg, 4ull * o->S )
     ORA_ARR( "snbr", o->snbr, 4ull * 32ull * o->Q )
+    ORA_ARR( "snbr_idx", o->snbrIdx, 32ull * o->Q )
     ORA_ARR( "tori", o->tori, 12ull * o->T )
     ORA_ARR( "counters", o->counters, (uint64_t)ORA_NCOUNTER )
 #undef ORA_ARR
@@ -1260,6 +1264,7 @@ void ora_free( void * h )
     free( o->clist );
     free( o->seg );
     free( o->snbr );
+    free( o->snbrIdx );
     free( o->tori );
     free( o );
 }
