@@ -277,7 +277,8 @@ def batch_extras(args, flush, rank=0, world=1):
 
 
 def sdf_extra(flush):
-    """SDF forward and adjoint: 20,000-atom globule, 1M query points within 3 A of its vdW surface."""
+    """SDF forward and adjoint (20,000-atom globule, 1M query points within 3 A of its vdW surface);
+    SES area of the same build and its adjoint."""
     import torch
     from sesdf_gb300 import SesBuild, synth
     atoms, q = synth.sdf_workload()
@@ -309,6 +310,33 @@ def sdf_extra(flush):
     res["queries"] = int(m)
     res["atoms"] = int(atoms.shape[0])
     res["band_A"] = 3.0
+    # SES area of the primitives (sesgb_ses_area synchronises: host wall clock around the call)
+    # and its adjoint (device events)
+    per = torch.empty(atoms.shape[0], dtype=torch.float32, device="cuda")
+    for _ in range(3):
+        area = g.ses_area(per.data_ptr(), stream.cuda_stream)
+    ms = []
+    for _ in range(10):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        area = g.ses_area(per.data_ptr(), stream.cuda_stream)
+        ms.append((time.perf_counter() - t0) * 1e3)
+    res["area_A2"] = round(area["total"], 3)
+    res["area_parts_A2"] = {k: round(area[k], 3) for k in ("convex", "toroidal", "concave")}
+    res["area_ms"] = round(float(np.median(ms)), 4)
+    for _ in range(3):
+        g.ses_area_backward(ga.data_ptr(), (1.0, 1.0, 1.0), stream.cuda_stream)
+    ms = []
+    for _ in range(10):
+        flush.zero_()
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        g.ses_area_backward(ga.data_ptr(), (1.0, 1.0, 1.0), stream.cuda_stream)
+        t1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(t0.elapsed_time(t1))
+    res["area_backward_ms"] = round(float(np.median(ms)), 4)
     g.close()
     return res
 

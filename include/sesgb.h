@@ -249,6 +249,21 @@ int sesgb_sdf( sesgb_ctx * ctx, const float * device_queries, uint32_t m, float 
 int sesgb_sdf_backward( sesgb_ctx * ctx, const float * device_queries, uint32_t m, const float * device_grad_sdf,
                         float * device_grad_atoms, void * stream );
 
+/* Solvent-excluded surface area of the primitives of the last full-surface build
+ * of one molecule (no counterpart in the reference): the convex patches (the
+ * accessible directions of every SAS sphere, scaled to the vdW sphere), the tori
+ * swept over the accessible circle arcs (trimmed at the axis where a torus
+ * self-intersects) and the concave probe triangles outside the spheres of their
+ * listed neighbour probes. host_parts receives double[3] = convex, toroidal,
+ * concave (the total is their sum); device_atom_area (may be NULL): float[n] in
+ * input order, each atom's convex patch plus half of its tori and a third of its
+ * probes' concave patches. Synchronises `stream`. */
+int sesgb_ses_area( sesgb_ctx * ctx, double * host_parts, float * device_atom_area, void * stream );
+/* Adjoint of sesgb_ses_area: device_grad_atoms (float4[n], input atom order)
+ * receives d (sum_k host_grad_parts[k] * part_k) / d (x, y, z, r) of every atom
+ * (probe positions follow their atoms by the implicit-function rule). */
+int sesgb_ses_area_backward( sesgb_ctx * ctx, const float * host_grad_parts, float * device_grad_atoms, void * stream );
+
 /* Number of kernels this library has launched in this process (host-side count). */
 uint64_t sesgb_launch_count( void );
 

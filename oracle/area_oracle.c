@@ -25,7 +25,11 @@
  * corner where circles m and n meet (s = sqrt(1 - c^2)). The Euler
  * characteristic is never needed: R is cut into three lunes of 120 degrees
  * around the z axis (two more constraints each); a lune has area 4 pi / 3 < 2 pi,
- * so the area of each piece is the Gauss-Bonnet sum reduced mod 2 pi.
+ * so the area of each piece is the Gauss-Bonnet sum reduced mod 2 pi. The
+ * corner terms are written per arc, as the change of the boundary tangent's
+ * angle against a fixed frame field between the arc's two ends: no corner has to
+ * be matched with the arc on its other side, and several circles through one
+ * point (the axis points of a self-intersecting torus) need no special case.
  *
  * Gradient: moving constraint m changes the area by dA/dc_m = dphi_m and
  * dA/dw_m = -integral of y dphi over the arcs of m on the boundary (the
@@ -52,8 +56,7 @@ static inline a3     across( a3 a, a3 b ) { return A3( a.y * b.z - a.z * b.y, a.
 static inline double alen( a3 a ) { return sqrt( adot( a, a ) ); }
 
 #define AREA_MAXC 256 /* constraints of one region (neighbours, or 3 edges + 32 probes) */
-static const double kPi   = 3.14159265358979323846;
-static const double kSnap = 1e-9; /* corner and arc resolution (radians) */
+static const double kPi = 3.14159265358979323846;
 
 typedef struct
 {
@@ -81,7 +84,7 @@ typedef struct
     cons_t k[ AREA_MAXC + 2 ];
     a3     e1[ AREA_MAXC + 2 ], e2[ AREA_MAXC + 2 ];
     double s[ AREA_MAXC + 2 ];
-    double ivS[ AREA_MAXC + 2 ], ivL[ AREA_MAXC + 2 ], enV[ AREA_MAXC + 2 ];
+    double ivS[ AREA_MAXC + 2 ], ivL[ AREA_MAXC + 2 ], enV[ AREA_MAXC + 2 ], enL[ AREA_MAXC + 2 ];
     int    ivN[ AREA_MAXC + 2 ], enN[ AREA_MAXC + 2 ];
     int    M;       /* constraints of the region (without the lune pair) */
     arc_t  arcs[ 4 * ( AREA_MAXC + 2 ) ];
@@ -105,11 +108,28 @@ static double wrap2pi( double a )
     return a < 0.0 ? a + 2.0 * kPi : a;
 }
 
-static double turn_angle( const region_t * R, int m, int n )
+/* Tangent-angle change of the boundary along the arc [pa, pa + len] of a circle,
+ * traversed with the region on its left (decreasing phi, the cap lies towards w),
+ * measured against the frame field xi(y) = a - (a . y) y (singular only at
+ * +-a): alpha(end) - alpha(start) with alpha = atan2((xi x t) . y, xi . t). At a
+ * corner the arcs meeting there share y, so the differences of their alphas
+ * are the corner's turning angle and no corner needs to know its partner. */
+static const a3 kFrameAxis = { 0.32140077, 0.55410134, 0.76790185 }; /* a generic unit direction */
+
+static double frame_angle( a3 y, a3 t )
 {
-    double v = ( adot( R->k[ m ].w, R->k[ n ].w ) - R->k[ m ].c * R->k[ n ].c ) / ( R->s[ m ] * R->s[ n ] );
-    v        = v > 1.0 ? 1.0 : ( v < -1.0 ? -1.0 : v );
-    return acos( v );
+    const a3 xi = asub( kFrameAxis, amul( y, adot( kFrameAxis, y ) ) );
+    return atan2( adot( across( xi, t ), y ), adot( xi, t ) );
+}
+
+static double arc_turn( a3 w, double c, double s, a3 e1, a3 e2, double pa, double len )
+{
+    const double p0 = pa + len, p1 = pa; /* traversal from p0 down to p1 */
+    const a3     y0 = aadd( amul( w, c ), amul( aadd( amul( e1, cos( p0 ) ), amul( e2, sin( p0 ) ) ), s ) );
+    const a3     y1 = aadd( amul( w, c ), amul( aadd( amul( e1, cos( p1 ) ), amul( e2, sin( p1 ) ) ), s ) );
+    const a3     t0 = asub( amul( e1, sin( p0 ) ), amul( e2, cos( p0 ) ) );
+    const a3     t1 = asub( amul( e1, sin( p1 ) ), amul( e2, cos( p1 ) ) );
+    return frame_angle( y1, t1 ) - frame_angle( y0, t0 );
 }
 
 /* area of R cut to lune L (azimuth in [2 pi L / 3, 2 pi (L + 1) / 3]); adds the
@@ -187,90 +207,47 @@ static double region_lune( region_t * R, int L, cons_sum_t * sums )
             }
             continue;
         }
-        /* allowed arcs: gaps between the forbidden intervals. Interval ends within
-         * kSnap of each other are one corner (several circles through one point,
-         * e.g. the axis points of a self-intersecting torus); its partner is the
-         * circle that turns most (the one bounding the corner), and a gap shorter
-         * than kSnap is no arc. */
-        int nE = 0;
+        /* allowed arcs: the gaps between the cuts. An end strictly inside another
+         * cut is covered (lengths re-measured from the rounded ends, so that equal
+         * ends compare equal); of equal uncovered ends the first one counts. */
+        for ( int q = 0; q < nIv; q++ )
+        {
+            R->enV[ q ]       = wrap2pi( R->ivS[ q ] + R->ivL[ q ] );
+            const double len2 = wrap2pi( R->enV[ q ] - R->ivS[ q ] );
+            R->enL[ q ]       = len2 >= 0.5 * R->ivL[ q ] ? len2 : R->ivL[ q ];
+        }
         for ( int a = 0; a < nIv; a++ )
         {
-            const double end     = wrap2pi( R->ivS[ a ] + R->ivL[ a ] );
-            int          covered = 0;
-            for ( int b = 0; b < nIv && !covered; b++ )
-                if ( b != a && wrap2pi( end - R->ivS[ b ] ) < R->ivL[ b ] - kSnap )
-                    covered = 1;
-            if ( covered )
+            R->enN[ a ] = 1;
+            for ( int b = 0; b < nIv && R->enN[ a ]; b++ )
+                if ( b != a && wrap2pi( R->enV[ a ] - R->ivS[ b ] ) < R->enL[ b ] )
+                    R->enN[ a ] = 0;
+        }
+        for ( int a = 0; a < nIv; a++ )
+        {
+            if ( !R->enN[ a ] )
                 continue;
-            /* insertion into the sorted list of uncovered ends */
-            int q = nE++;
-            while ( q > 0 && R->enV[ q - 1 ] > end )
-            {
-                R->enV[ q ] = R->enV[ q - 1 ];
-                R->enN[ q ] = R->enN[ q - 1 ];
-                q--;
-            }
-            R->enV[ q ] = end;
-            R->enN[ q ] = R->ivN[ a ];
-        }
-        /* a group that wraps past 2 pi starts at its first member after the wrap */
-        int first = 0;
-        if ( nE > 1 && R->enV[ 0 ] + 2.0 * kPi - R->enV[ nE - 1 ] <= kSnap )
-        {
-            first = nE - 1;
-            while ( first > 0 && R->enV[ first ] - R->enV[ first - 1 ] <= kSnap )
-                first--;
-        }
-        for ( int g0 = 0; g0 < nE; )
-        {
-            /* the group of ends starting at index (first + g0) mod nE */
-            int    cnt = 1;
-            int    ia  = ( first + g0 ) % nE;
-            int    na  = R->enN[ ia ];
-            double end = R->enV[ ia ];
-            double tha = turn_angle( R, m, na );
-            while ( g0 + cnt < nE )
-            {
-                const int    ib = ( first + g0 + cnt ) % nE;
-                const double dv = wrap2pi( R->enV[ ib ] - R->enV[ ( first + g0 + cnt - 1 ) % nE ] );
-                if ( dv > kSnap )
-                    break;
-                const double th = turn_angle( R, m, R->enN[ ib ] );
-                if ( th > tha )
-                {
-                    tha = th;
-                    na  = R->enN[ ib ];
-                }
-                end = R->enV[ ib ];
-                cnt++;
-            }
-            g0 += cnt;
-            /* the next interval start and the starts within kSnap of it */
+            const double end = R->enV[ a ];
+            int          dup = 0;
+            for ( int b = 0; b < a && !dup; b++ )
+                dup = R->enN[ b ] && R->enV[ b ] == end;
+            if ( dup )
+                continue;
             double gap = 2.0 * kPi;
+            int    nb  = -1;
             for ( int b = 0; b < nIv; b++ )
             {
                 const double g = wrap2pi( R->ivS[ b ] - end );
-                if ( g > 0.0 && g < gap )
-                    gap = g;
-            }
-            int    nbc = -1;
-            double thb = -1.0;
-            for ( int b = 0; b < nIv; b++ )
-            {
-                const double g = wrap2pi( R->ivS[ b ] - end );
-                if ( g > 0.0 && g <= gap + kSnap )
+                if ( g > 0.0 && ( nb < 0 || g < gap ) )
                 {
-                    const double th = turn_angle( R, m, R->ivN[ b ] );
-                    if ( th > thb )
-                    {
-                        thb = th;
-                        nbc = R->ivN[ b ];
-                    }
+                    gap = g;
+                    nb  = b;
                 }
             }
-            if ( !( gap > kSnap ) || nbc < 0 )
+            if ( nb < 0 )
                 continue;
-            total += cm * gap - 0.5 * ( tha + thb );
+            const int na = R->ivN[ a ], nbc = R->ivN[ nb ];
+            total += cm * gap + arc_turn( wm, cm, sm, e1, e2, end, gap );
             if ( m < M )
             {
                 sums[ m ].dphi += gap;
@@ -420,13 +397,14 @@ static void probe_back( const float * atoms, const int32_t * ids, const double *
 }
 
 /* Total SES area of the primitives of a full-surface build (sorted atoms xyzr,
- * CSR neighbour lists, probes: ids (i, j, k, neighbour count), FP64 positions,
+ * CSR neighbour lists with their circle statuses (an atom whose circles are all
+ * buried has no accessible patch), probes: ids (i, j, k, neighbour count), FP64 positions,
  * the first Q probes singular with neighbour lists snbrIdx[32 q + t]).
  * parts: convex, toroidal, concave. atomArea (n, optional): convex area of the
  * atom + half of its tori + a third of its probes' concave patches. With grad
  * (4n, sorted order, accumulated): d (sum_k gParts[k] parts[k]) / d (x, y, z, r).
  * Returns the number of regions whose arc list overflowed (0 when complete). */
-int ora_area( const float * atoms, uint32_t n, const uint32_t * noff, const uint32_t * nbr, const int32_t * ids,
+int ora_area( const float * atoms, uint32_t n, const uint32_t * noff, const uint32_t * nbr, const uint8_t * status, const int32_t * ids,
               const double * posd, uint32_t I, uint32_t Q, const uint32_t * snbrIdx, float rpf, const double * gParts,
               double * parts, double * atomArea, double * grad, int threads )
 {
@@ -456,6 +434,12 @@ int ora_area( const float * atoms, uint32_t n, const uint32_t * noff, const uint
             const double   Ri = (double)ai[ 3 ] + rp, ri = ai[ 3 ];
             const uint32_t b0 = noff[ i ], ni = noff[ i + 1 ] - b0;
             int            M  = 0;
+            /* an atom whose circles are all buried (status 0) has no accessible patch */
+            int open = ni == 0;
+            for ( uint32_t s = 0; s < ni && !open; s++ )
+                open = status[ b0 + s ] != 0;
+            if ( !open )
+                continue;
             for ( uint32_t s = 0; s < ni && M < AREA_MAXC; s++ )
             {
                 const float * aj = atoms + 4 * (size_t)nbr[ b0 + s ];

@@ -158,7 +158,7 @@ def area(built: dict, g_area=None, threads: int = 0):
     lib = _load()
     if not getattr(lib, "_area_ready", False):
         P = ctypes.c_void_p
-        lib.ora_area.argtypes = [P, ctypes.c_uint32, P, P, P, P, ctypes.c_uint32, ctypes.c_uint32, P, ctypes.c_float,
+        lib.ora_area.argtypes = [P, ctypes.c_uint32, P, P, P, P, P, ctypes.c_uint32, ctypes.c_uint32, P, ctypes.c_float,
                                  P, P, P, P, ctypes.c_int]
         lib.ora_area.restype = ctypes.c_int
         lib.ora_region_area.argtypes = [P, ctypes.c_int, P]
@@ -178,7 +178,8 @@ def area(built: dict, g_area=None, threads: int = 0):
 
     def ptr(a):
         return a.ctypes.data if a is not None and a.size else None
-    ov = lib.ora_area(ptr(atoms), n, ptr(noff), ptr(nbr), ptr(ids), ptr(posd), ids.shape[0], int(built["Q"]),
+    status = np.ascontiguousarray(built["status"], np.uint8)
+    ov = lib.ora_area(ptr(atoms), n, ptr(noff), ptr(nbr), ptr(status), ptr(ids), ptr(posd), ids.shape[0], int(built["Q"]),
                       ptr(sidx), ctypes.c_float(float(built["probe_radius"])),
                       gw.ctypes.data, parts.ctypes.data,
                       per_atom.ctypes.data, ptr(g), threads)

@@ -31,7 +31,7 @@ EXPORTS = [
     "sesgb_error_string", "sesgb_last_error", "sesgb_destroy", "sesgb_stage_times", "sesgb_stage_name",
     "sesgb_launch_count", "sesgb_build_async", "sesgb_finish", "sesgb_sort_atoms_noalloc",
     "sesgb_create_batch", "sesgb_batch_molecules", "sesgb_molecule_record", "sesgb_get_full_molecule",
-    "sesgb_get_exterior_molecule", "sesgb_sdf", "sesgb_sdf_backward",
+    "sesgb_get_exterior_molecule", "sesgb_sdf", "sesgb_sdf_backward", "sesgb_ses_area", "sesgb_ses_area_backward",
 ]
 SDF_BAND = 3.0
 MOL_FIELDS = ["atoms", "sectors", "full_circles", "partial_circles", "probes", "singular_probes", "segments", "tori",
@@ -129,6 +129,8 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         lib.sesgb_get_exterior_molecule.argtypes = [P, U32, ctypes.POINTER(ExteriorData)]
         lib.sesgb_sdf.argtypes = [P, P, U32, P, P, P]
         lib.sesgb_sdf_backward.argtypes = [P, P, U32, P, P, P]
+        lib.sesgb_ses_area.argtypes = [P, P, P, P]
+        lib.sesgb_ses_area_backward.argtypes = [P, P, P, P]
         _lib = lib
     return _lib
 
@@ -248,6 +250,19 @@ class SesBuild:
         """grad_atoms (float4[n], input order) = sum_q grad_sdf[q] d sdf_q / d (x, y, z, r)."""
         self._check(self._lib.sesgb_sdf_backward(self._h, queries_ptr, m, grad_sdf_ptr, grad_atoms_ptr, stream),
                     "sdf_backward")
+
+    def ses_area(self, atom_area_ptr: int | None = None, stream: int | None = None) -> dict:
+        """SES area of the primitives of the last full-surface build: {"convex", "toroidal", "concave",
+        "total"} in A^2. atom_area_ptr (device float[n], input order): per-atom areas. Synchronises."""
+        parts = np.zeros(3, np.float64)
+        self._check(self._lib.sesgb_ses_area(self._h, parts.ctypes.data, atom_area_ptr, stream), "ses_area")
+        return {"convex": float(parts[0]), "toroidal": float(parts[1]), "concave": float(parts[2]),
+                "total": float(parts.sum())}
+
+    def ses_area_backward(self, grad_atoms_ptr: int, grad_parts=(1.0, 1.0, 1.0), stream: int | None = None):
+        """grad_atoms (device float4[n], input order) = d (grad_parts . (convex, toroidal, concave)) / d (x, y, z, r)."""
+        g = np.ascontiguousarray(np.broadcast_to(np.asarray(grad_parts, np.float32), (3,)))
+        self._check(self._lib.sesgb_ses_area_backward(self._h, g.ctypes.data, grad_atoms_ptr, stream), "ses_area_backward")
 
     @property
     def max_neighbor_per_atom(self) -> int:

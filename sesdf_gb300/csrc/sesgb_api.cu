@@ -42,6 +42,9 @@ struct sesgb_ctx
     float * gradSorted = nullptr;
     void *  sdfScratch = nullptr;
     size_t  sdfScratchBytes = 0;
+    double * areaParts  = nullptr; // device double[3]
+    void *   areaScratch = nullptr;
+    size_t   areaScratchBytes = 0;
 
     Build          b {};
     DeviceCounts * hCounts = nullptr;
@@ -236,6 +239,7 @@ namespace
         b.probePos    = dalloc<float4>( c, L, PR, ok );
         b.probeCid    = dalloc<int4>( c, L, PR, ok );
         b.probeNbrs   = dalloc<float4>( c, L, PR * kMaxProbeNbr, ok );
+        b.probeNbrIdx = dalloc<uint32_t>( c, L, PR * kMaxProbeNbr, ok );
         b.singList    = c->nMol > 1 ? dalloc<uint32_t>( c, L, PR, ok ) : nullptr;
         b.ccount      = dalloc<uint32_t>( c, L, C1 + 1, ok );
         b.cstart      = dalloc<uint32_t>( c, L, C1 + 1, ok );
@@ -803,6 +807,10 @@ extern "C"
             cudaFree( c->gradSorted );
         if ( c->sdfScratch )
             cudaFree( c->sdfScratch );
+        if ( c->areaParts )
+            cudaFree( c->areaParts );
+        if ( c->areaScratch )
+            cudaFree( c->areaScratch );
         delete c;
     }
 
@@ -864,6 +872,75 @@ extern "C"
         launch_sdf_backward( c->b, device_queries, m, SESGB_SDF_BAND, device_grad_sdf, c->gradSorted, device_grad_atoms,
                              c->sdfScratch, s );
         return cuda_ok( c, cudaGetLastError(), "sdf backward" ) ? SESGB_OK : SESGB_ERR_CUDA;
+    }
+
+    // ---- SES area of the primitives ---------------------------------------------
+    static int area_prepare( sesgb_ctx * c, cudaStream_t s )
+    {
+        if ( !c->built )
+            return SESGB_ERR_NOT_BUILT;
+        if ( c->mode != SESGB_MODE_FULL || c->nMol != 1 )
+        {
+            c->err = "the SES area needs a full-surface build of one molecule";
+            return SESGB_ERR_MODE;
+        }
+        if ( !c->areaParts && !cuda_ok( c, cudaMalloc( &c->areaParts, 4 * sizeof( double ) ), "cudaMalloc" ) )
+            return SESGB_ERR_CUDA;
+        const size_t need = area_scratch_bytes( c->b );
+        if ( need > c->areaScratchBytes )
+        {
+            if ( c->areaScratch )
+            {
+                cudaStreamSynchronize( s );
+                cudaFree( c->areaScratch );
+                c->areaScratch = nullptr;
+            }
+            if ( !cuda_ok( c, cudaMalloc( &c->areaScratch, need ), "cudaMalloc" ) )
+            {
+                c->areaScratchBytes = 0;
+                return SESGB_ERR_CUDA;
+            }
+            c->areaScratchBytes = need;
+        }
+        // the overflow word of the build is free once its counts are on the host
+        cudaMemsetAsync( &c->b.counts->overflow, 0, sizeof( uint32_t ), s );
+        return SESGB_OK;
+    }
+
+    int sesgb_ses_area( sesgb_ctx * c, double * host_parts, float * device_atom_area, void * stream )
+    {
+        if ( !c || !host_parts )
+            return SESGB_ERR_INVALID;
+        cudaStream_t s  = static_cast<cudaStream_t>( stream );
+        int          st = area_prepare( c, s );
+        if ( st != SESGB_OK )
+            return st;
+        launch_area( c->b, c->areaParts, device_atom_area, s );
+        uint32_t ovf = 0;
+        cudaMemcpyAsync( host_parts, c->areaParts, 3 * sizeof( double ), cudaMemcpyDeviceToHost, s );
+        cudaMemcpyAsync( &ovf, &c->b.counts->overflow, sizeof( uint32_t ), cudaMemcpyDeviceToHost, s );
+        if ( !cuda_ok( c, cudaStreamSynchronize( s ), "ses area" ) )
+            return SESGB_ERR_CUDA;
+        if ( ovf & kOverflowArea )
+        {
+            c->err = "an area region held more constraints than the kernel does (more than 128 neighbours)";
+            return SESGB_ERR_OVERFLOW;
+        }
+        return SESGB_OK;
+    }
+
+    int sesgb_ses_area_backward( sesgb_ctx * c, const float * host_grad_parts, float * device_grad_atoms, void * stream )
+    {
+        if ( !c || !host_grad_parts || !device_grad_atoms )
+            return SESGB_ERR_INVALID;
+        cudaStream_t s  = static_cast<cudaStream_t>( stream );
+        int          st = area_prepare( c, s );
+        if ( st != SESGB_OK )
+            return st;
+        if ( !c->gradSorted && !cuda_ok( c, cudaMalloc( &c->gradSorted, sizeof( float ) * 4 * std::max<size_t>( c->n, 1 ) ), "cudaMalloc" ) )
+            return SESGB_ERR_CUDA;
+        launch_area_backward( c->b, host_grad_parts, c->gradSorted, device_grad_atoms, c->areaScratch, s );
+        return cuda_ok( c, cudaGetLastError(), "ses area backward" ) ? SESGB_OK : SESGB_ERR_CUDA;
     }
 
     int sesgb_create_batch( const float * atoms, const uint32_t * molecule_start, uint32_t molecules, float probe_radius,

@@ -1,0 +1,803 @@
+// sesgb_area.cu -- solvent-excluded surface area of the primitives of a
+// full-surface build, and its adjoint with respect to the atoms.
+//
+// The reference renders its primitives and computes no area; the area here is
+// the area of those primitives: the convex patch of every atom (the directions
+// of its SAS sphere outside every other SAS sphere of N(i), scaled to the vdW
+// sphere: the sectors of buildConvexPatchesSectors, operations.inl:175-228),
+// the torus swept over the accessible arcs of every circle (the segments and
+// full circles, operations.inl:552-668), trimmed at its axis when it
+// self-intersects, and the concave triangle of every probe (operations.inl:
+// 230-486) outside the spheres of its listed neighbour probes
+// (findIntersectionsNeighbors, operations.cu:271-338).
+//
+// Every patch is a region R = {y : |y| = 1, y . w_m <= c_m} of a sphere. By
+// Gauss-Bonnet its area is 2 pi chi + sum_m c_m dphi_m - sum_v theta_v, with
+// dphi_m the angle of circle m on the boundary of R and theta_v the turning
+// angle at a corner. Cut into three lunes of 120 degrees around z, every piece
+// has area < 2 pi, so the sum reduced mod 2 pi is the area and the Euler
+// characteristic is never needed. The corner terms are written per arc, as the
+// change of the boundary tangent's angle against a fixed frame field between the
+// arc's ends, so that no corner has to be matched with the arc on its other side
+// (several circles through one point, as at the axis points of a self-intersecting
+// torus, need no special case, and float32 rounding moves the sum only by as much
+// as it moves the arcs). Adjoint: dA/dc_m = dphi_m,
+// dA/dw_m = -integral of y over the boundary arcs of m; an arc's angle moves with
+// the circles that bound its ends; probe positions follow their atoms by the
+// implicit function of |p - c_a|^2 = R_a^2.
+//
+// Work split: a warp per atom (lanes over the circles of its region), a warp per
+// probe (lanes over the triangle edges and neighbour caps), float32 throughout.
+#include "sesgb_device.cuh"
+#include "sesgb_stages.cuh"
+
+namespace sesgb
+{
+    namespace
+    {
+        constexpr float    kPiF       = 3.14159265358979f;
+        constexpr float    k2PiF      = 6.28318530717959f;
+        constexpr int      kAreaWarps = 4;
+        constexpr int      kAreaNbr   = 128;             // neighbour constraints of one atom region
+        constexpr int      kAreaIv    = kAreaNbr + 2;    // cuts of one circle
+        constexpr int      kProbeCons = 3 + (int)kMaxProbeNbr;
+        static_assert( kMaxProbeNbr <= 32, "one neighbour cap per lane" );
+
+        struct Circ
+        {
+            f3    w, e1, e2;
+            float c, s;
+        };
+
+        // reduces an angle in (-4 pi, 6 pi) to [0, 2 pi)
+        __device__ __forceinline__ float wrapf( float a )
+        {
+            if ( a < 0.f )
+                a += k2PiF;
+            if ( a < 0.f )
+                a += k2PiF;
+            if ( a >= k2PiF )
+                a -= k2PiF;
+            if ( a >= k2PiF )
+                a -= k2PiF;
+            return a;
+        }
+
+        __device__ __forceinline__ Circ circ_of( float4 k )
+        {
+            Circ         C;
+            C.w            = F3( k.x, k.y, k.z );
+            C.c            = k.w;
+            C.s            = sqrtf( fmaxf( 0.f, ( 1.f - k.w ) * ( 1.f + k.w ) ) );
+            const float ax = fabsf( k.x ), ay = fabsf( k.y ), az = fabsf( k.z );
+            const f3    t  = ( ax <= ay && ax <= az ) ? F3( 1.f, 0.f, 0.f ) : ( ay <= az ? F3( 0.f, 1.f, 0.f ) : F3( 0.f, 0.f, 1.f ) );
+            C.e1           = normalize( cross( C.w, t ) );
+            C.e2           = cross( C.w, C.e1 );
+            return C;
+        }
+
+        // y . w <= 0 bounding lune L (side 0: the plane at 2 pi L / 3, side 1: the next one)
+        __device__ __forceinline__ float4 lune_cons( int L, int side )
+        {
+            float sn, cs;
+            sincosf( ( k2PiF / 3.f ) * (float)( L + side ), &sn, &cs );
+            return side == 0 ? make_float4( sn, -cs, 0.f, 0.f ) : make_float4( -sn, cs, 0.f, 0.f );
+        }
+
+        // Forbidden arc of circle C under constraint k: 0 none, 1 [start, start + len), 2 all of it.
+        __device__ __forceinline__ int cut_of( const Circ & C, float4 k, float & start, float & len )
+        {
+            if ( !( k.w < 1.f ) )
+                return 0;
+            const f3    wn  = F3( k.x, k.y, k.z );
+            const float p1  = dot( C.e1, wn ), p2 = dot( C.e2, wn );
+            const float B   = C.s * sqrtf( p1 * p1 + p2 * p2 );
+            const float rhs = k.w - C.c * dot( C.w, wn );
+            if ( !( B > fabsf( rhs ) ) )
+                return rhs < 0.f ? 2 : 0;
+            const float delta = atan2f( sqrtf( ( B - rhs ) * ( B + rhs ) ), rhs );
+            start             = wrapf( atan2f( p2, p1 ) - delta );
+            len               = 2.f * delta;
+            return 1;
+        }
+
+        __device__ __forceinline__ f3 point_at( const Circ & C, float phi )
+        {
+            float sn, cs;
+            sincosf( phi, &sn, &cs );
+            return C.w * C.c + ( C.e1 * cs + C.e2 * sn ) * C.s;
+        }
+
+        // Cuts of one circle: start, length, constraint, rounded end, re-measured length.
+        struct Cuts
+        {
+            float    s[ kAreaIv ], l[ kAreaIv ], ev[ kAreaIv ], el[ kAreaIv ];
+            uint16_t n[ kAreaIv ];
+            int      count;
+        };
+
+        // frame field xi(y) = a - (a . y) y, singular only at +-a (a generic direction)
+        __device__ __forceinline__ float frame_angle( f3 y, f3 t )
+        {
+            const f3    a  = F3( 0.32140077f, 0.55410134f, 0.76790185f );
+            const float ay = dot( a, y );
+            const f3    xi = a - y * ay;
+            return atan2f( dot( cross( xi, t ), y ), dot( xi, t ) );
+        }
+
+        // tangent-angle change against the frame field along the arc [st, st + ln] of C,
+        // traversed with the region on its left (decreasing phi: the cap lies towards w)
+        __device__ __forceinline__ float arc_turn( const Circ & C, float st, float ln )
+        {
+            float s0, c0, s1, c1;
+            sincosf( st + ln, &s0, &c0 );
+            sincosf( st, &s1, &c1 );
+            const f3 y0 = C.w * C.c + ( C.e1 * c0 + C.e2 * s0 ) * C.s, t0 = C.e1 * s0 - C.e2 * c0;
+            const f3 y1 = C.w * C.c + ( C.e1 * c1 + C.e2 * s1 ) * C.s, t1 = C.e1 * s1 - C.e2 * c1;
+            return frame_angle( y1, t1 ) - frame_angle( y0, t0 );
+        }
+
+        // Walks the allowed arcs (gaps between the cuts) of circle C; calls
+        // on_arc(start, length, na, nb) for each (na, nb: the constraints whose cuts
+        // bound it, -1 for a whole circle) and returns the circle's Gauss-Bonnet terms:
+        // c dphi plus the frame-relative tangent turn of every arc. Corners need no
+        // partner: the arcs that meet at a corner share its point, so their frame
+        // angles add up to its turning angle. An end strictly inside another cut is
+        // covered (lengths re-measured from the rounded ends, so that equal ends
+        // compare equal); of equal uncovered ends the first one counts.
+        template<class OnArc>
+        __device__ float circle_arcs( const Circ & C, Cuts & X, OnArc on_arc )
+        {
+            const int nIv = X.count;
+            if ( nIv == 0 )
+            {
+                on_arc( 0.f, k2PiF, -1, -1 );
+                return C.c * k2PiF;
+            }
+            for ( int q = 0; q < nIv; q++ )
+            {
+                X.ev[ q ]        = wrapf( X.s[ q ] + X.l[ q ] );
+                const float len2 = wrapf( X.ev[ q ] - X.s[ q ] );
+                X.el[ q ]        = len2 >= 0.5f * X.l[ q ] ? len2 : X.l[ q ];
+            }
+            float total = 0.f;
+            for ( int a = 0; a < nIv; a++ )
+            {
+                const float end  = X.ev[ a ];
+                bool        skip = false;
+                for ( int b = 0; b < nIv && !skip; b++ )
+                    skip = b != a && wrapf( end - X.s[ b ] ) < X.el[ b ];
+                if ( skip )
+                    continue;
+                // an equal end of an earlier uncovered cut already walks this gap
+                for ( int b = 0; b < a && !skip; b++ )
+                {
+                    if ( X.ev[ b ] != end )
+                        continue;
+                    bool covb = false;
+                    for ( int q = 0; q < nIv && !covb; q++ )
+                        covb = q != b && wrapf( X.ev[ b ] - X.s[ q ] ) < X.el[ q ];
+                    skip = !covb;
+                }
+                if ( skip )
+                    continue;
+                float gap = k2PiF;
+                int   nb  = -1;
+                for ( int b = 0; b < nIv; b++ )
+                {
+                    const float g = wrapf( X.s[ b ] - end );
+                    if ( g > 0.f && ( nb < 0 || g < gap ) )
+                    {
+                        gap = g;
+                        nb  = b;
+                    }
+                }
+                if ( nb < 0 )
+                    continue;
+                total += C.c * gap + arc_turn( C, end, gap );
+                on_arc( end, gap, (int)X.n[ a ], (int)X.n[ nb ] );
+            }
+            return total;
+        }
+
+        // One region of the unit sphere, held by a warp: constraints cons[0, M) in
+        // shared memory; each lane takes circles m = lane, lane + 32, ...; the three
+        // lunes add their two planes. per_arc(m, C, start, len, na, nb) is called for
+        // every allowed arc of an original circle. Returns the area (all lanes).
+        template<class PerArc>
+        __device__ float region_area_warp( const float4 * cons, int M, uint32_t & overflow, PerArc per_arc )
+        {
+            const uint32_t lane = lane_id();
+            float          tot[ 3 ] = { 0.f, 0.f, 0.f };
+            bool           empty    = false;
+            for ( int m = (int)lane; m < M; m += 32 )
+                if ( !( cons[ m ].w > -1.f ) )
+                    empty = true;
+            if ( __any_sync( 0xffffffffu, empty ) )
+                return 0.f;
+            Cuts X;
+            // the original circles, each over the three lunes
+            for ( int m = (int)lane; m < M; m += 32 )
+            {
+                const float4 km = cons[ m ];
+                if ( !( km.w < 1.f ) )
+                    continue;
+                const Circ C    = circ_of( km );
+                bool       gone = false;
+                int        nIv  = 0;
+                for ( int n = 0; n < M && !gone; n++ )
+                {
+                    if ( n == m )
+                        continue;
+                    const float4 kn = cons[ n ];
+                    if ( kn.x == km.x && kn.y == km.y && kn.z == km.z && kn.w == km.w )
+                    {
+                        gone = n < m; // the same constraint twice: the first keeps the circle
+                        continue;
+                    }
+                    float      st, ln;
+                    const int  r = cut_of( C, kn, st, ln );
+                    if ( r == 2 )
+                        gone = true;
+                    else if ( r == 1 )
+                    {
+                        if ( nIv < kAreaIv - 2 )
+                        {
+                            X.s[ nIv ] = st, X.l[ nIv ] = ln, X.n[ nIv ] = (uint16_t)n;
+                            nIv++;
+                        }
+                        else
+                            overflow = 1;
+                    }
+                }
+                if ( gone )
+                    continue;
+                for ( int L = 0; L < 3; L++ )
+                {
+                    X.count = nIv;
+                    bool out = false;
+                    for ( int side = 0; side < 2; side++ )
+                    {
+                        float     st, ln;
+                        const int r = cut_of( C, lune_cons( L, side ), st, ln );
+                        if ( r == 2 )
+                            out = true;
+                        else if ( r == 1 )
+                        {
+                            X.s[ X.count ] = st, X.l[ X.count ] = ln, X.n[ X.count ] = (uint16_t)( M + side );
+                            X.count++;
+                        }
+                    }
+                    if ( out )
+                        continue;
+                    tot[ L ] += circle_arcs( C, X, [ & ]( float st, float ln, int na, int nb ) { per_arc( m, C, st, ln, na, nb ); } );
+                }
+            }
+            // the lune planes: six circles, lanes 0..5
+            if ( lane < 6 )
+            {
+                const int L = (int)lane >> 1, side = (int)lane & 1;
+                const Circ C    = circ_of( lune_cons( L, side ) );
+                bool       gone = false;
+                int        nIv  = 0;
+                for ( int n = 0; n <= M && !gone; n++ )
+                {
+                    const float4 kn = n < M ? cons[ n ] : lune_cons( L, 1 - side );
+                    float        st, ln;
+                    const int    r = cut_of( C, kn, st, ln );
+                    if ( r == 2 )
+                        gone = true;
+                    else if ( r == 1 )
+                    {
+                        if ( nIv < kAreaIv )
+                        {
+                            X.s[ nIv ] = st, X.l[ nIv ] = ln, X.n[ nIv ] = (uint16_t)( n < M ? n : M + ( 1 - side ) );
+                            nIv++;
+                        }
+                        else
+                            overflow = 1;
+                    }
+                }
+                if ( !gone )
+                {
+                    X.count = nIv;
+                    tot[ L ] += circle_arcs( C, X, []( float, float, int, int ) {} );
+                }
+            }
+            float area = 0.f;
+            for ( int L = 0; L < 3; L++ )
+            {
+                float t = tot[ L ];
+                for ( int o = 16; o > 0; o >>= 1 )
+                    t += __shfl_xor_sync( 0xffffffffu, t, o );
+                // the sum spans many turns: reduce it with a full modulo
+                float r = fmodf( t, k2PiF );
+                if ( r < 0.f )
+                    r += k2PiF;
+                if ( r > 5.f * kPiF / 3.f )
+                    r -= k2PiF; // a piece of (nearly) zero area
+                area += fmaxf( r, 0.f );
+            }
+            return area;
+        }
+
+        // integral of y over the arc [st, st + ln] of C
+        __device__ __forceinline__ f3 arc_integral( const Circ & C, float st, float ln )
+        {
+            float s0, c0, s1, c1;
+            sincosf( st, &s0, &c0 );
+            sincosf( st + ln, &s1, &c1 );
+            return C.w * ( C.c * ln ) + ( C.e1 * ( s1 - s0 ) - C.e2 * ( c1 - c0 ) ) * C.s;
+        }
+
+        // Pair constraint of atom i and neighbour j: w = D / d, c = (R_i^2 - R_j^2 + d^2) / (2 d R_i).
+        struct PairGeo
+        {
+            f3    D;
+            float d, Ri, Rj;
+        };
+        __device__ __forceinline__ float4 pair_cons( const PairGeo & p )
+        {
+            if ( !( p.d > 0.f ) )
+                return make_float4( 0.f, 0.f, 1.f, 2.f ); // coincident centres: ignored
+            const f3 w = p.D * ( 1.f / p.d );
+            return make_float4( w.x, w.y, w.z, ( p.Ri * p.Ri - p.Rj * p.Rj + p.d * p.d ) / ( 2.f * p.d * p.Ri ) );
+        }
+
+        // toroidal patch per unit angle (rp times the integral of max(0, rho - rp cos beta)
+        // over [beta_i, beta_j]) and its derivatives by (d, R_i, R_j)
+        __device__ __forceinline__ float torus_F( float d, float Ri, float Rj, float rp, float dF[ 3 ] )
+        {
+            const float hi = ( Ri * Ri - Rj * Rj + d * d ) / ( 2.f * d ), hj = d - hi;
+            const float rr = Ri * Ri - hi * hi;
+            dF[ 0 ] = dF[ 1 ] = dF[ 2 ] = 0.f;
+            if ( !( rr > 0.f ) )
+                return 0.f;
+            const float rho = sqrtf( rr );
+            const float bi = -atan2f( hi, rho ), bj = atan2f( hj, rho );
+            float       F  = rho * ( bj - bi ) - rp * ( hj / Rj + hi / Ri );
+            float       Fr = ( bj - bi ) - rho * ( hj / ( Rj * Rj ) + hi / ( Ri * Ri ) )
+                       + rp * rho * ( hj / ( Rj * Rj * Rj ) + hi / ( Ri * Ri * Ri ) );
+            const float Fhi = ( rho * rho / ( Ri * Ri ) ) * ( 1.f - rp / Ri );
+            const float Fhj = ( rho * rho / ( Rj * Rj ) ) * ( 1.f - rp / Rj );
+            if ( rho < rp && hi > 0.f && hj > 0.f )
+            {
+                const float b0 = acosf( rho / rp );
+                F -= 2.f * rho * b0 - 2.f * rp * sqrtf( ( 1.f - rho / rp ) * ( 1.f + rho / rp ) );
+                Fr -= 2.f * b0;
+            }
+            const float rd = -hi * hj / ( d * rho ), rRi = Ri * hj / ( d * rho ), rRj = Rj * hi / ( d * rho );
+            dF[ 0 ] = rp * ( Fr * rd + Fhi * ( hj / d ) + Fhj * ( hi / d ) );
+            dF[ 1 ] = rp * ( Fr * rRi + Fhi * ( Ri / d ) - Fhj * ( Ri / d ) );
+            dF[ 2 ] = rp * ( Fr * rRj - Fhi * ( Rj / d ) + Fhj * ( Rj / d ) );
+            return rp * F;
+        }
+
+        __device__ __forceinline__ void add4( float * g, uint32_t a, f3 v, float r )
+        {
+            atomicAdd( g + 4 * (size_t)a + 0, v.x );
+            atomicAdd( g + 4 * (size_t)a + 1, v.y );
+            atomicAdd( g + 4 * (size_t)a + 2, v.z );
+            if ( r != 0.f )
+                atomicAdd( g + 4 * (size_t)a + 3, r );
+        }
+
+        struct AreaSmem
+        {
+            float4 cons[ kAreaNbr ];
+            float  dphi[ kAreaNbr ];
+            float4 iy[ kAreaNbr ];
+            float  gc[ kAreaNbr ];
+            float4 gw[ kAreaNbr ];
+            float  dist[ kAreaNbr ];
+            float  Rn[ kAreaNbr ];
+        };
+
+        // Warp per atom: convex patch and the tori of its circles (i, j), i < j.
+        // parts (double[3]) accumulate convex, toroidal (and concave in k_area_probes);
+        // atomArea (input order) receives convex + half of each torus. With kGrad,
+        // gradSorted (float4 per sorted atom) accumulates gConvex d convex + gTorus d tori.
+        template<bool kGrad>
+        __global__ void __launch_bounds__( 32 * kAreaWarps ) k_area_atoms( Build b, double * parts, float * atomArea,
+                                                                             float gConvex, float gTorus, float * gradSorted )
+        {
+            __shared__ AreaSmem sm[ kAreaWarps ];
+            const uint32_t      warp = threadIdx.x >> 5, lane = lane_id();
+            AreaSmem &          S    = sm[ warp ];
+            double              convexSum = 0.0, torusSum = 0.0;
+            uint32_t            overflow = 0;
+            for ( uint32_t i = blockIdx.x * kAreaWarps + warp; i < b.n; i += gridDim.x * kAreaWarps )
+            {
+                const float4   ai = b.atoms[ i ];
+                const float    Ri = ai.w + b.rp, ri = ai.w;
+                const uint32_t ni = b.nbrCount[ i ];
+                const size_t   row = (size_t)i * b.cap;
+                // an atom whose circles are all buried has no accessible patch
+                bool open = false;
+                for ( uint32_t s = lane; s < ni; s += 32 )
+                    open |= b.status[ row + s ] != 0;
+                if ( ni > 0 && !__any_sync( 0xffffffffu, open ) )
+                    continue;
+                if ( ni > (uint32_t)kAreaNbr )
+                {
+                    overflow = 1;
+                    continue;
+                }
+                const int M = (int)ni;
+                for ( int m = (int)lane; m < M; m += 32 )
+                {
+                    const float4 aj = b.atoms[ b.nbr[ row + m ] ];
+                    PairGeo      p;
+                    p.D          = F3( aj.x - ai.x, aj.y - ai.y, aj.z - ai.z );
+                    p.d          = sqrtf( dot( p.D, p.D ) );
+                    p.Ri         = Ri;
+                    p.Rj         = aj.w + b.rp;
+                    S.cons[ m ]  = pair_cons( p );
+                    S.dist[ m ]  = p.d;
+                    S.Rn[ m ]    = p.Rj;
+                    S.dphi[ m ]  = 0.f;
+                    S.iy[ m ]    = make_float4( 0.f, 0.f, 0.f, 0.f );
+                    S.gc[ m ]    = 0.f;
+                    S.gw[ m ]    = make_float4( 0.f, 0.f, 0.f, 0.f );
+                }
+                __syncwarp();
+                const float U = region_area_warp( S.cons, M, overflow, [ & ]( int m, const Circ & C, float st, float ln, int na, int nb ) {
+                    // the lane that owns circle m is the only writer of its sums
+                    S.dphi[ m ] += ln;
+                    if ( !kGrad )
+                        return;
+                    const f3 I = arc_integral( C, st, ln );
+                    S.iy[ m ].x += I.x, S.iy[ m ].y += I.y, S.iy[ m ].z += I.z;
+                    const uint32_t j = b.nbr[ row + m ];
+                    if ( !( j > i ) || !( S.dist[ m ] > 0.f ) )
+                        return;
+                    // angle part of the torus of (i, j): its arc ends move with the circles
+                    float       dF[ 3 ];
+                    const float G = gTorus * torus_F( S.dist[ m ], Ri, S.Rn[ m ], b.rp, dF );
+                    for ( int e = 0; e < 2; e++ )
+                    {
+                        const int nn = e == 0 ? na : nb;
+                        if ( nn < 0 || nn >= M )
+                            continue; // whole circle, or a cut between lunes
+                        const float  phi = e == 0 ? st : st + ln;
+                        const f3     y   = point_at( C, phi );
+                        const f3     yc  = y - C.w * C.c;
+                        const float4 kn  = S.cons[ nn ];
+                        const f3     wn  = F3( kn.x, kn.y, kn.z );
+                        const float  tw  = dot( cross( C.w, yc ), wn );
+                        if ( !( fabsf( tw ) > 0.f ) )
+                            continue;
+                        const float coef = ( e == 0 ? -G : G ) / tw;
+                        const float wwn  = dot( C.w, wn );
+                        atomicAdd( &S.gc[ nn ], coef );
+                        atomicAdd( &S.gw[ nn ].x, -coef * y.x );
+                        atomicAdd( &S.gw[ nn ].y, -coef * y.y );
+                        atomicAdd( &S.gw[ nn ].z, -coef * y.z );
+                        const f3 gwm = ( wn * C.c - yc * wwn ) * ( -coef );
+                        atomicAdd( &S.gc[ m ], -coef * ( wwn - ( C.c / ( C.s * C.s ) ) * dot( yc, wn ) ) );
+                        atomicAdd( &S.gw[ m ].x, gwm.x );
+                        atomicAdd( &S.gw[ m ].y, gwm.y );
+                        atomicAdd( &S.gw[ m ].z, gwm.z );
+                    }
+                } );
+                __syncwarp();
+                float mine = 0.f, tori = 0.f;
+                f3    gi   = F3( 0.f, 0.f, 0.f );
+                float gRi  = 0.f;
+                for ( int m = (int)lane; m < M; m += 32 )
+                {
+                    const uint32_t j = b.nbr[ row + m ];
+                    if ( j > i && S.dphi[ m ] > 0.f && S.dist[ m ] > 0.f )
+                    {
+                        float       dF[ 3 ];
+                        const float F = torus_F( S.dist[ m ], Ri, S.Rn[ m ], b.rp, dF );
+                        const float T = F * S.dphi[ m ];
+                        tori += T;
+                        mine += 0.5f * T;
+                        if ( atomArea )
+                            atomicAdd( atomArea + b.perm[ j ], 0.5f * T );
+                        if ( kGrad )
+                        {
+                            const float4 k  = S.cons[ m ];
+                            const f3     w  = F3( k.x, k.y, k.z );
+                            const float  gs = gTorus * S.dphi[ m ];
+                            add4( gradSorted, j, w * ( gs * dF[ 0 ] ), gs * dF[ 2 ] );
+                            gi  = gi - w * ( gs * dF[ 0 ] );
+                            gRi += gs * dF[ 1 ];
+                        }
+                    }
+                    if ( kGrad && S.dist[ m ] > 0.f )
+                    {
+                        // convex part and the angle parts gathered above, through (w, c) of the pair
+                        const float4 k   = S.cons[ m ];
+                        const f3     w   = F3( k.x, k.y, k.z );
+                        const float  d   = S.dist[ m ], Rj = S.Rn[ m ];
+                        const float  gc  = S.gc[ m ] + gConvex * ri * ri * S.dphi[ m ];
+                        const f3     gw  = F3( S.gw[ m ].x, S.gw[ m ].y, S.gw[ m ].z ) - F3( S.iy[ m ].x, S.iy[ m ].y, S.iy[ m ].z ) * ( gConvex * ri * ri );
+                        const float  dcd = 1.f / ( 2.f * Ri ) - ( Ri * Ri - Rj * Rj ) / ( 2.f * d * d * Ri );
+                        const float  dcRi = ( Ri * Ri + Rj * Rj - d * d ) / ( 2.f * d * Ri * Ri );
+                        const float  dcRj = -Rj / ( d * Ri );
+                        const f3     gD   = ( gw - w * dot( gw, w ) ) * ( 1.f / d ) + w * ( gc * dcd );
+                        add4( gradSorted, j, gD, gc * dcRj );
+                        gi  = gi - gD;
+                        gRi += gc * dcRi;
+                    }
+                }
+                for ( int o = 16; o > 0; o >>= 1 )
+                {
+                    mine += __shfl_xor_sync( 0xffffffffu, mine, o );
+                    tori += __shfl_xor_sync( 0xffffffffu, tori, o );
+                    if ( kGrad )
+                    {
+                        gi.x += __shfl_xor_sync( 0xffffffffu, gi.x, o );
+                        gi.y += __shfl_xor_sync( 0xffffffffu, gi.y, o );
+                        gi.z += __shfl_xor_sync( 0xffffffffu, gi.z, o );
+                        gRi += __shfl_xor_sync( 0xffffffffu, gRi, o );
+                    }
+                }
+                const float cA = ri * ri * U;
+                if ( lane == 0 )
+                {
+                    convexSum += cA;
+                    torusSum += tori;
+                    if ( atomArea )
+                        atomicAdd( atomArea + b.perm[ i ], cA + mine );
+                    if ( kGrad )
+                        add4( gradSorted, i, gi, gRi + gConvex * 2.f * ri * U );
+                }
+                __syncwarp();
+            }
+            if ( lane == 0 )
+            {
+                if ( parts && convexSum != 0.0 )
+                    atomicAdd( parts + 0, convexSum );
+                if ( parts && torusSum != 0.0 )
+                    atomicAdd( parts + 1, torusSum );
+            }
+            overflow = __any_sync( 0xffffffffu, overflow != 0 );
+            if ( lane == 0 && overflow )
+                atomicOr( &b.counts->overflow, (uint32_t)kOverflowArea );
+        }
+
+        struct ProbeAreaSmem
+        {
+            float4 cons[ kProbeCons ];
+            float  dphi[ kProbeCons ];
+            float4 iy[ kProbeCons ];
+            float  dist[ kProbeCons ];
+            uint32_t nq[ kProbeCons ];
+        };
+
+        // Warp per probe: its concave triangle outside the listed neighbour probes.
+        // With kGrad, probeGrad (float4 per probe) accumulates d/d(position) of every
+        // probe involved and gradSorted the direct terms of the contact directions.
+        template<bool kGrad>
+        __global__ void __launch_bounds__( 32 * kAreaWarps ) k_area_probes( Build b, double * parts, float * atomArea,
+                                                                              float gConcave, float * gradSorted, float4 * probeGrad )
+        {
+            __shared__ ProbeAreaSmem sm[ kAreaWarps ];
+            const uint32_t           warp = threadIdx.x >> 5, lane = lane_id();
+            ProbeAreaSmem &          S    = sm[ warp ];
+            const uint32_t           I    = min( b.counts->I, b.capProbes );
+            const uint32_t           Q    = min( b.counts->Q, b.capProbes );
+            const float              rp   = b.rp;
+            double                   concaveSum = 0.0;
+            uint32_t                 overflow   = 0;
+            for ( uint32_t p = blockIdx.x * kAreaWarps + warp; p < I; p += gridDim.x * kAreaWarps )
+            {
+                const int4   id = b.probeIds[ p ];
+                const float4 pp = b.probePos[ p ];
+                const f3     P  = F3( pp.x, pp.y, pp.z );
+                f3           v[ 3 ];
+                float        Lv[ 3 ];
+                const int    ia[ 3 ] = { id.x, id.y, id.z };
+                for ( int a = 0; a < 3; a++ )
+                {
+                    const float4 c = b.atoms[ ia[ a ] ];
+                    const f3     D = F3( c.x - P.x, c.y - P.y, c.z - P.z );
+                    Lv[ a ]        = sqrtf( dot( D, D ) );
+                    v[ a ]         = D * ( 1.f / Lv[ a ] );
+                }
+                f3    u[ 3 ];
+                float ul[ 3 ], sg[ 3 ];
+                bool  flat = false;
+                for ( int e = 0; e < 3; e++ )
+                {
+                    u[ e ]           = cross( v[ e ], v[ ( e + 1 ) % 3 ] );
+                    ul[ e ]          = sqrtf( dot( u[ e ], u[ e ] ) );
+                    const float side = dot( u[ e ], v[ ( e + 2 ) % 3 ] );
+                    flat |= !( ul[ e ] > 0.f ) || side == 0.f;
+                    sg[ e ] = side > 0.f ? 1.f : -1.f;
+                }
+                if ( flat )
+                    continue; // a flat triangle has no area
+                const uint32_t cnt = p < Q ? min( (uint32_t)id.w, kMaxProbeNbr ) : 0u;
+                const int      M   = 3 + (int)cnt;
+                if ( lane < 3 )
+                {
+                    const f3 w     = u[ lane ] * ( -sg[ lane ] / ul[ lane ] );
+                    S.cons[ lane ] = make_float4( w.x, w.y, w.z, 0.f );
+                }
+                // neighbour caps at 3 .. M - 1 (up to 35 constraints: lane + 3 covers them in one pass)
+                if ( lane < cnt )
+                {
+                    const int      m  = 3 + (int)lane;
+                    const uint32_t q  = b.probeNbrIdx[ (size_t)p * kMaxProbeNbr + lane ];
+                    const float4   pq = b.probePos[ q ];
+                    const f3       D  = F3( pq.x - P.x, pq.y - P.y, pq.z - P.z );
+                    const float    L  = sqrtf( dot( D, D ) );
+                    S.dist[ m ]       = L;
+                    S.nq[ m ]         = q;
+                    if ( L > 0.f && L < 2.f * rp )
+                    {
+                        const f3 w  = D * ( 1.f / L );
+                        S.cons[ m ] = make_float4( w.x, w.y, w.z, L / ( 2.f * rp ) );
+                    }
+                    else
+                        S.cons[ m ] = make_float4( 0.f, 0.f, 1.f, 2.f ); // vacuous
+                }
+                for ( int m = (int)lane; m < M; m += 32 )
+                {
+                    S.dphi[ m ] = 0.f;
+                    S.iy[ m ]   = make_float4( 0.f, 0.f, 0.f, 0.f );
+                }
+                __syncwarp();
+                const float U = region_area_warp( S.cons, M, overflow, [ & ]( int m, const Circ & C, float st, float ln, int, int ) {
+                    if ( !kGrad )
+                        return;
+                    S.dphi[ m ] += ln;
+                    const f3 Iy = arc_integral( C, st, ln );
+                    S.iy[ m ].x += Iy.x, S.iy[ m ].y += Iy.y, S.iy[ m ].z += Iy.z;
+                } );
+                __syncwarp();
+                const float cA = rp * rp * U;
+                if ( lane == 0 )
+                {
+                    concaveSum += cA;
+                    if ( atomArea )
+                        for ( int a = 0; a < 3; a++ )
+                            atomicAdd( atomArea + b.perm[ ia[ a ] ], cA * ( 1.f / 3.f ) );
+                }
+                if ( kGrad )
+                {
+                    const float k2 = gConcave * rp * rp;
+                    f3          gP = F3( 0.f, 0.f, 0.f );
+                    if ( lane == 0 )
+                    {
+                        f3 gv[ 3 ] = { F3( 0.f, 0.f, 0.f ), F3( 0.f, 0.f, 0.f ), F3( 0.f, 0.f, 0.f ) };
+                        for ( int e = 0; e < 3; e++ )
+                        {
+                            const f3  gw = F3( S.iy[ e ].x, S.iy[ e ].y, S.iy[ e ].z ) * ( -k2 );
+                            const f3  wh = u[ e ] * ( 1.f / ul[ e ] );
+                            const f3  gu = ( gw - wh * dot( gw, wh ) ) * ( -sg[ e ] / ul[ e ] );
+                            const int a = e, c2 = ( e + 1 ) % 3;
+                            gv[ a ]     = gv[ a ] + cross( v[ c2 ], gu );
+                            gv[ c2 ]    = gv[ c2 ] + cross( gu, v[ a ] );
+                        }
+                        for ( int a = 0; a < 3; a++ )
+                        {
+                            const f3 gD = ( gv[ a ] - v[ a ] * dot( gv[ a ], v[ a ] ) ) * ( 1.f / Lv[ a ] );
+                            add4( gradSorted, (uint32_t)ia[ a ], gD, 0.f );
+                            gP = gP - gD;
+                        }
+                    }
+                    if ( lane < cnt )
+                    {
+                        const int   m = 3 + (int)lane;
+                        const float L = S.dist[ m ];
+                        if ( L > 0.f && L < 2.f * rp )
+                        {
+                            const float4 k  = S.cons[ m ];
+                            const f3     w  = F3( k.x, k.y, k.z );
+                            const f3     gw = F3( S.iy[ m ].x, S.iy[ m ].y, S.iy[ m ].z ) * ( -k2 );
+                            const float  gc = k2 * S.dphi[ m ];
+                            const f3     gD = ( gw - w * dot( gw, w ) ) * ( 1.f / L ) + w * ( gc / ( 2.f * rp ) );
+                            gP              = gP - gD;
+                            atomicAdd( &probeGrad[ S.nq[ m ] ].x, gD.x );
+                            atomicAdd( &probeGrad[ S.nq[ m ] ].y, gD.y );
+                            atomicAdd( &probeGrad[ S.nq[ m ] ].z, gD.z );
+                        }
+                    }
+                    for ( int o = 16; o > 0; o >>= 1 )
+                    {
+                        gP.x += __shfl_xor_sync( 0xffffffffu, gP.x, o );
+                        gP.y += __shfl_xor_sync( 0xffffffffu, gP.y, o );
+                        gP.z += __shfl_xor_sync( 0xffffffffu, gP.z, o );
+                    }
+                    if ( lane == 0 )
+                    {
+                        atomicAdd( &probeGrad[ p ].x, gP.x );
+                        atomicAdd( &probeGrad[ p ].y, gP.y );
+                        atomicAdd( &probeGrad[ p ].z, gP.z );
+                    }
+                }
+                __syncwarp();
+            }
+            if ( lane == 0 && parts && concaveSum != 0.0 )
+                atomicAdd( parts + 2, concaveSum );
+            overflow = __any_sync( 0xffffffffu, overflow != 0 );
+            if ( lane == 0 && overflow )
+                atomicOr( &b.counts->overflow, (uint32_t)kOverflowArea );
+        }
+
+        // probe positions follow their atoms: M^T lambda = g with rows p - c_a;
+        // d/dc_a = lambda_a (p - c_a), d/dR_a = lambda_a R_a
+        __global__ void k_area_probe_back( Build b, const float4 * probeGrad, float * gradSorted )
+        {
+            const uint32_t I = min( b.counts->I, b.capProbes );
+            for ( uint32_t p = blockIdx.x * blockDim.x + threadIdx.x; p < I; p += gridDim.x * blockDim.x )
+            {
+                const float4 g4 = probeGrad[ p ];
+                if ( g4.x == 0.f && g4.y == 0.f && g4.z == 0.f )
+                    continue;
+                const f3     g  = F3( g4.x, g4.y, g4.z );
+                const int4   id = b.probeIds[ p ];
+                const float4 pp = b.probePos[ p ];
+                const int    ia[ 3 ] = { id.x, id.y, id.z };
+                f3           r[ 3 ];
+                float        R[ 3 ];
+                for ( int k = 0; k < 3; k++ )
+                {
+                    const float4 c = b.atoms[ ia[ k ] ];
+                    r[ k ]         = F3( pp.x - c.x, pp.y - c.y, pp.z - c.z );
+                    R[ k ]         = c.w + b.rp;
+                }
+                const float det = dot( r[ 0 ], cross( r[ 1 ], r[ 2 ] ) );
+                if ( !( fabsf( det ) > 0.f ) )
+                    continue;
+                const float lam[ 3 ] = { dot( g, cross( r[ 1 ], r[ 2 ] ) ) / det, dot( r[ 0 ], cross( g, r[ 2 ] ) ) / det,
+                                         dot( r[ 0 ], cross( r[ 1 ], g ) ) / det };
+                for ( int k = 0; k < 3; k++ )
+                    add4( gradSorted, (uint32_t)ia[ k ], r[ k ] * lam[ k ], lam[ k ] * R[ k ] );
+            }
+        }
+
+        __global__ void k_area_unsort( Build b, const float * gradSorted, float * gradInput )
+        {
+            for ( uint32_t s = blockIdx.x * blockDim.x + threadIdx.x; s < b.n; s += gridDim.x * blockDim.x )
+            {
+                const uint32_t i = b.perm[ s ];
+                for ( int k = 0; k < 4; k++ )
+                    gradInput[ 4 * (size_t)i + k ] = gradSorted[ 4 * (size_t)s + k ];
+            }
+        }
+
+        inline uint32_t area_blocks( uint64_t items )
+        {
+            const uint64_t want = ( items + kAreaWarps - 1 ) / kAreaWarps;
+            const uint64_t cap  = 152ull * 16ull;
+            return (uint32_t)( want < 1 ? 1 : ( want < cap ? want : cap ) );
+        }
+    } // namespace
+
+    size_t area_scratch_bytes( const Build & b ) { return sizeof( float4 ) * (size_t)b.capProbes + 256; }
+
+    void launch_area( const Build & b, double * parts, float * atomArea, cudaStream_t s )
+    {
+        cudaMemsetAsync( parts, 0, 3 * sizeof( double ), s );
+        if ( atomArea )
+            cudaMemsetAsync( atomArea, 0, sizeof( float ) * (size_t)b.n, s );
+        if ( !b.n )
+            return;
+        k_area_atoms<false><<<area_blocks( b.n ), 32 * kAreaWarps, 0, s>>>( b, parts, atomArea, 0.f, 0.f, nullptr );
+        k_area_probes<false><<<area_blocks( b.capProbes ), 32 * kAreaWarps, 0, s>>>( b, parts, atomArea, 0.f, nullptr, nullptr );
+        count_launches( 2 );
+    }
+
+    void launch_area_backward( const Build & b, const float gParts[ 3 ], float * gradSorted, float * gradInput, void * scratch,
+                               cudaStream_t s )
+    {
+        cudaMemsetAsync( gradSorted, 0, sizeof( float ) * 4 * (size_t)b.n, s );
+        if ( !b.n )
+        {
+            return;
+        }
+        float4 * probeGrad = static_cast<float4 *>( scratch );
+        cudaMemsetAsync( probeGrad, 0, sizeof( float4 ) * (size_t)b.capProbes, s );
+        k_area_atoms<true><<<area_blocks( b.n ), 32 * kAreaWarps, 0, s>>>( b, nullptr, nullptr, gParts[ 0 ], gParts[ 1 ], gradSorted );
+        k_area_probes<true><<<area_blocks( b.capProbes ), 32 * kAreaWarps, 0, s>>>( b, nullptr, nullptr, gParts[ 2 ], gradSorted, probeGrad );
+        k_area_probe_back<<<min( 152u * 8u, ( b.capProbes + 255 ) / 256 + 1 ), 256, 0, s>>>( b, probeGrad, gradSorted );
+        k_area_unsort<<<( b.n + 255 ) / 256, 256, 0, s>>>( b, gradSorted, gradInput );
+        count_launches( 4 );
+    }
+} // namespace sesgb

@@ -54,6 +54,7 @@ namespace sesgb
         kOverflowVisBand    = 1u << 11, // more visibility tests in the float32 band than the queue holds
         kOverflowPairs      = 1u << 12, // more neighbour pairs than the touch-mask buffer holds
         kOverflowSdfList    = 1u << 13, // a query point had more atoms within reach than the SDF search holds
+        kOverflowArea       = 1u << 14, // an area region had more constraints or cuts than the kernel holds
     };
 
     enum Fp64Stage : uint32_t

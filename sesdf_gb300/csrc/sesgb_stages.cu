@@ -1863,7 +1863,8 @@ namespace sesgb
                     const uint32_t p  = (uint32_t)( buf[ warp ][ lane ] & 0xffffffffull );
                     const float4   pp = b.probePos[ b.nMol > 1 ? b.singList[ p ] : p ];
                     const float    wv = b.mode == 0 ? __fmul_rn( __fmul_rn( pq.x, pq.y ), pq.z ) : 0.f;
-                    b.probeNbrs[ (size_t)q * kMaxProbeNbr + lane ] = make_float4( pp.x, pp.y, pp.z, wv );
+                    b.probeNbrs[ (size_t)q * kMaxProbeNbr + lane ]   = make_float4( pp.x, pp.y, pp.z, wv );
+                    b.probeNbrIdx[ (size_t)q * kMaxProbeNbr + lane ] = p;
                 }
                 if ( lane == 0 )
                 {

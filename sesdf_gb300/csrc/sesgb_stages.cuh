@@ -96,6 +96,7 @@ namespace sesgb
         float4 *   probePos;  // capProbes: output positions
         int4 *     probeCid;  // capProbes: circle ids (full: partial-circle numbers; exterior: slots)
         float4 *   probeNbrs; // capProbes * 32
+        uint32_t * probeNbrIdx; // capProbes * 32: singular index of each listed neighbour
         uint32_t * ccount;    // C1 + 1
         uint32_t * cstart;    // C1 + 1
         uint32_t * ccursor;   // C1
@@ -127,6 +128,14 @@ namespace sesgb
                        cudaStream_t s );
     void   launch_sdf_backward( const Build & b, const float * queries, uint32_t m, float band, const float * gradSdf,
                                 float * gradSorted, float * gradInput, void * scratch, cudaStream_t s );
+    // SES area of the primitives of a full-surface build (sesgb_area.cu): parts (device
+    // double[3]: convex, toroidal, concave), atomArea (optional, float[n], input order)
+    size_t area_scratch_bytes( const Build & b );
+    void   launch_area( const Build & b, double * parts, float * atomArea, cudaStream_t s );
+    // gradient of gParts . parts into gradInput (float4[n], input order); gradSorted
+    // (float4[n]) and scratch (area_scratch_bytes) are work buffers
+    void launch_area_backward( const Build & b, const float gParts[ 3 ], float * gradSorted, float * gradInput, void * scratch,
+                               cudaStream_t s );
     void launch_neighbors( const Build & b, cudaStream_t s );
     void launch_visibility( const Build & b, cudaStream_t s );
     void launch_visibility_resolve( const Build & b, cudaStream_t s );

@@ -1,6 +1,8 @@
-"""Optional torch binding: the SES signed distance as a differentiable function.
+"""Optional torch binding: the SES signed distance and the SES area as differentiable
+functions.
 
     sdf = ses_sdf(atoms, queries, probe_radius=1.4)
+    area = ses_area(atoms, probe_radius=1.4)   # scalar tensor, A^2
 
 atoms is a CUDA float32 tensor [n, 4] (x, y, z, vdW radius), queries a CUDA
 float32 tensor [m, 3]. The forward pass builds the full surface (sesgb_build_device)
@@ -46,3 +48,35 @@ class SesSdf(torch.autograd.Function):
 
 def ses_sdf(atoms: torch.Tensor, queries: torch.Tensor, probe_radius: float = 1.4) -> torch.Tensor:
     return SesSdf.apply(atoms, queries, probe_radius)
+
+
+class SesArea(torch.autograd.Function):
+    """Total SES area of the build's primitives; backward: sesgb_ses_area_backward."""
+
+    @staticmethod
+    def forward(ctx, atoms: torch.Tensor, probe_radius: float = 1.4):
+        if not atoms.is_cuda or atoms.dtype != torch.float32 or atoms.dim() != 2 or atoms.shape[1] != 4:
+            raise ValueError("atoms must be a CUDA float32 tensor [n, 4]")
+        a = atoms.detach().contiguous()
+        stream = torch.cuda.current_stream().cuda_stream
+        g = SesBuild(a.cpu().numpy(), probe_radius, "full")
+        g.build_device(a.data_ptr(), stream)
+        area = g.ses_area(None, stream)["total"]
+        ctx.build = g
+        ctx.n = a.shape[0]
+        ctx.device = a.device
+        return torch.tensor(area, dtype=torch.float32, device=a.device)
+
+    @staticmethod
+    def backward(ctx, grad_out: torch.Tensor):
+        g = ctx.build
+        gs = float(grad_out.detach().cpu())
+        grad = torch.empty((ctx.n, 4), dtype=torch.float32, device=ctx.device)
+        g.ses_area_backward(grad.data_ptr(), (gs, gs, gs), torch.cuda.current_stream().cuda_stream)
+        torch.cuda.current_stream().synchronize()
+        g.close()
+        return grad, None
+
+
+def ses_area(atoms: torch.Tensor, probe_radius: float = 1.4) -> torch.Tensor:
+    return SesArea.apply(atoms, probe_radius)
