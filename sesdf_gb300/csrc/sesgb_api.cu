@@ -324,7 +324,7 @@ namespace
             const ScanJob jobs[] = { { b.singCnt, b.singOff, &d->Q }, { b.regCnt, b.regOff, &d->regTotal } };
             exclusive_scan_many( jobs, 2, n, nullptr, sc, s );
         }
-        cudaMemsetAsync( b.ccount, 0, sizeof( uint32_t ) * ( b.capC1 + 1ull ), s );
+        launch_zero2( b.ccount, b.ccursor, b.capC1, &d->C1, s ); // per-circle probe counts and list cursors
         launch_place( b, s );
         mark( 7 );
 
@@ -332,7 +332,6 @@ namespace
         if ( c->mode == SESGB_MODE_FULL )
         {
             exclusive_scan( b.ccount, b.cstart, b.capC1, &d->C1, nullptr, sc, s );
-            cudaMemsetAsync( b.ccursor, 0, sizeof( uint32_t ) * ( b.capC1 + 1ull ), s );
             launch_lists( b, s );
             launch_segment_counts( b, s );
             exclusive_scan( b.segCnt, b.segOff, b.capC1, &d->C1, &d->S, sc, s );

@@ -155,6 +155,16 @@ namespace sesgb
     }
 
     // ---- warp helpers -------------------------------------------------------
+    // Programmatic dependent launch: a kernel launched with
+    // cudaLaunchAttributeProgrammaticStreamSerialization right after another one
+    // has its launch prepared while that grid runs. It waits here, before it reads
+    // anything, until the previous grid has completed and its writes are visible (a
+    // no-op when there is no such grid). No kernel triggers its dependents early:
+    // measured on GB300, dependents scheduled at the start of a grid take SM slots
+    // from its last wave and the build gets 2 % slower, while the prepared launch
+    // alone saves about 1 %.
+    __device__ __forceinline__ void pdl_begin() { asm volatile( "griddepcontrol.wait;" ::: "memory" ); }
+
     __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
     __device__ __forceinline__ uint32_t lanemask_lt() { return ( 1u << lane_id() ) - 1u; }
 

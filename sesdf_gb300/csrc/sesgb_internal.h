@@ -7,6 +7,26 @@
 
 namespace sesgb
 {
+    // Launches kernel k on stream s as a programmatic dependent of the work before
+    // it: the grid may be scheduled while the previous kernel drains and waits in
+    // pdl_begin() for its completion. Captured into a CUDA graph, the dependency
+    // becomes a programmatic edge.
+    template<typename... P, typename... A>
+    inline void pdl_launch( void ( *k )( P... ), dim3 grid, dim3 block, size_t smem, cudaStream_t s, A... args )
+    {
+        cudaLaunchConfig_t  cfg {};
+        cudaLaunchAttribute attr[ 1 ];
+        attr[ 0 ].id                                         = cudaLaunchAttributeProgrammaticStreamSerialization;
+        attr[ 0 ].val.programmaticStreamSerializationAllowed = 1;
+        cfg.gridDim                                          = grid;
+        cfg.blockDim                                         = block;
+        cfg.dynamicSmemBytes                                 = smem;
+        cfg.stream                                           = s;
+        cfg.attrs                                            = attr;
+        cfg.numAttrs                                         = 1;
+        cudaLaunchKernelEx( &cfg, k, static_cast<P>( args )... );
+    }
+
     // Counters written by the kernels and read back once at the end of a build.
     struct DeviceCounts
     {

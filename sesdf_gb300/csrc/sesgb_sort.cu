@@ -62,6 +62,7 @@ namespace sesgb
         __global__ void __launch_bounds__( kScanThreads ) k_tile_sums( ScanArrays a, uint64_t nHost, const uint32_t * nDevice,
                                                                         uint32_t * tileSums, uint32_t tiles )
         {
+            pdl_begin();
             __shared__ uint32_t warpSums[ 33 ];
             const uint64_t      n    = scan_len( nHost, nDevice );
             const uint64_t      base = (uint64_t)blockIdx.x * kScanTile;
@@ -88,6 +89,7 @@ namespace sesgb
         __global__ void __launch_bounds__( kScanThreads ) k_tile_scan( ScanArrays a, uint64_t nHost, const uint32_t * nDevice,
                                                                         const uint32_t * tileSums, uint32_t tiles )
         {
+            pdl_begin();
             __shared__ uint32_t tile[ kScanTile + kScanTile / 32 ];
             __shared__ uint32_t warpSums[ 33 ];
             const uint64_t      n    = scan_len( nHost, nDevice );
@@ -165,6 +167,7 @@ namespace sesgb
         __global__ void __launch_bounds__( kRadixThreads ) k_radix_hist( const uint32_t * keys, uint32_t n, int shift,
                                                                           uint32_t * hist, uint32_t tiles )
         {
+            pdl_begin();
             __shared__ uint32_t h[ 256 ];
             h[ threadIdx.x ] = 0;
             __syncthreads();
@@ -183,6 +186,7 @@ namespace sesgb
                                                                              uint32_t * keysOut, uint32_t * valsOut, uint32_t n,
                                                                              int shift, const uint32_t * offsets, uint32_t tiles )
         {
+            pdl_begin();
             __shared__ uint32_t base[ 256 ];
             __shared__ uint32_t warpCount[ kRadixWarps ][ 256 ];
             const uint32_t      warp = threadIdx.x >> 5;
@@ -252,10 +256,10 @@ namespace sesgb
         uint32_t *     tileSums = static_cast<uint32_t *>( scratch );
         if ( tiles > 1 )
         {
-            k_tile_sums<<<grid, kScanThreads, 0, stream>>>( a, nHost, nDevice, tileSums, tiles );
+            pdl_launch( k_tile_sums, grid, kScanThreads, 0, stream, a, nHost, nDevice, tileSums, tiles );
             count_launches( 1 );
         }
-        k_tile_scan<<<grid, kScanThreads, 0, stream>>>( a, nHost, nDevice, tileSums, tiles );
+        pdl_launch( k_tile_scan, grid, kScanThreads, 0, stream, a, nHost, nDevice, tileSums, tiles );
         count_launches( 1 );
     }
     void exclusive_scan( const uint32_t * in, uint32_t * out, uint64_t nHost, const uint32_t * nDevice, uint32_t * total,
@@ -294,9 +298,9 @@ namespace sesgb
         int       passes = 0;
         for ( int shift = 0; shift < bits; shift += 8, passes++ )
         {
-            k_radix_hist<<<tiles, kRadixThreads, 0, stream>>>( ka, n, shift, histBuf, tiles );
+            pdl_launch( k_radix_hist, tiles, kRadixThreads, 0, stream, ka, n, shift, histBuf, tiles );
             exclusive_scan( histBuf, histBuf, hist, nullptr, nullptr, scanScratch, stream );
-            k_radix_scatter<<<tiles, kRadixThreads, 0, stream>>>( ka, va, kb, vb, n, shift, histBuf, tiles );
+            pdl_launch( k_radix_scatter, tiles, kRadixThreads, 0, stream, ka, va, kb, vb, n, shift, histBuf, tiles );
             count_launches( 2 );
             std::swap( ka, kb );
             std::swap( va, vb );

@@ -181,6 +181,7 @@ namespace sesgb
         // ------------------------------------------------------------------
         __global__ void k_hash( Build b )
         {
+            pdl_begin();
             const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
             if ( i >= b.n )
                 return;
@@ -198,6 +199,7 @@ namespace sesgb
         // thread per molecule: neighbour-grid geometry from the molecule's reference grid box
         __global__ void k_fine_params( Build b, float cutoff )
         {
+            pdl_begin();
             if ( cutoff < 0.f )
                 cutoff = 2.f * ( b.counts->rmax + b.rp ) + 0.01f;
             for ( uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < b.nMol; m += gridDim.x * blockDim.x )
@@ -228,8 +230,22 @@ namespace sesgb
             }
         }
 
+        // zeroes a[0, n] and c[0, n] (c may be null), n = min(*nDevice, nHost) or nHost
+        __global__ void k_zero2( uint32_t * a, uint32_t * c, uint32_t nHost, const uint32_t * nDevice )
+        {
+            pdl_begin();
+            const uint32_t n = ( nDevice ? min( *nDevice, nHost ) : nHost ) + 1u;
+            for ( uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x )
+            {
+                a[ q ] = 0u;
+                if ( c )
+                    c[ q ] = 0u;
+            }
+        }
+
         __global__ void k_gather( Build b )
         {
+            pdl_begin();
             const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
             if ( s >= b.n )
                 return;
@@ -264,6 +280,7 @@ namespace sesgb
 
         __global__ void k_cell_count( Build b, int kind, uint32_t nHost, const uint32_t * nDevice )
         {
+            pdl_begin();
             const uint32_t n = nDevice ? min( *nDevice, nHost ) : nHost;
             for ( uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x )
             {
@@ -275,6 +292,7 @@ namespace sesgb
 
         __global__ void k_cell_scatter( Build b, int kind, uint32_t nHost, const uint32_t * nDevice )
         {
+            pdl_begin();
             const uint32_t n = nDevice ? min( *nDevice, nHost ) : nHost;
             for ( uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < n; q += gridDim.x * blockDim.x )
             {
@@ -289,6 +307,7 @@ namespace sesgb
         // ---- neighbour lists ---------------------------------------------
         __global__ void __launch_bounds__( 32 * kWarpsPerBlock ) k_neighbors( Build b )
         {
+            pdl_begin();
             __shared__ uint32_t buf[ kWarpsPerBlock ][ kNbrBuf ];
             const uint32_t      warp = threadIdx.x >> 5, lane = lane_id();
             const uint32_t      i    = blockIdx.x * kWarpsPerBlock + warp;
@@ -477,6 +496,7 @@ namespace sesgb
 
         __global__ void __launch_bounds__( 32 * kWarpsPerBlock ) k_visibility( Build b )
         {
+            pdl_begin();
             extern __shared__ __align__( 16 ) unsigned char smemRaw[];
             const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
             const uint32_t i    = blockIdx.x * kWarpsPerBlock + warp;
@@ -689,6 +709,7 @@ namespace sesgb
         // result bits go into the circle's status flags.
         __global__ void __launch_bounds__( 128 ) k_visibility_band( Build b )
         {
+            pdl_begin();
             const uint32_t nb   = min( b.counts->visBand, b.capVisBand );
             uint32_t       fp64 = 0;
             for ( uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nb; t += gridDim.x * blockDim.x )
@@ -715,6 +736,7 @@ namespace sesgb
         // the per-atom counts; four atoms per warp, eight lanes per atom
         __global__ void __launch_bounds__( 32 * kWarpsPerBlock ) k_visibility_final( Build b )
         {
+            pdl_begin();
             const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
             const uint32_t grp = lane / 8, gl = lane % 8;
             const uint32_t i    = ( blockIdx.x * kWarpsPerBlock + warp ) * 4 + grp;
@@ -776,6 +798,7 @@ namespace sesgb
 
         __global__ void __launch_bounds__( 32 * kWarpsPerBlock ) k_emit( Build b )
         {
+            pdl_begin();
             const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
             const uint32_t grp = lane / kEmitGroup, gl = lane % kEmitGroup;
             const uint32_t gmask = ( ( 1u << kEmitGroup ) - 1u ) << ( grp * kEmitGroup );
@@ -1160,6 +1183,7 @@ namespace sesgb
         // chunk; positions and undecided flags are completed by k_probe_jobs.
         __global__ void __launch_bounds__( 32 * kProbeWarps, 8 ) k_probes( Build b )
         {
+            pdl_begin();
             extern __shared__ __align__( 16 ) unsigned char smemRaw[];
             const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
             const uint32_t i    = blockIdx.x * kProbeWarps + warp;
@@ -1481,6 +1505,7 @@ namespace sesgb
         // left open.
         __global__ void __launch_bounds__( 128 ) k_probe_jobs( Build b )
         {
+            pdl_begin();
             const uint32_t nFill = min( b.counts->jobs, b.capProbes );
             const uint32_t nBand = min( b.counts->bandJobs, b.capProbes - nFill );
             const double   rp    = (double)b.rp;
@@ -1556,6 +1581,7 @@ namespace sesgb
 
         __global__ void __launch_bounds__( 32 * kWarpsPerBlock ) k_place( Build b )
         {
+            pdl_begin();
             const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
             const uint32_t grp = lane / kPlaceGroup, gl = lane % kPlaceGroup;
             const uint32_t gmask = ( ( 1u << kPlaceGroup ) - 1u ) << ( grp * kPlaceGroup );
@@ -1624,6 +1650,7 @@ namespace sesgb
 
         __global__ void k_lists( Build b )
         {
+            pdl_begin();
             const uint32_t I = min( b.counts->I, b.capProbes );
             for ( uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < I; q += gridDim.x * blockDim.x )
             {
@@ -1640,6 +1667,7 @@ namespace sesgb
 
         __global__ void k_segment_counts( Build b )
         {
+            pdl_begin();
             const uint32_t C1 = min( b.counts->C1, b.capC1 );
             for ( uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < C1; t += gridDim.x * blockDim.x )
             {
@@ -1666,6 +1694,7 @@ namespace sesgb
         // kKeyTol, or a side test is ambiguous, the double-precision keys decide.
         __global__ void __launch_bounds__( 128 ) k_segments( Build b )
         {
+            pdl_begin();
             const uint32_t nc  = min( b.counts->segCircles, b.capC1 );
             uint32_t       ovf = 0, fp64 = 0;
             for ( uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x; idx < nc; idx += gridDim.x * blockDim.x )
@@ -1804,6 +1833,7 @@ namespace sesgb
         // ---- neighbours of singular probes -------------------------------------
         __global__ void __launch_bounds__( 32 * kWarpsPerBlock ) k_probe_neighbors( Build b )
         {
+            pdl_begin();
             __shared__ unsigned long long buf[ kWarpsPerBlock ][ kSnbrBuf ];
             const uint32_t                warp = threadIdx.x >> 5, lane = lane_id();
             const uint32_t                Q    = min( b.counts->Q, b.capProbes );
@@ -1889,6 +1919,7 @@ namespace sesgb
         // (ssesdf/operations.cu:397); done after every neighbour search read xyz
         __global__ void k_probe_w( Build b )
         {
+            pdl_begin();
             const uint32_t Q = min( b.counts->Q, b.capProbes );
             for ( uint32_t q = blockIdx.x * blockDim.x + threadIdx.x; q < Q; q += gridDim.x * blockDim.x )
             {
@@ -1906,6 +1937,7 @@ namespace sesgb
         // ---- batches: per-molecule counts and molecule-local ids ----------------
         __global__ void k_mol_counts( Build b )
         {
+            pdl_begin();
             for ( uint32_t m = blockIdx.x * blockDim.x + threadIdx.x; m < b.nMol; m += gridDim.x * blockDim.x )
             {
                 const uint32_t a0 = b.molStart[ m ], a1 = b.molStart[ m + 1 ];
@@ -1943,6 +1975,7 @@ namespace sesgb
         // slice of a batch reads exactly like the buffers of its own build.
         __global__ void k_mol_rebase( Build b )
         {
+            pdl_begin();
             const uint32_t stride = gridDim.x * blockDim.x;
             const uint32_t t0     = blockIdx.x * blockDim.x + threadIdx.x;
             for ( uint32_t s = t0; s < b.n; s += stride )
@@ -1986,6 +2019,7 @@ namespace sesgb
         // ---- exterior tori ---------------------------------------------------
         __global__ void __launch_bounds__( 32 * kWarpsPerBlock ) k_tori_count( Build b )
         {
+            pdl_begin();
             const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
             const uint32_t i    = blockIdx.x * kWarpsPerBlock + warp;
             if ( i >= b.n )
@@ -2002,6 +2036,7 @@ namespace sesgb
 
         __global__ void __launch_bounds__( 32 * kWarpsPerBlock ) k_tori( Build b )
         {
+            pdl_begin();
             const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
             const uint32_t i    = blockIdx.x * kWarpsPerBlock + warp;
             if ( i >= b.n )
@@ -2107,30 +2142,39 @@ namespace sesgb
     {
         if ( !b.n )
             return;
-        k_hash<<<blocks_for( b.n, 256 ), 256, 0, s>>>( b );
+        pdl_launch( k_hash, blocks_for( b.n, 256 ), 256, 0, s, b );
         counted();
     }
     void launch_fine_params( const Build & b, float cutoff, uint32_t, cudaStream_t s )
     {
-        k_fine_params<<<blocks_for( b.nMol, 128 ), 128, 0, s>>>( b, cutoff );
+        pdl_launch( k_fine_params, blocks_for( b.nMol, 128 ), 128, 0, s, b, cutoff );
+        counted();
+    }
+    void launch_zero2( uint32_t * a, uint32_t * c, uint32_t nHost, const uint32_t * nDevice, cudaStream_t s )
+    {
+        pdl_launch( k_zero2, min( persistent_blocks( 256 ), blocks_for( (uint64_t)nHost + 1, 256 ) ), 256, 0, s, a, c, nHost, nDevice );
         counted();
     }
     void launch_gather( const Build & b, cudaStream_t s )
     {
         if ( !b.n )
             return;
-        k_gather<<<blocks_for( b.n, 256 ), 256, 0, s>>>( b );
+        pdl_launch( k_gather, blocks_for( b.n, 256 ), 256, 0, s, b );
         counted();
     }
     void launch_cells( const Build & b, int kind, uint32_t nHost, const uint32_t * nDevice, void * scanScratch,
                        cudaStream_t s )
     {
-        cudaMemsetAsync( b.cellCount, 0, sizeof( uint32_t ) * ( (size_t)b.capCells + 1 ), s );
-        cudaMemsetAsync( b.cellCursor, 0, sizeof( uint32_t ) * ( (size_t)b.capCells + 1 ), s );
+        {
+            // the cells of the grid just sized (one molecule), or every cell of a batch
+            const uint32_t * cells = b.nMol > 1 ? nullptr
+                                                : reinterpret_cast<const uint32_t *>( reinterpret_cast<const char *>( b.fine ) + offsetof( FineGrid, cells ) );
+            launch_zero2( b.cellCount, b.cellCursor, b.capCells, cells, s );
+        }
         if ( nHost == 0 )
             return;
         const uint32_t blocks = nDevice ? min( persistent_blocks( 256 ), blocks_for( nHost, 256 ) ) : blocks_for( nHost, 256 );
-        k_cell_count<<<blocks, 256, 0, s>>>( b, kind, nHost, nDevice );
+        pdl_launch( k_cell_count, blocks, 256, 0, s, b, kind, nHost, nDevice );
         if ( b.nMol > 1 )
             exclusive_scan( b.cellCount, b.cellStart, b.capCells, nullptr, nullptr, scanScratch, s ); // all molecules' cells
         else
@@ -2138,44 +2182,44 @@ namespace sesgb
             const uint32_t * cells = reinterpret_cast<const uint32_t *>( reinterpret_cast<const char *>( b.fine ) + offsetof( FineGrid, cells ) );
             exclusive_scan( b.cellCount, b.cellStart, b.capCells, cells, nullptr, scanScratch, s );
         }
-        k_cell_scatter<<<blocks, 256, 0, s>>>( b, kind, nHost, nDevice );
+        pdl_launch( k_cell_scatter, blocks, 256, 0, s, b, kind, nHost, nDevice );
         counted( 2 );
     }
     void launch_batch_finish( const Build & b, cudaStream_t s )
     {
         if ( b.nMol <= 1 || !b.n )
             return;
-        k_mol_counts<<<blocks_for( b.nMol, 128 ), 128, 0, s>>>( b );
-        k_mol_rebase<<<persistent_blocks( 256 ), 256, 0, s>>>( b );
+        pdl_launch( k_mol_counts, blocks_for( b.nMol, 128 ), 128, 0, s, b );
+        pdl_launch( k_mol_rebase, persistent_blocks( 256 ), 256, 0, s, b );
         counted( 2 );
     }
     void launch_neighbors( const Build & b, cudaStream_t s )
     {
         if ( !b.n )
             return;
-        k_neighbors<<<blocks_for( b.n, kWarpsPerBlock ), 32 * kWarpsPerBlock, 0, s>>>( b );
+        pdl_launch( k_neighbors, blocks_for( b.n, kWarpsPerBlock ), 32 * kWarpsPerBlock, 0, s, b );
         counted();
     }
     void launch_visibility( const Build & b, cudaStream_t s )
     {
         if ( !b.n )
             return;
-        k_visibility<<<blocks_for( b.n, kWarpsPerBlock ), 32 * kWarpsPerBlock, visibility_smem( b.cap ), s>>>( b );
+        pdl_launch( k_visibility, blocks_for( b.n, kWarpsPerBlock ), 32 * kWarpsPerBlock, visibility_smem( b.cap ), s, b );
         counted();
     }
     void launch_visibility_resolve( const Build & b, cudaStream_t s )
     {
         if ( !b.n )
             return;
-        k_visibility_band<<<min( persistent_blocks( 128 ), blocks_for( b.capVisBand, 128 ) + 1 ), 128, 0, s>>>( b );
-        k_visibility_final<<<blocks_for( b.n, kWarpsPerBlock * 4 ), 32 * kWarpsPerBlock, 0, s>>>( b );
+        pdl_launch( k_visibility_band, min( persistent_blocks( 128 ), blocks_for( b.capVisBand, 128 ) + 1 ), 128, 0, s, b );
+        pdl_launch( k_visibility_final, blocks_for( b.n, kWarpsPerBlock * 4 ), 32 * kWarpsPerBlock, 0, s, b );
         counted( 2 );
     }
     void launch_emit( const Build & b, cudaStream_t s )
     {
         if ( !b.n )
             return;
-        k_emit<<<blocks_for( b.n, kWarpsPerBlock * ( 32 / kEmitGroup ) ), 32 * kWarpsPerBlock, 0, s>>>( b );
+        pdl_launch( k_emit, blocks_for( b.n, kWarpsPerBlock * ( 32 / kEmitGroup ) ), 32 * kWarpsPerBlock, 0, s, b );
         counted();
     }
     void launch_probes( const Build & b, cudaStream_t s )
@@ -2183,43 +2227,43 @@ namespace sesgb
         if ( !b.n )
             return;
         const size_t smem = probe_smem_per_warp( b.cap ) * kProbeWarps;
-        k_probes<<<blocks_for( b.n, kProbeWarps ), 32 * kProbeWarps, smem, s>>>( b );
+        pdl_launch( k_probes, blocks_for( b.n, kProbeWarps ), 32 * kProbeWarps, smem, s, b );
         counted();
     }
     void launch_probe_jobs( const Build & b, cudaStream_t s )
     {
-        k_probe_jobs<<<min( persistent_blocks( 128 ), blocks_for( b.capProbes, 128 ) + 1 ), 128, 0, s>>>( b );
+        pdl_launch( k_probe_jobs, min( persistent_blocks( 128 ), blocks_for( b.capProbes, 128 ) + 1 ), 128, 0, s, b );
         counted();
     }
     void launch_place( const Build & b, cudaStream_t s )
     {
         if ( !b.n )
             return;
-        k_place<<<blocks_for( b.n, kWarpsPerBlock * ( 32 / kPlaceGroup ) ), 32 * kWarpsPerBlock, 0, s>>>( b );
+        pdl_launch( k_place, blocks_for( b.n, kWarpsPerBlock * ( 32 / kPlaceGroup ) ), 32 * kWarpsPerBlock, 0, s, b );
         counted();
     }
     void launch_lists( const Build & b, cudaStream_t s )
     {
-        k_lists<<<min( persistent_blocks( 256 ), blocks_for( b.capProbes, 256 ) + 1 ), 256, 0, s>>>( b );
+        pdl_launch( k_lists, min( persistent_blocks( 256 ), blocks_for( b.capProbes, 256 ) + 1 ), 256, 0, s, b );
         counted();
     }
     void launch_segment_counts( const Build & b, cudaStream_t s )
     {
-        k_segment_counts<<<min( persistent_blocks( 256 ), blocks_for( b.capC1, 256 ) + 1 ), 256, 0, s>>>( b );
+        pdl_launch( k_segment_counts, min( persistent_blocks( 256 ), blocks_for( b.capC1, 256 ) + 1 ), 256, 0, s, b );
         counted();
     }
     void launch_segments( const Build & b, cudaStream_t s )
     {
-        k_segments<<<min( persistent_blocks( 128 ), blocks_for( b.capC1, 128 ) + 1 ), 128, 0, s>>>( b );
+        pdl_launch( k_segments, min( persistent_blocks( 128 ), blocks_for( b.capC1, 128 ) + 1 ), 128, 0, s, b );
         counted();
     }
     void launch_probe_neighbors( const Build & b, cudaStream_t s )
     {
-        k_probe_neighbors<<<min( persistent_blocks( 256 ), blocks_for( b.capProbes, kWarpsPerBlock ) + 1 ), 32 * kWarpsPerBlock, 0, s>>>( b );
+        pdl_launch( k_probe_neighbors, min( persistent_blocks( 256 ), blocks_for( b.capProbes, kWarpsPerBlock ) + 1 ), 32 * kWarpsPerBlock, 0, s, b );
         counted();
         if ( b.mode == 1 )
         {
-            k_probe_w<<<min( persistent_blocks( 256 ), blocks_for( b.capProbes, 256 ) + 1 ), 256, 0, s>>>( b );
+            pdl_launch( k_probe_w, min( persistent_blocks( 256 ), blocks_for( b.capProbes, 256 ) + 1 ), 256, 0, s, b );
             counted();
         }
     }
@@ -2227,14 +2271,14 @@ namespace sesgb
     {
         if ( !b.n )
             return;
-        k_tori_count<<<blocks_for( b.n, kWarpsPerBlock ), 32 * kWarpsPerBlock, 0, s>>>( b );
+        pdl_launch( k_tori_count, blocks_for( b.n, kWarpsPerBlock ), 32 * kWarpsPerBlock, 0, s, b );
         counted();
     }
     void launch_tori_emit( const Build & b, cudaStream_t s )
     {
         if ( !b.n )
             return;
-        k_tori<<<blocks_for( b.n, kWarpsPerBlock ), 32 * kWarpsPerBlock, 0, s>>>( b );
+        pdl_launch( k_tori, blocks_for( b.n, kWarpsPerBlock ), 32 * kWarpsPerBlock, 0, s, b );
         counted();
     }
     uint64_t launch_count() { return g_launches.load(); }

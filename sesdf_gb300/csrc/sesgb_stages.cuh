@@ -116,6 +116,8 @@ namespace sesgb
     void launch_hash( const Build & b, cudaStream_t s );
     void launch_fine_params( const Build & b, float cutoff, uint32_t items, cudaStream_t s );
     void launch_gather( const Build & b, cudaStream_t s );
+    // zeroes a[0, n] and c[0, n] (c may be null) with n = min(*nDevice, nHost), or nHost without nDevice
+    void launch_zero2( uint32_t * a, uint32_t * c, uint32_t nHost, const uint32_t * nDevice, cudaStream_t s );
     // kind 0: the sorted atoms (n); kind 1: the singular probes (count read from *nDevice); kind 2: the
     // sorted atoms with the radius negated for atoms without accessible surface (SDF queries)
     void launch_cells( const Build & b, int kind, uint32_t nHost, const uint32_t * nDevice, void * scanScratch,
