@@ -39,7 +39,8 @@ namespace sesgb
         constexpr float    k2PiF      = 6.28318530717959f;
         constexpr int      kAreaWarps = 4;
         constexpr int      kAreaNbr   = 128;             // neighbour constraints of one atom region
-        constexpr int      kAreaIv    = kAreaNbr + 2;    // cuts of one circle
+        constexpr int      kAreaIv    = 64 + 2;          // cuts of one constraint circle (a lane's own, local memory)
+        constexpr int      kLuneIv    = kAreaNbr + 2;    // cuts of one lune-plane circle (the warp's, shared memory)
         constexpr int      kProbeCons = 3 + (int)kMaxProbeNbr;
         static_assert( kMaxProbeNbr <= 32, "one neighbour cap per lane" );
 
@@ -200,12 +201,70 @@ namespace sesgb
             return total;
         }
 
+        // Cuts of one lune-plane circle, shared by the warp.
+        struct WarpCuts
+        {
+            float    s[ kLuneIv ], l[ kLuneIv ], ev[ kLuneIv ], el[ kLuneIv ];
+            uint8_t  unc[ kLuneIv ];
+        };
+
+        // circle_arcs for a circle whose cuts are in shared memory, with the cuts
+        // spread over the lanes; returns this lane's part of the Gauss-Bonnet terms
+        __device__ float circle_arcs_warp( const Circ & C, WarpCuts & W, int count )
+        {
+            const int lane = (int)lane_id();
+            if ( count == 0 )
+                return lane == 0 ? C.c * k2PiF : 0.f;
+            for ( int q = lane; q < count; q += 32 )
+            {
+                W.ev[ q ]        = wrapf( W.s[ q ] + W.l[ q ] );
+                const float len2 = wrapf( W.ev[ q ] - W.s[ q ] );
+                W.el[ q ]        = len2 >= 0.5f * W.l[ q ] ? len2 : W.l[ q ];
+            }
+            __syncwarp();
+            for ( int a = lane; a < count; a += 32 )
+            {
+                bool covered = false;
+                for ( int b = 0; b < count && !covered; b++ )
+                    covered = b != a && wrapf( W.ev[ a ] - W.s[ b ] ) < W.el[ b ];
+                W.unc[ a ] = !covered;
+            }
+            __syncwarp();
+            float total = 0.f;
+            for ( int a = lane; a < count; a += 32 )
+            {
+                if ( !W.unc[ a ] )
+                    continue;
+                const float end = W.ev[ a ];
+                bool        dup = false;
+                for ( int b = 0; b < a && !dup; b++ )
+                    dup = W.unc[ b ] && W.ev[ b ] == end;
+                if ( dup )
+                    continue;
+                float gap = k2PiF;
+                bool  any = false;
+                for ( int b = 0; b < count; b++ )
+                {
+                    const float g = wrapf( W.s[ b ] - end );
+                    if ( g > 0.f && ( !any || g < gap ) )
+                    {
+                        gap = g;
+                        any = true;
+                    }
+                }
+                if ( any )
+                    total += C.c * gap + arc_turn( C, end, gap );
+            }
+            __syncwarp();
+            return total;
+        }
+
         // One region of the unit sphere, held by a warp: constraints cons[0, M) in
         // shared memory; each lane takes circles m = lane, lane + 32, ...; the three
         // lunes add their two planes. per_arc(m, C, start, len, na, nb) is called for
         // every allowed arc of an original circle. Returns the area (all lanes).
         template<class PerArc>
-        __device__ float region_area_warp( const float4 * cons, int M, uint32_t & overflow, PerArc per_arc )
+        __device__ float region_area_warp( const float4 * cons, int M, WarpCuts & W, uint32_t & overflow, PerArc per_arc )
         {
             const uint32_t lane = lane_id();
             float          tot[ 3 ] = { 0.f, 0.f, 0.f };
@@ -273,36 +332,39 @@ namespace sesgb
                     tot[ L ] += circle_arcs( C, X, [ & ]( float st, float ln, int na, int nb ) { per_arc( m, C, st, ln, na, nb ); } );
                 }
             }
-            // the lune planes: six circles, lanes 0..5
-            if ( lane < 6 )
+            // the lune planes: six circles, one after another, each over the whole warp
+            for ( int lc = 0; lc < 6; lc++ )
             {
-                const int L = (int)lane >> 1, side = (int)lane & 1;
+                const int  L = lc >> 1, side = lc & 1;
                 const Circ C    = circ_of( lune_cons( L, side ) );
                 bool       gone = false;
                 int        nIv  = 0;
-                for ( int n = 0; n <= M && !gone; n++ )
+                for ( int n0 = 0; n0 <= M; n0 += 32 )
                 {
-                    const float4 kn = n < M ? cons[ n ] : lune_cons( L, 1 - side );
-                    float        st, ln;
-                    const int    r = cut_of( C, kn, st, ln );
-                    if ( r == 2 )
-                        gone = true;
-                    else if ( r == 1 )
+                    const int n = n0 + (int)lane;
+                    float     st = 0.f, ln = 0.f;
+                    int       r  = 0;
+                    if ( n <= M )
+                        r = cut_of( C, n < M ? cons[ n ] : lune_cons( L, 1 - side ), st, ln );
+                    gone |= r == 2;
+                    const uint32_t mk  = __ballot_sync( 0xffffffffu, r == 1 );
+                    const int      pos = nIv + __popc( mk & lanemask_lt() );
+                    if ( r == 1 && pos < kLuneIv )
                     {
-                        if ( nIv < kAreaIv )
-                        {
-                            X.s[ nIv ] = st, X.l[ nIv ] = ln, X.n[ nIv ] = (uint16_t)( n < M ? n : M + ( 1 - side ) );
-                            nIv++;
-                        }
-                        else
-                            overflow = 1;
+                        W.s[ pos ] = st;
+                        W.l[ pos ] = ln;
                     }
+                    nIv += __popc( mk );
                 }
-                if ( !gone )
+                if ( nIv > kLuneIv )
                 {
-                    X.count = nIv;
-                    tot[ L ] += circle_arcs( C, X, []( float, float, int, int ) {} );
+                    overflow = 1;
+                    nIv      = kLuneIv;
                 }
+                __syncwarp();
+                if ( !__any_sync( 0xffffffffu, gone ) )
+                    tot[ L ] += circle_arcs_warp( C, W, nIv );
+                __syncwarp();
             }
             float area = 0.f;
             for ( int L = 0; L < 3; L++ )
@@ -391,6 +453,7 @@ namespace sesgb
             float4 gw[ kAreaNbr ];
             float  dist[ kAreaNbr ];
             float  Rn[ kAreaNbr ];
+            WarpCuts cuts;
         };
 
         // Warp per atom: convex patch and the tori of its circles (i, j), i < j.
@@ -441,7 +504,7 @@ namespace sesgb
                     S.gw[ m ]    = make_float4( 0.f, 0.f, 0.f, 0.f );
                 }
                 __syncwarp();
-                const float U = region_area_warp( S.cons, M, overflow, [ & ]( int m, const Circ & C, float st, float ln, int na, int nb ) {
+                const float U = region_area_warp( S.cons, M, S.cuts, overflow, [ & ]( int m, const Circ & C, float st, float ln, int na, int nb ) {
                     // the lane that owns circle m is the only writer of its sums
                     S.dphi[ m ] += ln;
                     if ( !kGrad )
@@ -566,6 +629,7 @@ namespace sesgb
             float4 iy[ kProbeCons ];
             float  dist[ kProbeCons ];
             uint32_t nq[ kProbeCons ];
+            WarpCuts cuts;
         };
 
         // Warp per probe: its concave triangle outside the listed neighbour probes.
@@ -642,7 +706,7 @@ namespace sesgb
                     S.iy[ m ]   = make_float4( 0.f, 0.f, 0.f, 0.f );
                 }
                 __syncwarp();
-                const float U = region_area_warp( S.cons, M, overflow, [ & ]( int m, const Circ & C, float st, float ln, int, int ) {
+                const float U = region_area_warp( S.cons, M, S.cuts, overflow, [ & ]( int m, const Circ & C, float st, float ln, int, int ) {
                     if ( !kGrad )
                         return;
                     S.dphi[ m ] += ln;
