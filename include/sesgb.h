@@ -117,9 +117,10 @@ typedef struct sesgb_counts
     uint32_t truncated_probe_neighbors; /* singular probes with more than 32 neighbours */
     uint32_t degenerate_tori; /* torus axes parallel to z (the reference produces NaN there) */
     uint32_t outside_atoms;  /* atoms outside the grid box given at creation */
-    uint32_t fp64_decisions[ 6 ]; /* settled in double precision: neighbour, visibility and occlusion predicates,
+    uint32_t fp64_decisions[ 7 ]; /* settled in double precision: neighbour, visibility and occlusion predicates,
                                      probe-neighbour distances, probe candidates re-solved after a float32 band hit,
-                                     circles whose float32 probe order was ambiguous */
+                                     circles whose float32 probe order was ambiguous, kept probes whose float-float
+                                     position lay too close to a float32 rounding boundary */
     uint32_t rebuilds;       /* capacity regrowths of the last build */
 } sesgb_counts;
 

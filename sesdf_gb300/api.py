@@ -75,7 +75,7 @@ COUNT_FIELDS = ["atoms", "pairs", "sectors", "full_circles", "partial_circles", 
 
 
 class Counts(ctypes.Structure):
-    _fields_ = [(f, ctypes.c_uint32) for f in COUNT_FIELDS] + [("fp64_decisions", ctypes.c_uint32 * 6),
+    _fields_ = [(f, ctypes.c_uint32) for f in COUNT_FIELDS] + [("fp64_decisions", ctypes.c_uint32 * 7),
                                                                ("rebuilds", ctypes.c_uint32)]
 
 

@@ -690,7 +690,7 @@ extern "C"
         o->truncated_probe_neighbors    = h.snbrTruncated;
         o->degenerate_tori              = h.torusDegenerate;
         o->outside_atoms                = h.outside;
-        for ( int k = 0; k < 6; k++ )
+        for ( int k = 0; k < 7; k++ )
             o->fp64_decisions[ k ] = h.fp64[ k ];
         o->rebuilds = c->rebuilds;
         return SESGB_OK;

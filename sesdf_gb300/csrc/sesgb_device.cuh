@@ -125,6 +125,71 @@ namespace sesgb
         return copysign( 1.0, det ) > 0.0 ? __dsub_rn( 1.0, c ) : __dadd_rn( 3.0, c );
     }
 
+    // ---- float-float ("double-float") arithmetic -----------------------------
+    // A value is hi + lo with two float32 numbers, |lo| <= ulp(hi) / 2: about 48
+    // significand bits on the float32 pipes (64x the FP64 rate on GB300). The
+    // error-free transforms are Knuth's two-sum, Dekker's fast two-sum and the
+    // FMA two-product; add, multiply, divide and square root follow the usual
+    // double-word algorithms (as in Dekker 1971 and the QD library of Hida, Li and
+    // Bailey, 2001), written here with explicitly rounded float intrinsics so that
+    // no contraction changes them.
+    struct ff
+    {
+        float hi, lo;
+    };
+    __device__ __forceinline__ ff ff_of( float a ) { return { a, 0.f }; }
+    __device__ __forceinline__ ff two_sum( float a, float b )
+    {
+        const float s  = __fadd_rn( a, b );
+        const float bb = __fsub_rn( s, a );
+        const float e  = __fadd_rn( __fsub_rn( a, __fsub_rn( s, bb ) ), __fsub_rn( b, bb ) );
+        return { s, e };
+    }
+    __device__ __forceinline__ ff fast_two_sum( float a, float b ) // |a| >= |b| (or a = 0)
+    {
+        const float s = __fadd_rn( a, b );
+        return { s, __fsub_rn( b, __fsub_rn( s, a ) ) };
+    }
+    __device__ __forceinline__ ff two_prod( float a, float b )
+    {
+        const float p = __fmul_rn( a, b );
+        return { p, __fmaf_rn( a, b, -p ) };
+    }
+    __device__ __forceinline__ ff ff_add( ff x, ff y )
+    {
+        ff       s = two_sum( x.hi, y.hi );
+        const ff t = two_sum( x.lo, y.lo );
+        s          = fast_two_sum( s.hi, __fadd_rn( s.lo, t.hi ) );
+        return fast_two_sum( s.hi, __fadd_rn( s.lo, t.lo ) );
+    }
+    __device__ __forceinline__ ff ff_neg( ff x ) { return { -x.hi, -x.lo }; }
+    __device__ __forceinline__ ff ff_sub( ff x, ff y ) { return ff_add( x, ff_neg( y ) ); }
+    __device__ __forceinline__ ff ff_mul( ff x, ff y )
+    {
+        ff p = two_prod( x.hi, y.hi );
+        p.lo = __fmaf_rn( x.hi, y.lo, __fmaf_rn( x.lo, y.hi, p.lo ) );
+        return fast_two_sum( p.hi, p.lo );
+    }
+    __device__ __forceinline__ ff ff_scale( ff x, float pow2 ) { return { __fmul_rn( x.hi, pow2 ), __fmul_rn( x.lo, pow2 ) }; }
+    // x / y: a float quotient refined twice by the float-float remainder
+    __device__ __forceinline__ ff ff_div( ff x, ff y )
+    {
+        const float q1 = __fdiv_rn( x.hi, y.hi );
+        ff          r  = ff_sub( x, ff_mul( y, ff_of( q1 ) ) );
+        const float q2 = __fdiv_rn( r.hi, y.hi );
+        r              = ff_sub( r, ff_mul( y, ff_of( q2 ) ) );
+        const float q3 = __fdiv_rn( r.hi, y.hi );
+        const ff    q  = fast_two_sum( q1, q2 );
+        return ff_add( q, ff_of( q3 ) );
+    }
+    // sqrt(x), x > 0: the float root corrected by one Newton step in float-float
+    __device__ __forceinline__ ff ff_sqrt( ff x )
+    {
+        const float s = __fsqrt_rn( x.hi );
+        const ff    r = ff_sub( x, two_prod( s, s ) );
+        return fast_two_sum( s, __fdiv_rn( r.hi, __fmul_rn( 2.f, s ) ) );
+    }
+
     // ---- reference grid hash (GridInfo, sesdf/include/bcs/cuda/grid.inl) ---
     struct GridRef
     {

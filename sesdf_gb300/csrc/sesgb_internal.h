@@ -85,6 +85,7 @@ namespace sesgb
         kFp64SingularNbr,
         kFp64Solve,    // probe candidates whose float32 screen hit the band
         kFp64Segments, // circles whose float32 angle order was ambiguous
+        kFp64Positions, // kept probes whose float-float position was too close to a rounding boundary
         kFp64Count
     };
 

@@ -916,6 +916,87 @@ namespace sesgb
             return true;
         }
 
+        // Float-float solve of a kept probe: the closed form of solve_d carried in
+        // float-float arithmetic (about 48 bits), with an a-priori bound Ex on the
+        // distance of its position from the exact point. The double-precision result
+        // lies within far less than Ex of the exact point too, so wherever the
+        // float-float coordinate is more than Ex from a float32 rounding boundary
+        // both round to the same float32 (and the singular test, more than its own
+        // bound from its threshold, decides alike). Returns false otherwise; the
+        // caller then solves in double precision (about 0.2 % of the jobs, mostly
+        // probes close to the plane of their centres).
+        __device__ __forceinline__ ff ff_dot3( ff ax, ff ay, ff az, ff bx, ff by, ff bz )
+        {
+            return ff_add( ff_add( ff_mul( ax, bx ), ff_mul( ay, by ) ), ff_mul( az, bz ) );
+        }
+        __device__ __forceinline__ float ff_margin( ff x )
+        {
+            // distance of x from the nearest boundary between two float32 values
+            const float v    = fabsf( x.hi );
+            const float up   = __int_as_float( __float_as_int( v ) + 1 ) - v;
+            const float down = v > 0.f ? v - __int_as_float( __float_as_int( v ) - 1 ) : up;
+            return 0.5f * fminf( up, down ) - fabsf( x.lo );
+        }
+        __device__ bool solve_ff( float4 ai, float4 aj, float4 ak, float rp, uint32_t side, bool wantSingular, float3 & pos,
+                                  bool & singular )
+        {
+            const ff ax = two_sum( aj.x, -ai.x ), ay = two_sum( aj.y, -ai.y ), az = two_sum( aj.z, -ai.z );
+            const ff bx = two_sum( ak.x, -ai.x ), by = two_sum( ak.y, -ai.y ), bz = two_sum( ak.z, -ai.z );
+            const ff nx = ff_sub( ff_mul( ay, bz ), ff_mul( az, by ) );
+            const ff ny = ff_sub( ff_mul( az, bx ), ff_mul( ax, bz ) );
+            const ff nz = ff_sub( ff_mul( ax, by ), ff_mul( ay, bx ) );
+            const ff Ri = two_sum( ai.w, rp ), Rj = two_sum( aj.w, rp ), Rk = two_sum( ak.w, rp );
+            const ff Ri2 = ff_mul( Ri, Ri ), Rj2 = ff_mul( Rj, Rj ), Rk2 = ff_mul( Rk, Rk );
+            const ff aa  = ff_dot3( ax, ay, az, ax, ay, az );
+            const ff bb  = ff_dot3( bx, by, bz, bx, by, bz );
+            const ff p   = ff_scale( ff_sub( ff_add( aa, Ri2 ), Rj2 ), 0.5f );
+            const ff q   = ff_scale( ff_sub( ff_add( bb, Ri2 ), Rk2 ), 0.5f );
+            const ff nn  = ff_dot3( nx, ny, nz, nx, ny, nz );
+            if ( !( nn.hi > 0.f ) )
+                return false;
+            const ff inv = ff_div( ff_of( 1.f ), nn );
+            // y0 = (p (b x n) + q (n x a)) / |n|^2
+            const ff cx  = ff_add( ff_mul( p, ff_sub( ff_mul( by, nz ), ff_mul( bz, ny ) ) ), ff_mul( q, ff_sub( ff_mul( ny, az ), ff_mul( nz, ay ) ) ) );
+            const ff cy  = ff_add( ff_mul( p, ff_sub( ff_mul( bz, nx ), ff_mul( bx, nz ) ) ), ff_mul( q, ff_sub( ff_mul( nz, ax ), ff_mul( nx, az ) ) ) );
+            const ff cz  = ff_add( ff_mul( p, ff_sub( ff_mul( bx, ny ), ff_mul( by, nx ) ) ), ff_mul( q, ff_sub( ff_mul( nx, ay ), ff_mul( ny, ax ) ) ) );
+            const ff yx = ff_mul( cx, inv ), yy = ff_mul( cy, inv ), yz = ff_mul( cz, inv );
+            const ff h2 = ff_sub( Ri2, ff_dot3( yx, yy, yz, yx, yy, yz ) );
+            if ( !( h2.hi > 0.f ) )
+                return false;
+            const ff s = ff_sqrt( ff_mul( h2, inv ) );
+            // error bound, with u = 2^-42 (a float-float operation rounds by at most
+            // ~2^-46 relative to the magnitudes bounded below; ~10 of them feed each
+            // term, and every term carries a factor >= 4 on top) and
+            // kappa = |a| |b| / |n| = 1 / sin(angle at c_i)
+            const float u     = 2.2737367544323206e-13f;
+            const float A     = sqrtf( aa.hi ), B = sqrtf( bb.hi ), N = sqrtf( nn.hi );
+            const float kappa = A * B / N;
+            const float Pm    = aa.hi + Ri2.hi + Rj2.hi, Qm = bb.hi + Ri2.hi + Rk2.hi;
+            const float Y     = sqrtf( yx.hi * yx.hi + yy.hi * yy.hi + yz.hi * yz.hi );
+            const float root  = sqrtf( h2.hi );
+            const float Ey0   = u * ( ( Pm * B + Qm * A ) / N + Y ) * ( 4.f + 2.f * kappa );
+            const float Eh2   = 2.f * Y * Ey0 + u * ( Ri2.hi + Y * Y );
+            const float Eroot = Eh2 / ( 2.f * root ) + u * ( 2.f + 2.f * kappa ) * root;
+            const float amax  = fmaxf( fabsf( ai.x ), fmaxf( fabsf( ai.y ), fabsf( ai.z ) ) );
+            const float Ex    = Ey0 + Eroot + u * ( amax + Y + root );
+            const ff    px = ff_add( ff_add( ff_of( ai.x ), yx ), side ? ff_neg( ff_mul( nx, s ) ) : ff_mul( nx, s ) );
+            const ff    py = ff_add( ff_add( ff_of( ai.y ), yy ), side ? ff_neg( ff_mul( ny, s ) ) : ff_mul( ny, s ) );
+            const ff    pz = ff_add( ff_add( ff_of( ai.z ), yz ), side ? ff_neg( ff_mul( nz, s ) ) : ff_mul( nz, s ) );
+            if ( !( ff_margin( px ) > Ex && ff_margin( py ) > Ex && ff_margin( pz ) > Ex ) )
+                return false;
+            pos = make_float3( px.hi, py.hi, pz.hi );
+            if ( wantSingular )
+            {
+                // h2 - rp^2 < -1e-4 (the threshold as the double of the float 1e-4)
+                const ff    v  = ff_add( ff_sub( h2, two_prod( rp, rp ) ), ff_of( 1e-4f ) );
+                const float Ev = Eh2 + u * rp * rp;
+                if ( !( fabsf( v.hi ) > Ev ) )
+                    return false;
+                singular = v.hi < 0.f;
+            }
+            return true;
+        }
+
         // singular flag (operations.inl:441-451): the point closer than rp to the
         // plane of the centres, d^2 - rp^2 < -1e-4 with d^2 = h2
         __device__ __forceinline__ bool singular_d( double h2, double rp )
@@ -924,7 +1005,11 @@ namespace sesgb
         }
 
         // Occlusion of the double-precision points by N(i) \ {j, k} (operations.inl:401-430):
-        // float32 filter around the rounded relative positions, double precision in the band.
+        // float32 filter around the rounded relative positions, double precision in
+        // the band. The neighbours are fetched eight at a time (independent loads in
+        // flight instead of one dependent id-then-atom pair per neighbour); the test
+        // is an "inside some l" test, so the order does not matter.
+        constexpr uint32_t kOccChunk = 8;
         __device__ __forceinline__ void occlusion_d( const Build & b, uint32_t i, const float4 & ai, uint32_t sj, uint32_t sk,
                                                      const d3 x[ 2 ], bool vis[ 2 ], uint32_t & fp64 )
         {
@@ -934,31 +1019,44 @@ namespace sesgb
             for ( int e = 0; e < 2; e++ )
                 xr[ e ] = F3( __double2float_rn( __dsub_rn( x[ e ].x, ci.x ) ), __double2float_rn( __dsub_rn( x[ e ].y, ci.y ) ),
                               __double2float_rn( __dsub_rn( x[ e ].z, ci.z ) ) );
-            const uint32_t ni = b.nbrCount[ i ];
-            for ( uint32_t sl = 0; sl < ni && ( vis[ 0 ] || vis[ 1 ] ); sl++ )
+            const uint32_t   ni  = b.nbrCount[ i ];
+            const uint32_t * row = b.nbr + (size_t)i * b.cap;
+            for ( uint32_t s0 = 0; s0 < ni && ( vis[ 0 ] || vis[ 1 ] ); s0 += kOccChunk )
             {
-                if ( sl == sj || sl == sk )
-                    continue;
-                const float4 al  = b.atoms[ b.nbr[ (size_t)i * b.cap + sl ] ];
-                const f3     dl  = F3( al.x - ai.x, al.y - ai.y, al.z - ai.z );
-                const float  Rl  = al.w + b.rp;
-                const float  Rl2 = Rl * Rl;
-                for ( int e = 0; e < 2; e++ )
+                uint32_t id[ kOccChunk ];
+                float4   al[ kOccChunk ];
+#pragma unroll
+                for ( uint32_t c = 0; c < kOccChunk; c++ )
+                    id[ c ] = s0 + c < ni ? row[ s0 + c ] : 0u;
+#pragma unroll
+                for ( uint32_t c = 0; c < kOccChunk; c++ )
+                    al[ c ] = b.atoms[ id[ c ] ];
+#pragma unroll
+                for ( uint32_t c = 0; c < kOccChunk; c++ )
                 {
-                    if ( !vis[ e ] )
+                    const uint32_t sl = s0 + c;
+                    if ( sl >= ni || sl == sj || sl == sk )
                         continue;
-                    const f3    ev = dl - xr[ e ];
-                    const float ee = dot( ev, ev );
-                    const float m  = ee - Rl2;
-                    const float em = kRel * ( ee + Rl2 + 1.f );
-                    if ( m < -em )
-                        vis[ e ] = false;
-                    else if ( !( m > em ) )
+                    const f3    dl  = F3( al[ c ].x - ai.x, al[ c ].y - ai.y, al[ c ].z - ai.z );
+                    const float Rl  = al[ c ].w + b.rp;
+                    const float Rl2 = Rl * Rl;
+                    for ( int e = 0; e < 2; e++ )
                     {
-                        const double Rld = __dadd_rn( (double)al.w, rp );
-                        const d3     dv  = dsub( D3( al ), x[ e ] );
-                        vis[ e ]         = __dsub_rn( ddot( dv, dv ), __dmul_rn( Rld, Rld ) ) > 0.0;
-                        fp64++;
+                        if ( !vis[ e ] )
+                            continue;
+                        const f3    ev = dl - xr[ e ];
+                        const float ee = dot( ev, ev );
+                        const float m  = ee - Rl2;
+                        const float em = kRel * ( ee + Rl2 + 1.f );
+                        if ( m < -em )
+                            vis[ e ] = false;
+                        else if ( !( m > em ) )
+                        {
+                            const double Rld = __dadd_rn( (double)al[ c ].w, rp );
+                            const d3     dv  = dsub( D3( al[ c ] ), x[ e ] );
+                            vis[ e ]         = __dsub_rn( ddot( dv, dv ), __dmul_rn( Rld, Rld ) ) > 0.0;
+                            fp64++;
+                        }
                     }
                 }
             }
@@ -1509,38 +1607,53 @@ namespace sesgb
             const uint32_t nFill = min( b.counts->jobs, b.capProbes );
             const uint32_t nBand = min( b.counts->bandJobs, b.capProbes - nFill );
             const double   rp    = (double)b.rp;
-            uint32_t       fp64 = 0, full64 = 0;
-            // fill jobs first, then the band jobs stored from the top of the array
-            for ( uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nFill + nBand; t += gridDim.x * blockDim.x )
+            const uint32_t lane  = lane_id();
+            uint32_t       fp64 = 0, full64 = 0, ffMiss = 0;
+            // fill jobs, one per thread: float-float first, double precision only where
+            // the float-float result cannot decide
+            for ( uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < nFill; t += gridDim.x * blockDim.x )
             {
-                const uint4    jb   = b.jobs[ t < nFill ? t : b.capProbes - 1u - ( t - nFill ) ];
+                const uint4    jb   = b.jobs[ t ];
                 const uint32_t ent  = jb.x, i = jb.y;
                 const uint32_t sj   = jb.z & 0xffffu, sk = jb.z >> 16;
-                const uint32_t info = jb.w >> 16;
-                const uint32_t side = info & 0xffu, kind = info >> 8;
+                const uint32_t side = ( jb.w >> 16 ) & 0xffu;
                 const size_t   row  = (size_t)i * b.cap;
                 const float4   ai = b.atoms[ i ], aj = b.atoms[ b.nbr[ row + sj ] ], ak = b.atoms[ b.nbr[ row + sk ] ];
-                const d3       ci = D3( ai ), cj = D3( aj ), ck = D3( ak );
+                int4           cid  = b.stageCid[ ent ];
+                int            aw   = cid.w < 0 ? -cid.w : cid.w;
+                float3         pf;
+                bool           sing = false;
+                if ( !solve_ff( ai, aj, ak, b.rp, side, aw == 3, pf, sing ) )
+                {
+                    ffMiss++;
+                    d3         x[ 2 ];
+                    double     h2 = 0.0;
+                    solve_d( D3( ai ), (double)ai.w, D3( aj ), (double)aj.w, D3( ak ), (double)ak.w, rp, x[ 0 ], x[ 1 ], h2 );
+                    const d3 xs = side ? x[ 1 ] : x[ 0 ];
+                    pf          = make_float3( __double2float_rn( xs.x ), __double2float_rn( xs.y ), __double2float_rn( xs.z ) );
+                    sing        = singular_d( h2, rp );
+                }
+                if ( aw == 3 )
+                {
+                    aw                = sing ? 2 : 1;
+                    cid.w             = cid.w < 0 ? -aw : aw;
+                    b.stageCid[ ent ] = cid;
+                    atomicAdd( aw == 2 ? &b.singCnt[ i ] : &b.regCnt[ i ], 1u );
+                }
+                b.stagePos[ ent ] = make_float4( pf.x, pf.y, pf.z, (float)cid.w );
+            }
+            // band candidates, one per thread (the double-precision solve, occlusion and
+            // singular test), stored from the top of the job array
+            for ( uint32_t g = blockIdx.x * blockDim.x + threadIdx.x; g < nBand; g += gridDim.x * blockDim.x )
+            {
+                const uint4    jb  = b.jobs[ b.capProbes - 1u - g ];
+                const uint32_t ent = jb.x, i = jb.y;
+                const uint32_t sj  = jb.z & 0xffffu, sk = jb.z >> 16;
+                const size_t   row = (size_t)i * b.cap;
+                const float4   ai = b.atoms[ i ], aj = b.atoms[ b.nbr[ row + sj ] ], ak = b.atoms[ b.nbr[ row + sk ] ];
                 d3             x[ 2 ];
                 double         h2 = 0.0;
-                const bool     ok = solve_d( ci, (double)ai.w, cj, (double)aj.w, ck, (double)ak.w, rp, x[ 0 ], x[ 1 ], h2 );
-                if ( kind == kJobFill )
-                {
-                    int4 cid = b.stageCid[ ent ];
-                    int  aw  = cid.w < 0 ? -cid.w : cid.w;
-                    if ( aw == 3 )
-                    {
-                        aw    = singular_d( h2, rp ) ? 2 : 1;
-                        cid.w = cid.w < 0 ? -aw : aw;
-                        b.stageCid[ ent ] = cid;
-                        atomicAdd( aw == 2 ? &b.singCnt[ i ] : &b.regCnt[ i ], 1u );
-                    }
-                    const d3 xs       = side ? x[ 1 ] : x[ 0 ];
-                    b.stagePos[ ent ] = make_float4( __double2float_rn( xs.x ), __double2float_rn( xs.y ),
-                                                     __double2float_rn( xs.z ), (float)cid.w );
-                    continue;
-                }
-                // band candidate: entries ent (x1) and ent + 1 (x2)
+                const bool     ok = solve_d( D3( ai ), (double)ai.w, D3( aj ), (double)aj.w, D3( ak ), (double)ak.w, rp, x[ 0 ], x[ 1 ], h2 );
                 full64++;
                 if ( !ok )
                     continue;
@@ -1563,13 +1676,16 @@ namespace sesgb
             {
                 fp64 += __shfl_xor_sync( 0xffffffffu, fp64, o );
                 full64 += __shfl_xor_sync( 0xffffffffu, full64, o );
+                ffMiss += __shfl_xor_sync( 0xffffffffu, ffMiss, o );
             }
-            if ( lane_id() == 0 )
+            if ( lane == 0 )
             {
                 if ( fp64 )
                     atomicAdd( &b.counts->fp64[ kFp64Occlusion ], fp64 );
                 if ( full64 )
                     atomicAdd( &b.counts->fp64[ kFp64Solve ], full64 );
+                if ( ffMiss )
+                    atomicAdd( &b.counts->fp64[ kFp64Positions ], ffMiss );
             }
         }
 
