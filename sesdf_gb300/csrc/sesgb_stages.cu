@@ -484,6 +484,65 @@ namespace sesgb
             return dcircle_vs_atom( dc, D3( ak ), __dadd_rn( (double)ak.w, (double)b.rp ) );
         }
 
+        // circle_test_d in float-float: the same quantities (circle geometry of
+        // getCircleGeometry, then the two extremes first = r +- p, complete =
+        // first^2 + second^2 of computeCirclesVisibilityStatus, operations.cu:164-197)
+        // with a bound on their distance from the exact values that also covers the
+        // double-precision twin's own rounding (its sqrt(1 - cos^2) loses half the
+        // digits next to the axis). Returns the bits when both tests are farther than
+        // that from the 1e-4 threshold, -1 otherwise (the caller then decides in
+        // double precision).
+        __device__ int circle_test_ff( const float4 & ai, const float4 & aj, const float4 & ak, float rp )
+        {
+            const ff R1 = two_sum( ai.w, rp ), R2 = two_sum( aj.w, rp ), Rk = two_sum( ak.w, rp );
+            const ff dx = two_sum( aj.x, -ai.x ), dy = two_sum( aj.y, -ai.y ), dz = two_sum( aj.z, -ai.z ); // c_j - c_i
+            const ff d  = ff_add( ff_add( ff_mul( dx, dx ), ff_mul( dy, dy ) ), ff_mul( dz, dz ) );
+            if ( !( d.hi > 0.f ) )
+                return -1;
+            const ff R12 = ff_mul( R1, R1 );
+            const ff tt  = ff_div( ff_add( ff_sub( R12, ff_mul( R2, R2 ) ), d ), ff_scale( d, 2.f ) );
+            // circle centre relative to c_i: t (c_j - c_i); radius^2 = R1^2 - t^2 d
+            const ff ccx = ff_mul( dx, tt ), ccy = ff_mul( dy, tt ), ccz = ff_mul( dz, tt );
+            const ff r2  = ff_sub( R12, ff_mul( ff_mul( tt, tt ), d ) );
+            if ( !( r2.hi > 0.f ) )
+                return -1;
+            const ff rad = ff_sqrt( r2 );
+            const ff inv = ff_div( ff_of( 1.f ), ff_sqrt( d ) );
+            const ff nx = ff_mul( dx, inv ), ny = ff_mul( dy, inv ), nz = ff_mul( dz, inv );
+            // centre - c_k
+            const ff kx = ff_add( ccx, two_sum( ai.x, -ak.x ) ), ky = ff_add( ccy, two_sum( ai.y, -ak.y ) ), kz = ff_add( ccz, two_sum( ai.z, -ak.z ) );
+            const ff k2   = ff_add( ff_add( ff_mul( kx, kx ), ff_mul( ky, ky ) ), ff_mul( kz, kz ) );
+            if ( !( k2.hi > 0.f ) )
+                return -1;
+            const ff dist = ff_sqrt( k2 );
+            const ff sec  = ff_add( ff_add( ff_mul( kx, nx ), ff_mul( ky, ny ) ), ff_mul( kz, nz ) );
+            const ff cs   = ff_div( sec, dist );
+            const ff s2   = ff_sub( ff_of( 1.f ), ff_mul( cs, cs ) );
+            if ( !( s2.hi > 0.f ) )
+                return -1;
+            const ff sn   = ff_sqrt( s2 );
+            const ff p    = ff_mul( sn, dist ); // distance of c_k from the circle's axis
+            const ff sec2 = ff_mul( sec, sec );
+            const ff Rk2  = ff_mul( Rk, Rk );
+            const ff tol  = ff_of( 1e-4f );
+            const ff fp = ff_add( p, rad ), fm = ff_add( ff_neg( p ), rad );
+            const ff vp = ff_sub( ff_sub( ff_add( ff_mul( fp, fp ), sec2 ), Rk2 ), tol );
+            const ff vm = ff_sub( ff_sub( ff_add( ff_mul( fm, fm ), sec2 ), Rk2 ), tol );
+            // bound: u per operation on the magnitudes involved (u = 2^-42 covers the
+            // float-float chain, far more than the double one), plus the conditioning
+            // of the radius (cancellation in R1^2 - t^2 d) and of sin(theta) near the
+            // axis, for float-float (u / sin, at most 2 sqrt(u)) and for double
+            // (2^-50 / sin, at most 2^-24)
+            const float u   = 2.2737367544323206e-13f;
+            const float F   = fabsf( fp.hi ), D = dist.hi, R = rad.hi, S = sn.hi;
+            const float mag = F * F + sec2.hi + Rk2.hi + R12.hi + d.hi + 2.f * F * D;
+            const float eSin = fminf( 4.f * u / S, 2.f * sqrtf( u ) ) + fminf( 8.8817842e-16f / S, 5.9604645e-08f );
+            const float E    = 64.f * u * mag + 2.f * F * ( 64.f * u * R12.hi / R ) + 2.f * F * D * eSin;
+            if ( !( fabsf( vp.hi ) > E && fabsf( vm.hi ) > E ) )
+                return -1;
+            return ( vp.hi < 0.f ? 1 : 0 ) | ( vm.hi < 0.f ? 2 : 0 );
+        }
+
         // one test to the global double-precision queue (capacity exceeded: the build is redone larger)
         __device__ __forceinline__ void band_push( const Build & b, uint32_t i, uint32_t sk )
         {
@@ -705,8 +764,9 @@ namespace sesgb
                 b.status[ row + s ] = m.res[ s ];
         }
 
-        // Band tests in double precision, one per thread with full warps; the
-        // result bits go into the circle's status flags.
+        // Band tests, one per thread with full warps: float-float first, the double
+        // precision twin only where that cannot decide (counted); the result bits go
+        // into the circle's status flags.
         __global__ void __launch_bounds__( 128 ) k_visibility_band( Build b )
         {
             pdl_begin();
@@ -721,10 +781,17 @@ namespace sesgb
                 const size_t pos = (size_t)i * b.cap + s;
                 if ( b.status[ pos ] & kVisBuried )
                     continue;
-                const int rd = circle_test_d( b, b.atoms[ i ], i, s, k );
+                const float4 ai = b.atoms[ i ];
+                const float4 aj = b.atoms[ b.nbr[ (size_t)i * b.cap + s ] ];
+                const float4 ak = b.atoms[ b.nbr[ (size_t)i * b.cap + k ] ];
+                int          rd = circle_test_ff( ai, aj, ak, b.rp );
+                if ( rd < 0 )
+                {
+                    rd = circle_test_d( b, ai, i, s, k );
+                    fp64++;
+                }
                 if ( rd & 3 )
                     atomicOr( reinterpret_cast<uint32_t *>( b.status + ( pos & ~(size_t)3 ) ), (uint32_t)( rd & 3 ) << ( 8 * ( pos & 3 ) ) );
-                fp64++;
             }
             for ( int o = 16; o > 0; o >>= 1 )
                 fp64 += __shfl_xor_sync( 0xffffffffu, fp64, o );
