@@ -1872,9 +1872,77 @@ namespace sesgb
         // ---- segments (buildSegments, operations.inl:552-668) ---------------
         constexpr float kKeyTol = 1.0f / 32768.0f; // 2^-15: float32 pseudo-angles closer than this go to double
 
+        __device__ __forceinline__ ff ff_dot( ff ax, ff ay, ff az, ff bx, ff by, ff bz )
+        {
+            return ff_add( ff_add( ff_mul( ax, bx ), ff_mul( ay, by ) ), ff_mul( az, bz ) );
+        }
+        __device__ __forceinline__ bool ff_gt( ff a, ff b ) { return a.hi > b.hi || ( a.hi == b.hi && a.lo > b.lo ); }
+
+        // Float-float pseudo-angle keys of the probes of circle (i, j) (the double-
+        // precision keys' formula): their order is the double-precision order whenever
+        // every key is more than the bound E away from its neighbours in the order
+        // (the start key 0 included) and every side test more than its bound from 0.
+        // Returns false otherwise (the caller then sorts in double precision).
+        __device__ bool segment_order_ff( const Build & b, const float4 & ai, const float4 & aj, const float4 & spos,
+                                          const uint32_t * lst, uint32_t nb, bool reverse, uint8_t * ord )
+        {
+            const ff R1 = two_sum( ai.w, b.rp ), R2 = two_sum( aj.w, b.rp );
+            const ff dx = two_sum( aj.x, -ai.x ), dy = two_sum( aj.y, -ai.y ), dz = two_sum( aj.z, -ai.z );
+            const ff d  = ff_dot( dx, dy, dz, dx, dy, dz );
+            if ( !( d.hi > 0.f ) )
+                return false;
+            const ff tt  = ff_div( ff_add( ff_sub( ff_mul( R1, R1 ), ff_mul( R2, R2 ) ), d ), ff_scale( d, 2.f ) );
+            const ff cx  = ff_mul( dx, tt ), cy = ff_mul( dy, tt ), cz = ff_mul( dz, tt ); // centre - c_i
+            const ff inv = ff_div( ff_of( 1.f ), ff_sqrt( d ) );
+            const ff nx = ff_mul( dx, inv ), ny = ff_mul( dy, inv ), nz = ff_mul( dz, inv );
+            const ff rx = ff_sub( two_sum( spos.x, -ai.x ), cx ), ry = ff_sub( two_sum( spos.y, -ai.y ), cy ),
+                     rz = ff_sub( two_sum( spos.z, -ai.z ), cz );
+            const float E = 5.820766091346741e-11f; // 2^-34: 256 float-float roundings on keys of size <= 4
+            ff          key[ kSegBuf ];
+            key[ 0 ] = ff_of( 0.f );
+            ord[ 0 ] = 0;
+            for ( uint32_t m = 1; m < nb; m++ )
+            {
+                const float4 pm = b.probePos[ lst[ m ] ];
+                const ff     wx = ff_sub( two_sum( pm.x, -ai.x ), cx ), wy = ff_sub( two_sum( pm.y, -ai.y ), cy ),
+                         wz = ff_sub( two_sum( pm.z, -ai.z ), cz );
+                const ff ux = reverse ? wx : rx, uy = reverse ? wy : ry, uz = reverse ? wz : rz;
+                const ff vx = reverse ? rx : wx, vy = reverse ? ry : wy, vz = reverse ? rz : wz;
+                const ff uu = ff_dot( ux, uy, uz, ux, uy, uz ), vv = ff_dot( vx, vy, vz, vx, vy, vz );
+                const ff l  = ff_sqrt( ff_mul( uu, vv ) );
+                if ( !( l.hi > 0.f ) )
+                    return false;
+                ff c = ff_div( ff_dot( ux, uy, uz, vx, vy, vz ), l );
+                // det = u . (v x n)
+                const ff det = ff_dot( ux, uy, uz, ff_sub( ff_mul( vy, nz ), ff_mul( vz, ny ) ), ff_sub( ff_mul( vz, nx ), ff_mul( vx, nz ) ),
+                                       ff_sub( ff_mul( vx, ny ), ff_mul( vy, nx ) ) );
+                if ( !( fabsf( det.hi ) > E * l.hi ) )
+                    return false;
+                if ( c.hi > 1.f )
+                    c = ff_of( 1.f );
+                if ( c.hi < -1.f )
+                    c = ff_of( -1.f );
+                const ff kv = det.hi > 0.f ? ff_sub( ff_of( 1.f ), c ) : ff_add( ff_of( 3.f ), c );
+                uint32_t p  = m;
+                while ( p > 0 && ff_gt( key[ p - 1 ], kv ) )
+                {
+                    key[ p ] = key[ p - 1 ];
+                    ord[ p ] = ord[ p - 1 ];
+                    p--;
+                }
+                key[ p ] = kv;
+                ord[ p ] = (uint8_t)m;
+            }
+            for ( uint32_t m = 1; m < nb; m++ )
+                if ( !( ff_sub( key[ m ], key[ m - 1 ] ).hi > E ) )
+                    return false;
+            return true;
+        }
+
         // Orders the probes of circle t along the circle and writes its segments:
         // float32 keys first; when two keys (or a key and the start) are closer than
-        // kKeyTol, or a side test is ambiguous, the double-precision keys decide.
+        // kKeyTol, or a side test is ambiguous, float-float keys, and where even those
+        // are too close, the double-precision keys decide.
         __global__ void __launch_bounds__( 128 ) k_segments( Build b )
         {
             pdl_begin();
@@ -1960,7 +2028,7 @@ namespace sesgb
                         if ( key[ m ] - key[ m - 1 ] < kKeyTol )
                             exact = false;
                 }
-                if ( !exact )
+                if ( !exact && !segment_order_ff( b, ai, aj, spos, lst, nb, reverse, ord ) )
                 {
                     // double-precision keys (the oracle's), same stable ordering
                     fp64++;
