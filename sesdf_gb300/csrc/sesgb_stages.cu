@@ -1859,10 +1859,18 @@ namespace sesgb
                 b.segCnt[ t ]     = c / 2u;
                 if ( cc > b.segCap )
                     atomicAdd( &b.counts->segTruncated, 1u );
+                // circles carrying segments, in any order: one atomic per warp (a single
+                // counter taken by every circle serialises)
+                const uint32_t active = __activemask();
+                const uint32_t mk     = __ballot_sync( active, cc >= 2 );
+                const uint32_t leader = (uint32_t)( __ffs( active ) - 1 );
+                uint32_t       base   = 0;
+                if ( lane_id() == leader && mk )
+                    base = atomicAdd( &b.counts->segCircles, (uint32_t)__popc( mk ) );
+                base = __shfl_sync( active, base, leader );
                 if ( cc >= 2 )
                 {
-                    // circles carrying segments, in any order (each writes at its own offset)
-                    const uint32_t at = atomicAdd( &b.counts->segCircles, 1u );
+                    const uint32_t at = base + __popc( mk & lanemask_lt() );
                     if ( at < b.capC1 )
                         b.segList[ at ] = t;
                 }
