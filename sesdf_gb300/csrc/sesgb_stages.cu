@@ -652,10 +652,14 @@ namespace sesgb
                             const bool ok  = ( p2 > v.theta ) & ( fabsf( A ) > v.eA ) & ( fabsf( G2 ) > eG );
                             const bool neg = A < 0.f;
                             bur            = bur | ( ok & neg & ( G2 > 0.f ) );
-                            tch            = tch | ( ok & ( neg | ( G2 < 0.f ) ) );
-                            uw |= (uint32_t)!ok << u;
-                            tw |= (uint32_t)( !ok | neg | ( G2 < 0.f ) ) << u;
+                            // bits shifted in (the bit of test u ends at position uN - 1 - u)
+                            uw = ( uw << 1 ) | (uint32_t)!ok;
+                            tw = ( tw << 1 ) | (uint32_t)( !ok | neg | ( G2 < 0.f ) );
                         }
+                        // into place (bit u for test u); a decided test touches when its tw bit is set
+                        uw = __brev( uw ) >> ( 32u - uN );
+                        tw = __brev( tw ) >> ( 32u - uN );
+                        tch = tch | ( ( tw & ~uw ) != 0u );
                         // the circle's own j is always undecided and never tested
                         const uint32_t us = s / G;
                         if ( gl == s % G && us >= u0 && us < u0 + uN )
