@@ -553,6 +553,11 @@ namespace sesgb
                 atomicOr( &b.counts->overflow, (uint32_t)kOverflowVisBand );
         }
 
+        struct UnitStride
+        {
+        };
+        __device__ __forceinline__ uint32_t operator*( UnitStride, uint32_t u ) { return u; }
+
         __global__ void __launch_bounds__( 32 * kWarpsPerBlock ) k_visibility( Build b )
         {
             pdl_begin();
@@ -638,11 +643,12 @@ namespace sesgb
                         const float4 * qp = m.rel + gl + G * u0;
                         const float *  dp = m.dd + gl + G * u0;
                         uint32_t       uw = 0, tw = 0;
-#pragma unroll 4
+                        auto           run = [ & ]( auto stride ) {
+#pragma unroll 8
                         for ( uint32_t u = 0; u < uN; u++ )
                         {
-                            const float4 q  = qp[ G * u ];
-                            const float  dk = dp[ G * u ];
+                            const float4 q  = qp[ stride * u ];
+                            const float  dk = dp[ stride * u ];
                             const float  g  = v.dj.x * q.x + v.dj.y * q.y + v.dj.z * q.z;
                             const float  A  = fmaf( v.m2t, g, q.w );
                             const float  p2 = fmaf( -g * v.inv, g, dk );
@@ -650,12 +656,18 @@ namespace sesgb
                             const float  eG = fmaf( v.alpha, fabsf( A ), fmaf( v.beta, p2, v.gamma ) );
                             // false on NaN: the test is then left to double precision
                             const bool ok  = ( p2 > v.theta ) & ( fabsf( A ) > v.eA ) & ( fabsf( G2 ) > eG );
-                            const bool neg = A < 0.f;
-                            bur            = bur | ( ok & neg & ( G2 > 0.f ) );
+                            const bool neg  = A < 0.f;
+                            const bool gneg = G2 < 0.f; // a decided G2 is nonzero: G2 > 0 is !gneg
+                            bur             = bur | ( ok & neg & !gneg );
                             // bits shifted in (the bit of test u ends at position uN - 1 - u)
                             uw = ( uw << 1 ) | (uint32_t)!ok;
-                            tw = ( tw << 1 ) | (uint32_t)( !ok | neg | ( G2 < 0.f ) );
+                            tw = ( tw << 1 ) | (uint32_t)( !ok | neg | gneg );
                         }
+                        };
+                        if ( G == 1 )
+                            run( UnitStride {} );
+                        else
+                            run( G );
                         // into place (bit u for test u); a decided test touches when its tw bit is set
                         uw = __brev( uw ) >> ( 32u - uN );
                         tw = __brev( tw ) >> ( 32u - uN );
