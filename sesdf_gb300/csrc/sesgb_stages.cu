@@ -1313,7 +1313,8 @@ namespace sesgb
                 const float  a  = ql.w - ( xc.x * ql.x + xc.y * ql.y + xc.z * ql.z );
                 const float  c  = root * ( nn.x * ql.x + nn.y * ql.y + nn.z * ql.z );
                 const float  h1 = a - c, h2 = a + c; // K_l - x . d_l for x1 and x2
-                if ( ( v1 && fabsf( h1 ) <= eh ) || ( v2 && fabsf( h2 ) <= eh ) || ( v1 && h1 != h1 ) || ( v2 && h2 != h2 ) )
+                // inside the band, or NaN: left to double precision
+                if ( ( v1 && !( fabsf( h1 ) > eh ) ) || ( v2 && !( fabsf( h2 ) > eh ) ) )
                     return 1;
                 v1 = v1 && h1 > 0.f;
                 v2 = v2 && h2 > 0.f;
