@@ -126,7 +126,7 @@ namespace sesgb
 
         // Bitonic sort of up to 64 keys held in registers, two per lane: key
         // index lane + 32 r is held in v[r]; ascending on return.
-        __device__ __forceinline__ void warp_sort64( uint32_t & v0, uint32_t & v1, bool two )
+        template<class T> __device__ __forceinline__ void warp_sort64( T & v0, T & v1, bool two )
         {
             const uint32_t lane = lane_id();
             const uint32_t top  = two ? 64u : 32u;
@@ -136,20 +136,20 @@ namespace sesgb
                     if ( j == 32 )
                     {
                         // partner in the lane's other register; k == 64: ascending
-                        const uint32_t lo = min( v0, v1 ), hi = max( v0, v1 );
+                        const T lo = min( v0, v1 ), hi = max( v0, v1 );
                         v0 = lo;
                         v1 = hi;
                         continue;
                     }
                     const bool lower = ( lane & j ) == 0;
                     {
-                        const uint32_t p   = __shfl_xor_sync( 0xffffffffu, v0, j );
+                        const T        p   = __shfl_xor_sync( 0xffffffffu, v0, j );
                         const bool     asc = ( lane & k ) == 0;
                         v0                 = ( lower == asc ) ? min( v0, p ) : max( v0, p );
                     }
                     if ( two )
                     {
-                        const uint32_t p   = __shfl_xor_sync( 0xffffffffu, v1, j );
+                        const T        p   = __shfl_xor_sync( 0xffffffffu, v1, j );
                         const bool     asc = ( ( lane + 32u ) & k ) == 0;
                         v1                 = ( lower == asc ) ? min( v1, p ) : max( v1, p );
                     }
@@ -1381,33 +1381,63 @@ namespace sesgb
             uint32_t   p       = 0;
             uint64_t   partial = 0; // slots of the partial circles (i, j), i < j
             float      d2max = 0.f, bmax = 0.f;
-            for ( uint32_t base = 0; base < ni; base += 32 )
+            for ( uint32_t base0 = 0; base0 < ni; base0 += 64 )
             {
-                const uint32_t s   = base + lane;
-                bool           isP = false;
-                if ( s < ni )
+                // two rows of 32 neighbours: the loads of both issued before their use
+                uint32_t jj[ 2 ] = { 0u, 0u }, st[ 2 ] = { 0u, 0u }, cn[ 2 ] = { 0u, 0u };
+                float4   aa[ 2 ];
+#pragma unroll
+                for ( int h = 0; h < 2; h++ )
                 {
-                    const uint32_t j  = b.nbr[ row + s ];
-                    const float4   aj = b.atoms[ j ];
-                    const f3       d  = F3( aj.x - ai.x, aj.y - ai.y, aj.z - ai.z );
-                    const float    dd = dot( d, d );
-                    const float    Rl = aj.w + b.rp;
-                    m.rel[ s ]        = make_float4( d.x, d.y, d.z, 0.5f * ( ( Ri * Ri + dd ) - Rl * Rl ) );
-                    m.rad[ s ]        = Rl;
-                    m.nid[ s ]        = j;
-                    m.full[ s ]       = b.nbrCount[ j ] >= b.cap;
-                    isP               = b.status[ row + s ] == 1 && i < j;
-                    if ( isP && useMask )
-                        m.touch[ s ] = b.touch[ b.pairOff[ i ] + s ];
-                    d2max = fmaxf( d2max, dd );
-                    bmax  = fmaxf( bmax, Ri * Ri + dd + Rl * Rl );
+                    const uint32_t s = base0 + 32 * h + lane;
+                    if ( s < ni )
+                    {
+                        jj[ h ] = b.nbr[ row + s ];
+                        st[ h ] = b.status[ row + s ];
+                    }
                 }
-                const uint32_t mk = __ballot_sync( 0xffffffffu, isP );
-                if ( isP )
-                    m.plist[ p + __popc( mk & lanemask_lt() ) ] = (uint16_t)s;
-                p += __popc( mk );
-                if ( base < 64 )
-                    partial |= (uint64_t)mk << base;
+#pragma unroll
+                for ( int h = 0; h < 2; h++ )
+                {
+                    const uint32_t s = base0 + 32 * h + lane;
+                    if ( s < ni )
+                    {
+                        aa[ h ] = b.atoms[ jj[ h ] ];
+                        cn[ h ] = b.nbrCount[ jj[ h ] ];
+                    }
+                }
+#pragma unroll
+                for ( int h = 0; h < 2; h++ )
+                {
+                    const uint32_t base = base0 + 32 * h;
+                    if ( base >= ni )
+                        break;
+                    const uint32_t s   = base + lane;
+                    bool           isP = false;
+                    if ( s < ni )
+                    {
+                        const uint32_t j  = jj[ h ];
+                        const float4   aj = aa[ h ];
+                        const f3       d  = F3( aj.x - ai.x, aj.y - ai.y, aj.z - ai.z );
+                        const float    dd = dot( d, d );
+                        const float    Rl = aj.w + b.rp;
+                        m.rel[ s ]        = make_float4( d.x, d.y, d.z, 0.5f * ( ( Ri * Ri + dd ) - Rl * Rl ) );
+                        m.rad[ s ]        = Rl;
+                        m.nid[ s ]        = j;
+                        m.full[ s ]       = cn[ h ] >= b.cap;
+                        isP               = st[ h ] == 1 && i < j;
+                        if ( isP && useMask )
+                            m.touch[ s ] = b.touch[ b.pairOff[ i ] + s ];
+                        d2max = fmaxf( d2max, dd );
+                        bmax  = fmaxf( bmax, Ri * Ri + dd + Rl * Rl );
+                    }
+                    const uint32_t mk = __ballot_sync( 0xffffffffu, isP );
+                    if ( isP )
+                        m.plist[ p + __popc( mk & lanemask_lt() ) ] = (uint16_t)s;
+                    p += __popc( mk );
+                    if ( base < 64 )
+                        partial |= (uint64_t)mk << base;
+                }
             }
             for ( int o = 16; o > 0; o >>= 1 )
             {
@@ -2161,12 +2191,24 @@ namespace sesgb
                     count += __popc( mask );
                 }
                 __syncwarp();
-                const uint32_t held = count < kSnbrBuf ? count : kSnbrBuf;
-                warp_bitonic_sort<unsigned long long>( buf[ warp ], held, kSnbrBuf, ~0ull );
-                const uint32_t kept = held < kMaxProbeNbr ? held : kMaxProbeNbr;
+                const uint32_t     held = count < kSnbrBuf ? count : kSnbrBuf;
+                const uint32_t     kept = held < kMaxProbeNbr ? held : kMaxProbeNbr;
+                unsigned long long key0;
+                if ( held <= 64 )
+                {
+                    // in registers (the common case)
+                    key0                    = lane < held ? buf[ warp ][ lane ] : ~0ull;
+                    unsigned long long key1 = lane + 32 < held ? buf[ warp ][ lane + 32 ] : ~0ull;
+                    warp_sort64( key0, key1, held > 32 );
+                }
+                else
+                {
+                    warp_bitonic_sort<unsigned long long>( buf[ warp ], held, kSnbrBuf, ~0ull );
+                    key0 = buf[ warp ][ lane ];
+                }
                 if ( lane < kept )
                 {
-                    const uint32_t p  = (uint32_t)( buf[ warp ][ lane ] & 0xffffffffull );
+                    const uint32_t p  = (uint32_t)( key0 & 0xffffffffull );
                     const float4   pp = b.probePos[ b.nMol > 1 ? b.singList[ p ] : p ];
                     const float    wv = b.mode == 0 ? __fmul_rn( __fmul_rn( pq.x, pq.y ), pq.z ) : 0.f;
                     b.probeNbrs[ (size_t)q * kMaxProbeNbr + lane ]   = make_float4( pp.x, pp.y, pp.z, wv );
