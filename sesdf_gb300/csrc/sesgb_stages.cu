@@ -320,18 +320,34 @@ namespace sesgb
             stencil_rows( g, b.cellStart + cell_base( b, m ), fine_cell( g, ai.x, ai.y, ai.z ), rows );
             const float Ri    = ai.w + b.rp;
             uint32_t    count = 0, fp64 = 0;
-            for ( uint32_t base = 0; base < rows.total; base += 32 )
+            for ( uint32_t base0 = 0; base0 < rows.total; base0 += 64 )
             {
-                const uint32_t f    = base + lane;
-                bool           pass = false;
-                uint32_t       j    = 0;
-                if ( f < rows.total )
+                // two rows of 32 items: the loads of both issued before their use
+                uint32_t jj[ 2 ] = { 0u, 0u };
+                float4   pp[ 2 ];
+#pragma unroll
+                for ( int h = 0; h < 2; h++ )
                 {
-                    const uint32_t idx = row_item( rows, f );
-                    j                  = b.cellItems[ idx ];
-                    if ( j != i )
+                    const uint32_t f = base0 + 32 * h + lane;
+                    if ( f < rows.total )
                     {
-                        const float4 aj = b.cellPos[ idx ];
+                        const uint32_t idx = row_item( rows, f );
+                        jj[ h ]            = b.cellItems[ idx ];
+                        pp[ h ]            = b.cellPos[ idx ];
+                    }
+                }
+#pragma unroll
+                for ( int h = 0; h < 2; h++ )
+                {
+                    const uint32_t base = base0 + 32 * h;
+                    if ( base >= rows.total )
+                        break;
+                    const uint32_t f    = base + lane;
+                    bool           pass = false;
+                    const uint32_t j    = jj[ h ];
+                    if ( f < rows.total && j != i )
+                    {
+                        const float4 aj = pp[ h ];
                         const f3     dj = F3( aj.x - ai.x, aj.y - ai.y, aj.z - ai.z );
                         const float  d  = dot( dj, dj );
                         const float  R  = Ri + ( aj.w + b.rp );
@@ -345,12 +361,12 @@ namespace sesgb
                             fp64++;
                         }
                     }
+                    const uint32_t mask = __ballot_sync( 0xffffffffu, pass );
+                    const uint32_t pos  = count + __popc( mask & lanemask_lt() );
+                    if ( pass && pos < kNbrBuf )
+                        buf[ warp ][ pos ] = j;
+                    count += __popc( mask );
                 }
-                const uint32_t mask = __ballot_sync( 0xffffffffu, pass );
-                const uint32_t pos  = count + __popc( mask & lanemask_lt() );
-                if ( pass && pos < kNbrBuf )
-                    buf[ warp ][ pos ] = j;
-                count += __popc( mask );
             }
             __syncwarp();
             const uint32_t held = count < kNbrBuf ? count : kNbrBuf;
@@ -1624,35 +1640,54 @@ namespace sesgb
                 fillHere += __popc( __ballot_sync( 0xffffffffu, fill ) );
                 bandHere += __popc( __ballot_sync( 0xffffffffu, band ) );
             }
-            // slot of k in N(j) for every kept entry, found by the whole warp (one coalesced
-            // pass over the row instead of a binary search per lane)
+            // slot of k in N(j) for every kept entry, found by the whole warp: coalesced
+            // passes over the rows of four entries at a time, their loads in flight together
+            // (the row is read before its count arrives; slots past the count do not match)
             uint16_t * sjkS = reinterpret_cast<uint16_t *>( m.cand ); // free after the screening (2 kCandBuf slots)
-            for ( uint32_t e = 0; e < kept && fits; e++ )
+            for ( uint32_t e0 = 0; e0 < kept && fits; e0 += 4 )
             {
-                const uint32_t ex = m.ent[ e ].x;
-                if ( e > 0 && m.ent[ e - 1 ].x == ex )
+                uint32_t jv[ 4 ], kv[ 4 ], nv[ 4 ], pos[ 4 ];
+#pragma unroll
+                for ( int u = 0; u < 4; u++ )
                 {
-                    if ( lane == 0 )
-                        sjkS[ e ] = sjkS[ e - 1 ]; // second side of the same candidate
-                    __syncwarp();
-                    continue;
+                    const uint32_t ex = m.ent[ min( e0 + (uint32_t)u, kept - 1u ) ].x;
+                    jv[ u ]           = m.nid[ ex & 0xffffu ];
+                    kv[ u ]           = m.nid[ ex >> 16 ];
+                    pos[ u ]          = 0xffffffffu;
                 }
-                const uint32_t j = m.nid[ ex & 0xffffu ], k = m.nid[ ex >> 16 ];
-                const uint32_t nj = b.nbrCount[ j ];
-                uint32_t       pos = 0;
-                for ( uint32_t base = 0; base < nj; base += 32 )
+#pragma unroll
+                for ( int u = 0; u < 4; u++ )
+                    nv[ u ] = b.nbrCount[ jv[ u ] ];
+                uint32_t base = 0;
+                do
                 {
-                    const uint32_t s  = base + lane;
-                    const uint32_t mk = __ballot_sync( 0xffffffffu, s < nj && b.nbr[ (size_t)j * b.cap + s ] == k );
-                    if ( mk )
+                    const uint32_t s = base + lane;
+                    uint32_t       id[ 4 ];
+#pragma unroll
+                    for ( int u = 0; u < 4; u++ )
+                        id[ u ] = s < b.cap ? b.nbr[ (size_t)jv[ u ] * b.cap + s ] : 0xffffffffu;
+                    uint32_t span = 0;
+#pragma unroll
+                    for ( int u = 0; u < 4; u++ )
                     {
-                        pos = base + (uint32_t)( __ffs( mk ) - 1 );
-                        break;
+                        const uint32_t mk = __ballot_sync( 0xffffffffu, s < nv[ u ] && id[ u ] == kv[ u ] );
+                        if ( mk && pos[ u ] == 0xffffffffu )
+                            pos[ u ] = base + (uint32_t)( __ffs( mk ) - 1 );
+                        if ( pos[ u ] == 0xffffffffu )
+                            span = max( span, nv[ u ] );
                     }
+                    base += 32;
+                    if ( base >= span )
+                        break;
+                } while ( true );
+                if ( lane < 4 && e0 + lane < kept )
+                {
+                    uint32_t r = pos[ 0 ];
+#pragma unroll
+                    for ( int u = 1; u < 4; u++ )
+                        r = lane == (uint32_t)u ? pos[ u ] : r;
+                    sjkS[ e0 + lane ] = (uint16_t)( r == 0xffffffffu ? 0u : r );
                 }
-                if ( lane == 0 )
-                    sjkS[ e ] = (uint16_t)pos;
-                __syncwarp();
             }
             __syncwarp();
             uint32_t jbase = 0, gbase = 0;
