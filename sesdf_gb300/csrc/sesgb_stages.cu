@@ -305,6 +305,20 @@ namespace sesgb
         }
 
         // ---- neighbour lists ---------------------------------------------
+        // The double-precision twins of the float32 screens below are out of line: their
+        // float-to-double conversions then run only in the rare band branch instead of
+        // being hoisted into every warp (the FP64 pipe of GB300 issues one warp
+        // instruction per 64 cycles).
+        __device__ __noinline__ bool neighbor_d( float4 ai, float4 aj, float rp )
+        {
+            return dneighbor( D3( ai ), ai.w, D3( aj ), aj.w, (double)rp );
+        }
+        __device__ __noinline__ bool probe_pair_d( float4 pq, float4 pp, float rp )
+        {
+            const d3 dd = dsub( D3( pq ), D3( pp ) );
+            return __dsqrt_rn( ddot( dd, dd ) ) < 2.0 * (double)rp;
+        }
+
         __global__ void __launch_bounds__( 32 * kWarpsPerBlock ) k_neighbors( Build b )
         {
             pdl_begin();
@@ -357,7 +371,7 @@ namespace sesgb
                             pass = true;
                         else if ( m <= e )
                         {
-                            pass = dneighbor( D3( ai ), ai.w, D3( aj ), aj.w, (double)b.rp );
+                            pass = neighbor_d( ai, aj, b.rp );
                             fp64++;
                         }
                     }
@@ -1746,6 +1760,20 @@ namespace sesgb
             }
         }
 
+        // Exact position of one side of a kept probe in double precision, rounded once to
+        // float32; returns the singular flag. Out of line, so that its conversions run
+        // only for the few probes whose float-float position cannot be rounded safely.
+        __device__ __noinline__ bool fill_position_d( float4 ai, float4 aj, float4 ak, float rpf, uint32_t side, float3 & pf )
+        {
+            const double rp = (double)rpf;
+            d3           x[ 2 ];
+            double       h2 = 0.0;
+            solve_d( D3( ai ), (double)ai.w, D3( aj ), (double)aj.w, D3( ak ), (double)ak.w, rp, x[ 0 ], x[ 1 ], h2 );
+            const d3 xs = side ? x[ 1 ] : x[ 0 ];
+            pf          = make_float3( __double2float_rn( xs.x ), __double2float_rn( xs.y ), __double2float_rn( xs.z ) );
+            return singular_d( h2, rp );
+        }
+
         // The double-precision pass, one job per thread with full warps: exact
         // probe positions (the solve of findIntersectionsBetweenCircles in IEEE
         // double, rounded once to float32) and the decisions the float32 screen
@@ -1775,12 +1803,7 @@ namespace sesgb
                 if ( !solve_ff( ai, aj, ak, b.rp, side, aw == 3, pf, sing ) )
                 {
                     ffMiss++;
-                    d3         x[ 2 ];
-                    double     h2 = 0.0;
-                    solve_d( D3( ai ), (double)ai.w, D3( aj ), (double)aj.w, D3( ak ), (double)ak.w, rp, x[ 0 ], x[ 1 ], h2 );
-                    const d3 xs = side ? x[ 1 ] : x[ 0 ];
-                    pf          = make_float3( __double2float_rn( xs.x ), __double2float_rn( xs.y ), __double2float_rn( xs.z ) );
-                    sing        = singular_d( h2, rp );
+                    sing = fill_position_d( ai, aj, ak, b.rp, side, pf );
                 }
                 if ( aw == 3 )
                 {
@@ -2179,7 +2202,6 @@ namespace sesgb
             const uint32_t                warp = threadIdx.x >> 5, lane = lane_id();
             const uint32_t                Q    = min( b.counts->Q, b.capProbes );
             const float                   t2   = 2.f * b.rp;
-            const double                  t2d  = 2.0 * (double)b.rp;
             uint32_t                      fp64 = 0, trunc = 0;
             for ( uint32_t q = blockIdx.x * kWarpsPerBlock + warp; q < Q; q += gridDim.x * kWarpsPerBlock )
             {
@@ -2211,8 +2233,7 @@ namespace sesgb
                                 pass = true;
                             else if ( !( m > e ) )
                             {
-                                const d3 dd = dsub( D3( pq ), D3( pp ) );
-                                pass        = __dsqrt_rn( ddot( dd, dd ) ) < t2d;
+                                pass = probe_pair_d( pq, pp, b.rp );
                                 fp64++;
                             }
                             if ( pass )
