@@ -1953,32 +1953,50 @@ namespace sesgb
             }
         }
 
-        __global__ void k_segment_counts( Build b )
+        // Segment counts per partial circle, and the list of the circles carrying
+        // segments (in any order) for the full-warp segment pass: one counter atomic per
+        // block and step (a single counter taken by every warp serialises at L2).
+        __global__ void __launch_bounds__( 256 ) k_segment_counts( Build b )
         {
             pdl_begin();
-            const uint32_t C1 = min( b.counts->C1, b.capC1 );
-            for ( uint32_t t = blockIdx.x * blockDim.x + threadIdx.x; t < C1; t += gridDim.x * blockDim.x )
+            __shared__ uint32_t warpBase[ 8 ];
+            __shared__ uint32_t blockBase;
+            const uint32_t      C1   = min( b.counts->C1, b.capC1 );
+            const uint32_t      warp = threadIdx.x >> 5, lane = lane_id();
+            for ( uint32_t t0 = blockIdx.x * blockDim.x; t0 < C1; t0 += gridDim.x * blockDim.x )
             {
-                const uint32_t cc = b.ccount[ t ];
-                const uint32_t c  = min( cc, b.segCap );
-                b.segCnt[ t ]     = c / 2u;
-                if ( cc > b.segCap )
-                    atomicAdd( &b.counts->segTruncated, 1u );
-                // circles carrying segments, in any order: one atomic per warp (a single
-                // counter taken by every circle serialises)
-                const uint32_t active = __activemask();
-                const uint32_t mk     = __ballot_sync( active, cc >= 2 );
-                const uint32_t leader = (uint32_t)( __ffs( active ) - 1 );
-                uint32_t       base   = 0;
-                if ( lane_id() == leader && mk )
-                    base = atomicAdd( &b.counts->segCircles, (uint32_t)__popc( mk ) );
-                base = __shfl_sync( active, base, leader );
+                const uint32_t t  = t0 + threadIdx.x;
+                uint32_t       cc = 0;
+                if ( t < C1 )
+                {
+                    cc            = b.ccount[ t ];
+                    b.segCnt[ t ] = min( cc, b.segCap ) / 2u;
+                    if ( cc > b.segCap )
+                        atomicAdd( &b.counts->segTruncated, 1u );
+                }
+                const uint32_t mk = __ballot_sync( 0xffffffffu, cc >= 2 );
+                if ( lane == 0 )
+                    warpBase[ warp ] = (uint32_t)__popc( mk );
+                __syncthreads();
+                if ( threadIdx.x == 0 )
+                {
+                    uint32_t tot = 0;
+                    for ( uint32_t w = 0; w < ( blockDim.x >> 5 ); w++ )
+                    {
+                        const uint32_t c = warpBase[ w ];
+                        warpBase[ w ]    = tot;
+                        tot += c;
+                    }
+                    blockBase = tot ? atomicAdd( &b.counts->segCircles, tot ) : 0u;
+                }
+                __syncthreads();
                 if ( cc >= 2 )
                 {
-                    const uint32_t at = base + __popc( mk & lanemask_lt() );
+                    const uint32_t at = blockBase + warpBase[ warp ] + __popc( mk & lanemask_lt() );
                     if ( at < b.capC1 )
                         b.segList[ at ] = t;
                 }
+                __syncthreads(); // warpBase and blockBase are rewritten by the next step
             }
         }
 
