@@ -588,12 +588,14 @@ namespace sesgb
         };
         __device__ __forceinline__ uint32_t operator*( UnitStride, uint32_t u ) { return u; }
 
-        __global__ void __launch_bounds__( 32 * kWarpsPerBlock ) k_visibility( Build b )
+        // one warp (one atom) per block, as k_probes: a slot is freed when its atom is done
+        constexpr int kVisWarps = 1;
+        __global__ void __launch_bounds__( 32 * kVisWarps, 32 / kVisWarps ) k_visibility( Build b )
         {
             pdl_begin();
             extern __shared__ __align__( 16 ) unsigned char smemRaw[];
             const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
-            const uint32_t i    = blockIdx.x * kWarpsPerBlock + warp;
+            const uint32_t i    = blockIdx.x * kVisWarps + warp;
             if ( i >= b.n )
                 return;
             const VisSmem  m   = vis_smem( smemRaw + warp * vis_smem_per_warp( b.cap ), b.cap );
@@ -881,7 +883,7 @@ namespace sesgb
             }
         }
 
-        __host__ inline size_t visibility_smem( uint32_t cap ) { return vis_smem_per_warp( cap ) * kWarpsPerBlock; }
+        __host__ inline size_t visibility_smem( uint32_t cap ) { return vis_smem_per_warp( cap ) * kVisWarps; }
 
         // ---- sectors, complete circles, partial-circle numbering -----------
         // sector of buildConvexPatchesSectors (operations.inl:186-213) in
@@ -1179,7 +1181,9 @@ namespace sesgb
         // accumulated rounding of its ~25 dependent operations).
         constexpr float kSolve = 1.0f / 262144.0f; // 2^-18
 
-        constexpr int kProbeWarps = 4;   // warps per block of k_probes
+        // One warp per block: the work of an atom varies a lot, and a block's slot (its
+        // registers and shared memory) is freed only when its last warp ends.
+        constexpr int kProbeWarps = 1;   // warps per block of k_probes
         constexpr int kCandBuf    = 64;  // candidates queued per warp
         constexpr int kProbeBuf   = 128; // probes of one atom (the reference's per-block buffer, operations.inl:248)
 
@@ -1393,7 +1397,7 @@ namespace sesgb
         // whose far atoms are neighbours. Entries of the atom's probe list are kept
         // in order (circle (i, j), then k, then x1 before x2) and written as one
         // chunk; positions and undecided flags are completed by k_probe_jobs.
-        __global__ void __launch_bounds__( 32 * kProbeWarps, 8 ) k_probes( Build b )
+        __global__ void __launch_bounds__( 32 * kProbeWarps, 32 / kProbeWarps ) k_probes( Build b )
         {
             pdl_begin();
             extern __shared__ __align__( 16 ) unsigned char smemRaw[];
@@ -2596,7 +2600,7 @@ namespace sesgb
     {
         if ( !b.n )
             return;
-        pdl_launch( k_visibility, blocks_for( b.n, kWarpsPerBlock ), 32 * kWarpsPerBlock, visibility_smem( b.cap ), s, b );
+        pdl_launch( k_visibility, blocks_for( b.n, kVisWarps ), 32 * kVisWarps, visibility_smem( b.cap ), s, b );
         counted();
     }
     void launch_visibility_resolve( const Build & b, cudaStream_t s )
