@@ -674,7 +674,7 @@ namespace sesgb
                         const uint32_t uN = U - u0 < 32 ? U - u0 : 32;
                         const float4 * qp = m.rel + gl + G * u0;
                         const float *  dp = m.dd + gl + G * u0;
-                        uint32_t       uw = 0, tw = 0;
+                        uint32_t       uw = 0, tw = 0, bw = 0;
                         auto           run = [ & ]( auto stride ) {
 #pragma unroll 8
                         for ( uint32_t u = 0; u < uN; u++ )
@@ -687,13 +687,15 @@ namespace sesgb
                             const float  G2 = fmaf( A, A, -v.r2x4 * p2 );
                             const float  eG = fmaf( v.alpha, fabsf( A ), fmaf( v.beta, p2, v.gamma ) );
                             // false on NaN: the test is then left to double precision
-                            const bool ok  = ( p2 > v.theta ) & ( fabsf( A ) > v.eA ) & ( fabsf( G2 ) > eG );
-                            const bool neg  = A < 0.f;
-                            const bool gneg = G2 < 0.f; // a decided G2 is nonzero: G2 > 0 is !gneg
-                            bur             = bur | ( ok & neg & !gneg );
-                            // bits shifted in (the bit of test u ends at position uN - 1 - u)
-                            uw = ( uw << 1 ) | (uint32_t)!ok;
-                            tw = ( tw << 1 ) | (uint32_t)( !ok | neg | gneg );
+                            const bool ok = ( p2 > v.theta ) & ( fabsf( A ) > v.eA ) & ( fabsf( G2 ) > eG );
+                            // bits shifted in (the bit of test u ends at position uN - 1 - u); the
+                            // sign bits of A and G2 go in without a compare: a decided test has
+                            // A != 0 and G2 != 0, so they are A < 0 and G2 < 0 there (undecided
+                            // bits are masked by uw below)
+                            const uint32_t ab = __float_as_uint( A ), gb = __float_as_uint( G2 );
+                            uw                = ( uw << 1 ) | (uint32_t)!ok;
+                            tw                = __funnelshift_l( ab | gb, tw, 1 );  // A < 0 or G2 < 0: touches
+                            bw                = __funnelshift_l( ab & ~gb, bw, 1 ); // A < 0 and G2 > 0: buries
                         }
                         };
                         if ( G == 1 )
@@ -701,9 +703,12 @@ namespace sesgb
                         else
                             run( G );
                         // into place (bit u for test u); a decided test touches when its tw bit is set
-                        uw = __brev( uw ) >> ( 32u - uN );
-                        tw = __brev( tw ) >> ( 32u - uN );
+                        uw  = __brev( uw ) >> ( 32u - uN );
+                        tw  = __brev( tw ) >> ( 32u - uN );
+                        bw  = __brev( bw ) >> ( 32u - uN );
                         tch = tch | ( ( tw & ~uw ) != 0u );
+                        bur = bur | ( ( bw & ~uw ) != 0u );
+                        tw |= uw; // an undecided test may touch (the touch mask is conservative)
                         // the circle's own j is always undecided and never tested
                         const uint32_t us = s / G;
                         if ( gl == s % G && us >= u0 && us < u0 + uN )
