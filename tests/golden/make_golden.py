@@ -28,6 +28,10 @@ RP = 1.4
 def golden_inputs():
     cases = {k: v for k, v in hand_cases().items() if v.shape[0] > 0}
     cases["globule2k"] = synth.globule(2000, 1000)
+    # the reference's own sample structures (tests/golden/structures.npz, made by make_structures.py)
+    with np.load(os.path.join(HERE, "structures.npz")) as s:
+        for e in ("1AGA", "101M"):
+            cases[e] = s[e]
     return cases
 
 

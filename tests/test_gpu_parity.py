@@ -5,6 +5,8 @@ neighbours) must be identical; probe positions are compared bit for bit (both
 sides solve in double precision with the same operations and round to float32);
 sectors and tori, which the GPU computes in float32, within 1e-4 A (rad).
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -101,6 +103,20 @@ def test_globule_2k(mode):
 @pytest.mark.parametrize("mode", ["full", "exterior"])
 def test_globule_20k(mode):
     atoms = synth.globule(20000, 1500)
+    out, o = run_both(atoms, mode)
+    compare(atoms, out, o, mode)
+
+
+STRUCTURES = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "structures.npz")
+
+
+@pytest.mark.parametrize("entry", ["1AGA", "101M", "1VIS", "7SC0"])
+@pytest.mark.parametrize("mode", ["full", "exterior"])
+def test_sample_structures(entry, mode):
+    """The reference's own sample structures (MMTF, read as its loader does; coordinates on a
+    0.001 A grid, so exact ties in the predicates are common)."""
+    with np.load(STRUCTURES) as s:
+        atoms = s[entry]
     out, o = run_both(atoms, mode)
     compare(atoms, out, o, mode)
 
