@@ -1,0 +1,118 @@
+"""Headless depth and normal images of the SES by sphere tracing its signed distance.
+
+The reference draws its primitives through an OpenGL renderer; here the image is an array and needs no
+graphics stack: each pixel's ray advances by a step that never crosses the surface, the signed distance
+of ``sesgb_sdf`` (``SesBuild.sdf``) being evaluated for all live rays at once per step.
+
+Safe steps. With kind the primitive that decided the value (1 atom outside the SAS, 2 beyond the band
+outside, 3 SAS sphere, 4 circle arc, 5 probe, 0 deeper than the band):
+  * outside the SAS (kinds 1, 2) the value is min_i(|x - c_i| - r_i) (clamped at the band), so value - rp
+    bounds the distance to the SAS, and the SES lies inside the SAS;
+  * inside the SAS (kinds 3-5) the value is rp - dist(x, E) with E the probe-centre positions: every SES
+    point y has dist(y, E) = rp, so |x - y| >= rp - dist(x, E): the value bounds the distance to the SES.
+A ray stops when an inside-SAS value falls below ``eps`` (a hit at depth t) or t passes ``t_far``.
+Normals are the normalised central differences of the signed distance at the hit points.
+
+The tracer takes the signed distance as a function of (m, 3) float32 points, so the same code runs on
+the GPU build (``gpu_sdf_fn``) and, in the tests, on the FP64 oracle.
+"""
+from __future__ import annotations
+
+import numpy as np
+
+INSIDE_SAS = (3, 4, 5)
+
+
+def camera_rays(eye, target, up, fov_deg: float, width: int, height: int):
+    """Unit ray directions (height*width, 3) float64 of a pinhole camera, row-major from the top left."""
+    eye = np.asarray(eye, np.float64)
+    f = np.asarray(target, np.float64) - eye
+    f /= np.linalg.norm(f)
+    r = np.cross(f, np.asarray(up, np.float64))
+    r /= np.linalg.norm(r)
+    u = np.cross(r, f)
+    h = np.tan(np.radians(fov_deg) / 2.0)
+    xs = (2.0 * (np.arange(width) + 0.5) / width - 1.0) * h * width / height
+    ys = (1.0 - 2.0 * (np.arange(height) + 0.5) / height) * h
+    d = f[None, None, :] + xs[None, :, None] * r[None, None, :] + ys[:, None, None] * u[None, None, :]
+    d /= np.linalg.norm(d, axis=2, keepdims=True)
+    return d.reshape(-1, 3)
+
+
+def sphere_trace(sdf_fn, origin, dirs, probe_radius: float, t_near: float, t_far: float, eps: float = 1e-3,
+                 max_steps: int = 256):
+    """Depth t (float64 [m], inf where the ray misses) of the first SES point along origin + t * dirs.
+    sdf_fn(points float32 [k, 3]) -> (value [k], kind [k]) as numpy arrays."""
+    m = dirs.shape[0]
+    t = np.full(m, float(t_near))
+    depth = np.full(m, np.inf)
+    live = np.arange(m)
+    o = np.asarray(origin, np.float64)
+    for _ in range(max_steps):
+        if live.size == 0:
+            break
+        p = (o[None, :] + t[live, None] * dirs[live]).astype(np.float32)
+        v, k = sdf_fn(p)
+        v = np.asarray(v, np.float64)
+        k = np.asarray(k)
+        inside = np.isin(k, INSIDE_SAS)
+        hit = inside & (v < eps)
+        depth[live[hit]] = t[live[hit]]
+        step = np.where(inside, v, v - probe_radius)
+        # deeper than the band (kind 0) cannot be reached with these steps; such a ray stops as a hit
+        hit |= k == 0
+        depth[live[k == 0]] = t[live[k == 0]]
+        t[live] += np.where(hit, 0.0, np.maximum(step, 0.25 * eps))
+        live = live[~hit & (t[live] <= t_far)]
+    return depth
+
+
+def normals(sdf_fn, points, h: float = 1e-2):
+    """Unit gradients (float64 [k, 3]) of the signed distance at points by central differences."""
+    p = np.asarray(points, np.float64)
+    g = np.zeros_like(p)
+    for a in range(3):
+        e = np.zeros(3)
+        e[a] = h
+        vp, _ = sdf_fn((p + e).astype(np.float32))
+        vm, _ = sdf_fn((p - e).astype(np.float32))
+        g[:, a] = (np.asarray(vp, np.float64) - np.asarray(vm, np.float64)) / (2 * h)
+    n = np.linalg.norm(g, axis=1, keepdims=True)
+    return g / np.where(n > 0, n, 1.0)
+
+
+def depth_image(sdf_fn, atoms, probe_radius: float, width: int = 128, height: int = 128, view=(0.3, -1.0, 0.5),
+                fov_deg: float = 40.0, eps: float = 1e-3, with_normals: bool = True):
+    """Depth (height, width) float32 (inf = background) and normals (height, width, 3) float32 (0 where
+    the ray misses) of the SES of atoms seen from the direction view, the camera framing the SAS bounds."""
+    a = np.asarray(atoms, np.float64)
+    lo = (a[:, :3] - a[:, 3:4] - probe_radius).min(axis=0)
+    hi = (a[:, :3] + a[:, 3:4] + probe_radius).max(axis=0)
+    centre = 0.5 * (lo + hi)
+    radius = 0.5 * np.linalg.norm(hi - lo)
+    v = np.asarray(view, np.float64)
+    v /= np.linalg.norm(v)
+    dist = radius / np.sin(np.radians(fov_deg) / 2.0)
+    eye = centre - dist * v
+    up = (0.0, 0.0, 1.0) if abs(v[2]) < 0.9 else (0.0, 1.0, 0.0)
+    dirs = camera_rays(eye, centre, up, fov_deg, width, height)
+    depth = sphere_trace(sdf_fn, eye, dirs, probe_radius, max(dist - radius, 0.0), dist + radius, eps)
+    nrm = np.zeros((width * height, 3))
+    hit = np.isfinite(depth)
+    if with_normals and hit.any():
+        nrm[hit] = normals(sdf_fn, eye[None, :] + depth[hit, None] * dirs[hit])
+    return depth.reshape(height, width).astype(np.float32), nrm.reshape(height, width, 3).astype(np.float32)
+
+
+def gpu_sdf_fn(build):
+    """The signed distance of a built full-surface SesBuild on the GPU, as a function of host points."""
+    import torch
+
+    def fn(points):
+        q = torch.from_numpy(np.ascontiguousarray(points, np.float32)).cuda()
+        out = torch.empty(q.shape[0], dtype=torch.float32, device="cuda")
+        kind = torch.empty(q.shape[0], dtype=torch.int32, device="cuda")
+        build.sdf(q.data_ptr(), q.shape[0], out.data_ptr(), kind.data_ptr(), torch.cuda.current_stream().cuda_stream)
+        return out.cpu().numpy(), kind.cpu().numpy()
+
+    return fn
