@@ -1,24 +1,26 @@
 // sesgb_stages.cu -- the kernels of the SES build (full surface and exterior only).
 //
 // Stage map (reference functions restated, file:line of PlathC/SESDF):
-//   k_hash / k_gather        AccelerationGrid::build, computeHashes, buildAccelerationGrid
+//   k_hash / radix sort / k_gather   AccelerationGrid::build, computeHashes, buildAccelerationGrid
 //                            (sesdf/src/cuda/grid.cu:15-132) -- same cell hash and stable order
 //   k_neighbors              findCirclesBetweenAtoms (sesdf/src/sesdf/operations.cu:34-124)
-//   k_visibility             computeCirclesVisibilityStatus (operations.cu:126-204; ssesdf :169-244)
+//   k_visibility (+ _band, _final)   computeCirclesVisibilityStatus (operations.cu:126-204; ssesdf :169-244)
 //   k_emit                   scans of findCircles + buildConvexPatchesSectors
 //                            (sesdf/include/bcs/sesdf/operations.inl:46-93,175-228)
-//   k_candidates/k_triplets  findIntersectionsBetweenCircles (operations.inl:230-486; ssesdf operation.inl:100-351)
+//   k_probes / k_probe_jobs  findIntersectionsBetweenCircles (operations.inl:230-486; ssesdf operation.inl:100-351)
 //   k_place/k_lists          thrust::sort by |w| + fillIntersections (operations.inl:128-141; operations.cu:206-269;
 //                            ssesdf/operations.cu:287-329)
-//   k_segments               buildConicPatches + buildSegments (operations.inl:488-668)
+//   k_segment_counts/k_segments      buildConicPatches + buildSegments (operations.inl:488-668)
 //   k_probe_neighbors        handleIntersectionSingularities + findIntersectionsNeighbors (operations.cu:14-32,271-338)
-//   k_tori                   fillCircles (ssesdf/operations.cu:246-285)
+//   k_tori_count/k_tori      fillCircles (ssesdf/operations.cu:246-285)
+//   k_sdf                    signed distance at query points and its adjoint (no reference counterpart)
 //
 // Every predicate is first evaluated in float32 in coordinates relative to the
 // owning atom; when its margin is inside a conservative band (kRel times the
-// magnitudes involved, about 30x the float32 error bound) it is decided by the
-// double-precision twin in sesgb_device.cuh, which evaluates the reference's
-// formula exactly as the FP64 oracle does.
+// magnitudes involved, about 30x the float32 error bound) it is decided again,
+// in float-float (pairs of float32 with an a-priori error bound) where that
+// settles it and otherwise by the double-precision twin in sesgb_device.cuh,
+// which evaluates the reference's formula exactly as the FP64 oracle does.
 #include <atomic>
 #include <cfloat>
 
