@@ -20,6 +20,9 @@ from __future__ import annotations
 import numpy as np
 
 
+MAX_VOXELS = 1 << 28  # the labels take 4 bytes per voxel
+
+
 def accessible_grid(atoms: np.ndarray, probe_radius: float, h: float = 0.25):
     """Boolean grid (nx, ny, nz) of voxel centres outside every SAS sphere, and the centre of voxel 0.
     The grid covers the SAS bounds with two voxels of margin, so its border is exterior."""
@@ -28,6 +31,8 @@ def accessible_grid(atoms: np.ndarray, probe_radius: float, h: float = 0.25):
     lo = (a[:, :3] - R[:, None]).min(axis=0) - 2 * h
     hi = (a[:, :3] + R[:, None]).max(axis=0) + 2 * h
     dims = np.ceil((hi - lo) / h).astype(np.int64) + 1
+    if int(np.prod(dims)) > MAX_VOXELS:
+        raise ValueError(f"a {dims.tolist()} grid at h = {h} A exceeds {MAX_VOXELS} voxels: use a larger h")
     occupied = np.zeros(tuple(dims), dtype=bool)
     # rasterise each SAS sphere over its bounding cube of voxels, grouped by radius
     for rad in np.unique(R):

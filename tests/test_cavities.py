@@ -51,3 +51,10 @@ def test_single_atom_and_globule():
     assert sizes[ext] == sizes[1:].max()  # the exterior is the largest component
     assert np.mean(c["probe_resolved"]) > 0.9
     assert not np.any(c["probe_in_cavity"] & ~c["probe_resolved"])
+
+
+def test_grid_size_guard():
+    import pytest
+    atoms = np.array([[0, 0, 0, 1.7], [400, 0, 0, 1.7], [0, 400, 0, 1.7], [0, 0, 400, 1.7]], np.float32)
+    with pytest.raises(ValueError):
+        cavities.accessible_grid(atoms, RP, h=0.25)
