@@ -14,6 +14,7 @@
 #ifndef SESGB_H
 #define SESGB_H
 
+#include <stddef.h>
 #include <stdint.h>
 
 #ifdef __cplusplus
@@ -267,6 +268,14 @@ int sesgb_ses_area_backward( sesgb_ctx * ctx, const float * host_grad_parts, flo
 
 /* Number of kernels this library has launched in this process (host-side count). */
 uint64_t sesgb_launch_count( void );
+
+/* Atoms of an MMTF structure file held in memory (data, size bytes; no compression): the first
+ * model's atoms as float4 (x, y, z, vdW radius) in file order, the radius by element as the
+ * reference's loader gives it (replaces bcs::load, sesdf/src/core/loader.cpp:14-71, for MMTF; the
+ * C++ bcs::load of include/bcs/core/loader.hpp reads a file through it). *n receives the atom count;
+ * with capacity below it nothing is written and SESGB_ERR_OVERFLOW is returned; a document that
+ * cannot be read gives SESGB_ERR_INVALID. Host only, no GPU needed. */
+int sesgb_load_mmtf( const void * data, size_t size, float * atoms_xyzr, uint32_t capacity, uint32_t * n );
 
 const char * sesgb_error_string( int status );
 const char * sesgb_last_error( const sesgb_ctx * ctx );

@@ -32,6 +32,7 @@ EXPORTS = [
     "sesgb_launch_count", "sesgb_build_async", "sesgb_finish", "sesgb_sort_atoms_noalloc",
     "sesgb_create_batch", "sesgb_batch_molecules", "sesgb_molecule_record", "sesgb_get_full_molecule",
     "sesgb_get_exterior_molecule", "sesgb_sdf", "sesgb_sdf_backward", "sesgb_ses_area", "sesgb_ses_area_backward",
+    "sesgb_load_mmtf",
 ]
 SDF_BAND = 3.0
 MOL_FIELDS = ["atoms", "sectors", "full_circles", "partial_circles", "probes", "singular_probes", "segments", "tori",
@@ -107,6 +108,7 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         for f in ("sesgb_max_neighbor_per_atom", "sesgb_max_intersections_per_circle", "sesgb_max_intersection_neighbors"):
             getattr(lib, f).argtypes = [P]
             getattr(lib, f).restype = ctypes.c_uint16
+        lib.sesgb_load_mmtf.argtypes = [P, ctypes.c_size_t, P, U32, ctypes.POINTER(U32)]
         lib.sesgb_error_string.argtypes = [I32]
         lib.sesgb_error_string.restype = ctypes.c_char_p
         lib.sesgb_last_error.argtypes = [P]
@@ -148,6 +150,27 @@ def aabb(atoms: np.ndarray) -> np.ndarray:
     lo = (a[:, :3] - a[:, 3:4]).min(0)
     hi = (a[:, :3] + a[:, 3:4]).max(0)
     return np.concatenate([lo, hi]).astype(np.float32)
+
+
+def load_mmtf(data: bytes) -> np.ndarray:
+    """(N, 4) float32 atoms of the first model of an MMTF document (bytes, gzip-compressed or not)
+    through the library's native reader (sesgb_load_mmtf)."""
+    import gzip
+
+    if data[:2] == b"\x1f\x8b":
+        data = gzip.decompress(data)
+    lib = load_library()
+    n = ctypes.c_uint32()
+    buf = ctypes.create_string_buffer(bytes(data), len(data))
+    st = lib.sesgb_load_mmtf(buf, len(data), None, 0, ctypes.byref(n))
+    if st == -1:
+        raise SesgbError("sesgb_load_mmtf: not a readable MMTF document")
+    out = np.zeros((n.value, 4), np.float32)
+    if n.value:
+        st = lib.sesgb_load_mmtf(buf, len(data), out.ctypes.data, n.value, ctypes.byref(n))
+        if st != 0:
+            raise SesgbError(f"sesgb_load_mmtf: {lib.sesgb_error_string(st).decode()}")
+    return out
 
 
 class SesBuild:

@@ -128,6 +128,45 @@ def test_minimal_document():
     assert np.array_equal(mmtf.load_bytes(gzip.compress(doc)), atoms)
 
 
+def minimal_document(elements=("C", "O"), coords=(1000, 500, -250)):
+    def mp_str(s):
+        b = s.encode()
+        return bytes([0xA0 | len(b)]) + b
+
+    def mp_bin(b):
+        return bytes([0xC4, len(b)]) + b
+
+    xs = header(10, len(coords), 1000) + struct.pack(f">{len(coords)}h", *coords)
+    group = bytes([0x81]) + mp_str("elementList") + bytes([0x90 | len(elements)]) + b"".join(mp_str(e) for e in elements)
+    return (bytes([0x87])
+            + mp_str("xCoordList") + mp_bin(xs) + mp_str("yCoordList") + mp_bin(xs) + mp_str("zCoordList") + mp_bin(xs)
+            + mp_str("groupTypeList") + mp_bin(header(4, 1) + struct.pack(">i", 0))
+            + mp_str("groupList") + bytes([0x91]) + group
+            + mp_str("chainsPerModel") + bytes([0x91, 1])
+            + mp_str("groupsPerChain") + bytes([0x91, 1]))
+
+
+def test_native_reader():
+    """sesgb_load_mmtf (C++, in the library) reads what the Python reader reads, and reports errors."""
+    import ctypes
+
+    from sesdf_gb300 import api
+    doc = minimal_document(("C", "fe", "Xx"))
+    got = api.load_mmtf(doc)
+    assert np.array_equal(got, mmtf.load_bytes(doc))
+    assert np.array_equal(got[:, 3], np.array([1.77, 2.44, 1.20], np.float32))
+    import gzip
+    assert np.array_equal(api.load_mmtf(gzip.compress(doc)), got)
+    lib = api.load_library()
+    n = ctypes.c_uint32()
+    small = np.zeros((1, 4), np.float32)
+    assert lib.sesgb_load_mmtf(doc, len(doc), small.ctypes.data, 1, ctypes.byref(n)) == -3 and n.value == 3
+    for bad in (b"", b"\x93\x01\x02", doc[:40], b"\xc1" + doc):
+        assert lib.sesgb_load_mmtf(bad, len(bad), None, 0, ctypes.byref(n)) == -1, bad[:8]
+    with pytest.raises(api.SesgbError):
+        api.load_mmtf(b"\x80")
+
+
 def test_structure_fixture():
     with np.load(STRUCTURES) as s:
         sizes = {k: s[k].shape for k in s.files}
@@ -149,6 +188,11 @@ def test_against_reference_checkout():
     with np.load(STRUCTURES) as s:
         for k in s.files:
             assert np.array_equal(mmtf.load(os.path.join(REFERENCE, "samples", f"{k}.mmtf")), s[k]), k
+    from sesdf_gb300 import api
+    for path in sorted(os.listdir(os.path.join(REFERENCE, "samples"))):
+        if path.endswith(".mmtf"):
+            data = open(os.path.join(REFERENCE, "samples", path), "rb").read()
+            assert np.array_equal(api.load_mmtf(data), mmtf.load_bytes(data)), path
     msgpack = pytest.importorskip("msgpack")
     data = open(os.path.join(REFERENCE, "samples", "101M.mmtf"), "rb").read()
     assert mmtf.unpack_msgpack(data) == msgpack.unpackb(data, raw=False)
