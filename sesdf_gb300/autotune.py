@@ -10,8 +10,6 @@ by the register and shared-memory budgets of the kernels and are not tuned.
 """
 from __future__ import annotations
 
-import numpy as np
-
 from .api import SesBatch
 
 DEFAULT_CAP = 128

@@ -14,7 +14,6 @@ from __future__ import annotations
 
 import ctypes
 import math
-import os
 
 import numpy as np
 

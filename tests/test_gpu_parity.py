@@ -10,7 +10,6 @@ import os
 import numpy as np
 import pytest
 
-import canon
 from cases import hand_cases
 from oracle import oracle
 from sesdf_gb300 import SesBuild, synth
