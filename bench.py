@@ -341,50 +341,69 @@ def sdf_extra(flush):
     return res
 
 
-def profiled(kernel: str) -> dict:
-    """From the kernel's committed ncu summary (profiles/<kernel>_assembly100k.txt): DRAM bytes per launch
-    and the issue-slot, ALU-pipe and FMA-pipe utilisations of the same capture (fractions)."""
-    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles", f"{kernel}_assembly100k.txt")
+def profiled(kernel: str, workload: str = "assembly100k") -> dict:
+    """From the kernel's committed ncu summary (profiles/<kernel>_<workload>.txt): DRAM bytes and warp
+    instructions per launch, threads per instruction, and the issue-slot, ALU-pipe and FMA-pipe
+    utilisations of the same capture (fractions)."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "profiles", f"{kernel}_{workload}.txt")
     out = {}
     keys = {"dram_bytes_per_launch:": "traffic", "issue active %": "issue_active", "ALU pipe %": "alu_pipe",
-            "FMA pipe %": "fma_pipe", "threads per instruction": "threads_per_instruction"}
+            "FMA pipe %": "fma_pipe", "threads per instruction": "threads_per_instruction",
+            "warp instructions": "warp_instructions"}
     try:
         with open(path) as f:
             for line in f:
                 for k, name in keys.items():
                     if line.startswith(k):
                         v = float(line[len(k):].split()[0])
-                        out[name] = int(v) if name == "traffic" else (round(v / 100, 3) if "%" in k else v)
+                        out[name] = int(v) if name in ("traffic", "warp_instructions") else (
+                            round(v / 100, 3) if "%" in k else v)
     except (OSError, ValueError):
         pass
     return out
 
 
-def roofline(stages, counts, nbr, n_atoms):
-    """The dominant kernel of the build (k_visibility or k_probes, one launch per build):
-    algorithmic bytes and flops per launch over its CUDA-event time in the timed builds."""
+ISSUE_SLOTS = 152 * 4  # SMs x warp schedulers (one warp instruction per scheduler and cycle)
+
+
+def issue_roofline(kernel: str, ms: float, sm_mhz: float, bytes_alg: float, workload: str = "assembly100k") -> dict:
+    """Issue-rate roofline of a SIMT kernel that is not a dense contraction and not HBM-bound: the warp
+    instructions of one launch (committed ncu summary of the same workload) over its CUDA-event time,
+    against 152 SMs x 4 schedulers x the SM clock sampled during the timed builds. lane_efficiency =
+    threads per instruction / 32; useful_lane_frac = frac x lane_efficiency is the fraction of the SIMT
+    lanes' peak that does work. The HBM fraction (algorithmic bytes over the same time) is secondary."""
     hbm, sm_max, src = peaks()
+    prof = profiled(kernel, workload)
+    clk = sm_mhz or sm_max
+    peak = ISSUE_SLOTS * clk * 1e6 / 1e9  # G warp instructions/s
+    inst = prof.get("warp_instructions")
+    achieved = inst / (ms * 1e-3) / 1e9 if inst else None
+    lane = prof["threads_per_instruction"] / 32 if "threads_per_instruction" in prof else None
+    frac = achieved / peak if achieved else None
+    hbm_achieved = bytes_alg / (ms * 1e-3) / 1e9
+    return {"kernel": kernel, "bound": "issue", "achieved": round(achieved, 1) if achieved else None, "peak": round(peak, 1),
+            "unit": "G warp-instructions/s", "frac": round(frac, 4) if frac else None,
+            "traffic": prof.get("traffic"), "lane_efficiency": round(lane, 4) if lane else None,
+            "useful_lane_frac": round(frac * lane, 4) if frac and lane else None,
+            "warp_instructions_per_launch": inst, "ms_per_launch": round(ms, 4),
+            "peak_basis": f"152 SMs x 4 schedulers x {clk:.0f} MHz (SM clock sampled during the timed builds)",
+            "profile": f"profiles/{kernel}_{workload}.txt",
+            "hbm": {"achieved": round(hbm_achieved, 1), "peak": hbm, "unit": "GB/s", "frac": round(hbm_achieved / hbm, 4),
+                    "bytes_per_launch": bytes_alg, "peak_source": src}}
+
+
+def roofline(stages, counts, n_atoms, sm_mhz):
+    """The dominant kernel of the build (k_visibility or k_probes, one launch per build), by its
+    CUDA-event time in the timed builds."""
     P, C1, I = counts["pairs"], counts["partial_circles"], counts["probes"]
-    nb = nbr.astype(np.float64)
-    fp32_peak = FP32_LANES * 2 * sm_max * 1e6 / 1e12
     if stages.get("probes", 0.0) > stages.get("visibility", 0.0):
         kernel, ms = "k_probes", stages["probes"]
         # staged neighbourhood (ids, atoms, statuses, neighbour counts), touch masks, staged probes and jobs
         bytes_alg = 25.0 * P + 8.0 * C1 + 64.0 * I + 36.0 * n_atoms
-        flops_alg = 180.0 * counts.get("candidates", 0)  # solve, plane occlusion tests, singular test
     else:
         kernel, ms = "k_visibility", stages["visibility"]
         bytes_alg = 21.0 * P + 32.0 * n_atoms  # neighbour ids + neighbour atoms + status + per-atom I/O
-        flops_alg = 30.0 * float(np.sum(nb * np.maximum(nb - 1, 0)))  # one circle-vs-atom test
-    achieved = bytes_alg / (ms * 1e-3) / 1e9
-    prof = profiled(kernel)
-    return {"kernel": kernel, "bound": "hbm", "achieved": round(achieved, 1), "peak": hbm, "unit": "GB/s",
-            "frac": round(achieved / hbm, 4), "traffic": prof.get("traffic"), "peak_source": src,
-            "issue": {k: v for k, v in prof.items() if k != "traffic"},
-            "ms_per_launch": round(ms, 4), "bytes_per_launch": bytes_alg,
-            "alu": {"flops_per_launch": flops_alg, "achieved_tflops": round(flops_alg / (ms * 1e-3) / 1e12, 2),
-                    "fp32_nominal_tflops": round(fp32_peak, 1),
-                    "frac": round(flops_alg / (ms * 1e-3) / 1e12 / fp32_peak, 4)}}
+    return issue_roofline(kernel, ms, sm_mhz, bytes_alg)
 
 
 def cpu_baseline(atoms, budget_s: float = 12.0):
@@ -400,6 +419,13 @@ def cpu_baseline(atoms, budget_s: float = 12.0):
             break
     return {"value": round(atoms.shape[0] * runs / total, 1), "unit": "atoms/s", "cores": cores, "kind": "port",
             "sample": f"FP64 oracle, full surface of the whole 100k-atom assembly, {runs} build(s) in {total:.1f} s"}
+
+
+def bench_config(n: int, world: int) -> dict:
+    """The workload both arms time (identical dicts, so that their lines compare)."""
+    return {"workload": "assembly100k: 20 globules x 5,000 atoms, full SES, probe 1.4 A", "atoms": n,
+            "probe_radius": RP, "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
+            "l2": "flushed between builds (256 MB write outside the timed events)"}
 
 
 def run_ours(args, rank, world, local):
@@ -419,7 +445,6 @@ def run_ours(args, rank, world, local):
     clocks = sampler.stop()
     total_ms = max_over_ranks(float(np.sum(ms)), world)
     counts = g.counts()
-    nbr = g.analysis(1, np.uint32)  # neighbour counts
     g.close()
     # per-stage CUDA events (recorded inside the replayed graph) over as many builds again,
     # right after the timed ones: the timed builds carry no events
@@ -444,25 +469,33 @@ def run_ours(args, rank, world, local):
         gx.close()
         shell = workload("shell1m")
         for mode in ("full", "exterior"):
-            sm, _, gs = time_ours(shell, mode, max(3, args.steps // 4), 2, flush)
+            k1m = max(3, args.steps // 4)
+            sm, _, gs = time_ours(shell, mode, k1m, 2, flush)
             c = gs.counts()
             extra[f"{mode}_1m"] = {"ms_per_step": round(float(np.mean(sm)), 4),
                                    "atoms_per_s": round(shell.shape[0] / (np.mean(sm) * 1e-3), 1),
                                    "probes": c["probes"], "fp64_decisions": c["fp64_decisions"]}
+            if not args.no_error_report:
+                # error of the build's probes and sectors against FP64, and its band counts (after the timing)
+                from sesdf_gb300 import precision
+                extra[f"{mode}_1m"]["error_vs_fp64"] = precision.error_report(gs.fetch(analysis=True), RP, mode)
             gs.close()
+            em = time_e2e(shell, mode, k1m, 2, flush)
+            extra[f"{mode}_1m"]["e2e"] = {"ms_per_step": round(float(np.mean(em)), 4),
+                                          "atoms_per_s": round(shell.shape[0] / (np.mean(em) * 1e-3), 1),
+                                          "h2d_bytes_per_step": shell.shape[0] * 16,
+                                          "d2h_bytes_per_step": COUNTS_BYTES}
         del shell
         extra.update(batch_extras(args, flush, rank, world))
         extra["sdf_20k_1m"] = sdf_extra(flush)
 
-    roof = roofline(stages, counts, nbr, n)
+    roof = roofline(stages, counts, n, clocks.get("sm_mhz"))
     line = {
         "metric": METRIC, "value": round(value, 1), "unit": "atoms/s", "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": round(total_ms / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (f64 triplet solve and band re-evaluation)",
         "data": "synthetic (seeded protein-like globules; no PDB files)",
-        "config": {"workload": "assembly100k: 20 globules x 5,000 atoms, full SES, probe 1.4 A", "atoms": n,
-                   "probe_radius": RP, "parallelism": f"replicas x{world}" if world > 1 else "single GPU",
-                   "l2": "flushed between builds (256 MB write outside the timed events)"},
+        "config": bench_config(n, world),
         "e2e": {"value": round(n * args.steps * world / (e2e_total * 1e-3), 1), "unit": "atoms/s",
                 "h2d_bytes_per_step": n * 16, "d2h_bytes_per_step": COUNTS_BYTES,
                 "ms_per_step": round(e2e_total / args.steps, 4)},
@@ -482,7 +515,19 @@ def run_ours(args, rank, world, local):
         print(json.dumps(line), flush=True)
 
 
+# read-backs inside one reference build (oracle/ref/ref_driver.cu, as sesdf/src/sesdf/sesdf.cu:172-264 does
+# them): five blocking 4-byte counter reads, plus the 8-byte results of one thrust::count_if and two
+# thrust::copy_if calls
+REF_D2H_BYTES_FULL = 5 * 4 + 3 * 8
+# exterior build (sesdf/src/ssesdf/ssesdf.cu:133-187): one 4-byte counter read, the results of four
+# thrust::count_if calls and one thrust::copy_if
+REF_D2H_BYTES_EXTERIOR = 4 + 5 * 8
+
+
 def run_reference(args, rank, world, local):
+    """The reference's own kernels under its restated host orchestration. This process maps only the
+    reference harness (oracle/_ref/libsesref.so, which also carries the synthetic-input generator):
+    nothing of sesdf_gb300's native code is built or loaded here."""
     if rank != 0:
         return
     import torch
@@ -490,7 +535,8 @@ def run_reference(args, rank, world, local):
     if not refharness.available():
         print(json.dumps({"impl": "reference", "unavailable": "reference kernels not built (oracle/_ref missing)"}))
         return
-    refharness.build_driver()
+    from sesdf_gb300 import synth
+    synth.use_library(refharness.build_driver())
     flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
     atoms = workload("assembly100k")
     n = atoms.shape[0]
@@ -524,11 +570,16 @@ def run_reference(args, rank, world, local):
             rs.build()
             sm = [float(rs.time(1)[0]) for _ in range(max(3, args.steps // 4))]
             rs.close()
+            # the reference's build() uploads the atoms itself: its time is end to end
             extra[f"{mode}_1m"] = {"ms_per_step": round(float(np.mean(sm)), 4),
-                                   "atoms_per_s": round(shell.shape[0] / (np.mean(sm) * 1e-3), 1)}
+                                   "atoms_per_s": round(shell.shape[0] / (np.mean(sm) * 1e-3), 1),
+                                   "e2e": {"ms_per_step": round(float(np.mean(sm)), 4),
+                                           "atoms_per_s": round(shell.shape[0] / (np.mean(sm) * 1e-3), 1),
+                                           "h2d_bytes_per_step": shell.shape[0] * 16,
+                                           "d2h_bytes_per_step": REF_D2H_BYTES_FULL if mode == "full"
+                                           else REF_D2H_BYTES_EXTERIOR}}
         del shell
         # the reference's per-molecule loop over the same 256-molecule batch (context for the batched build)
-        from sesdf_gb300 import synth
         mols = [synth.globule(int(nm), 1300 + k) for k, nm in enumerate(synth.batch_sizes())]
         refs = [refharness.RefBuild(m, RP, "full") for m in mols]
         for rr in refs:
@@ -547,9 +598,11 @@ def run_reference(args, rank, world, local):
         "warmup": args.warmup, "ms_per_step": round(total / args.steps, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32 (--use_fast_math)", "impl": "reference",
         "data": "synthetic (seeded protein-like globules; no PDB files)",
-        "config": {"workload": "assembly100k: 20 globules x 5,000 atoms, full SES, probe 1.4 A", "atoms": n,
-                   "probe_radius": RP, "l2": "flushed between builds (256 MB write outside the timed events)"},
-        "e2e": {"value": round(value, 1), "unit": "atoms/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "config": bench_config(n, world),
+        # the timed build() uploads the atoms from host memory (pageable cudaMemcpy, sesdf/src/sesdf/sesdf.cu:212-213)
+        # and reads its counters back: the device-timed value is already end to end
+        "e2e": {"value": round(value, 1), "unit": "atoms/s", "h2d_bytes_per_step": n * 16,
+                "d2h_bytes_per_step": REF_D2H_BYTES_FULL, "ms_per_step": round(total / args.steps, 4)},
         "cpu_baseline": {"value": round(value, 1), "unit": "atoms/s", "cores": 1, "kind": "reference",
                          "sample": "the reference's own implementation of this path is CUDA: its kernels (built from "
                                    "its sources) run on the GPU under its restated host orchestration, one host thread"},
@@ -565,14 +618,19 @@ def main():
     ap.add_argument("--warmup", type=int, default=5)
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-extras", action="store_true")
+    ap.add_argument("--no-error-report", action="store_true", help="skip the FP64 error report of the 1M builds")
     ap.add_argument("--kernels-only", action="store_true",
                     help="only the device-timed builds (for profiler runs): no e2e, extras, stage profile or CPU baseline")
     args = ap.parse_args()
     args.warmup = max(args.warmup, 3)
     rank, world, local = dist_init()
-    import __graft_entry__
-    if rank == 0 or world == 1:
+    if args.impl == "ours" and (rank == 0 or world == 1):
+        import __graft_entry__
         __graft_entry__.build()
+    elif args.impl == "reference" and rank == 0:
+        # the reference harness only (its cubin from the checkout where present, else the prebuilt one)
+        from oracle import refharness
+        refharness.build_cubin()
     barrier(world)
     if args.impl == "reference":
         run_reference(args, rank, world, local)

@@ -193,15 +193,20 @@ const char * sesgb_stage_name( uint32_t stage );
  * {min x, y, z, max x, y, z}) and `probe_radius` -- writing the sorted atoms and
  * the sorted-to-input permutation to the caller's device buffers, without
  * allocating any memory. It is for callers that cannot call cudaMalloc when
- * they need the sort (a stream capture in progress, a host that owns a fixed
- * device-memory budget, a loop that must not enter the allocator). Its scratch
- * is a fixed array in this library's device image (about 3.3 MB on every GPU
- * that loads the library, kept until the process exits), so n is limited to
- * SESGB_NOALLOC_MAX_ATOMS (larger n: SESGB_ERR_TOO_LARGE, nothing launched).
- * The first call on a device looks up the array's device address with that
- * device current; make that first call before any stream capture. All calls on
- * a device share the array: calls whose GPU work overlaps (other streams, other
- * host threads) race on it and must be serialised by the caller. */
+ * they need the sort: a plugin whose host application owns a fixed
+ * device-memory budget and passes it every buffer, or a real-time loop that
+ * must not enter the allocator (cudaMalloc may synchronise the device). Its
+ * scratch is a fixed array in this library's device image (about 3.3 MB on
+ * every GPU that loads the library, kept until the process exits), so n is
+ * limited to SESGB_NOALLOC_MAX_ATOMS (larger n: SESGB_ERR_TOO_LARGE, nothing
+ * launched). The first call on a device looks up the array's device address
+ * with that device current; make that first call before any stream capture.
+ * The address is kept for the life of the process: a device reset while the
+ * library is loaded is not supported. All calls on a device share the array:
+ * calls whose GPU work overlaps (other streams, other host threads) race on it
+ * and must be serialised by the caller. A launch error left pending on the
+ * calling thread by earlier work is returned as SESGB_ERR_CUDA before anything
+ * is launched. */
 #define SESGB_NOALLOC_MAX_ATOMS 262144u
 int sesgb_sort_atoms_noalloc( const void * device_atoms, uint32_t n, const float * aabb, float probe_radius,
                               void * device_sorted_atoms, uint32_t * device_sorted_to_input, void * stream );

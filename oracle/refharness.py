@@ -14,18 +14,28 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 OUT = os.path.join(HERE, "_ref")
 CUBIN = os.path.join(OUT, "ref_kernels.cubin")
 LIB = os.path.join(OUT, "libsesref.so")
-REFERENCE = "/root/reference"
+
+
+def reference_checkout() -> str | None:
+    """The reference checkout the cubin is compiled from: $SESDF_REFERENCE, else a
+    checkout named `reference` beside this repository; None when neither exists
+    (the prebuilt cubin is used then)."""
+    for c in (os.environ.get("SESDF_REFERENCE"), os.path.join(os.path.dirname(HERE), "..", "reference")):
+        if c and os.path.isdir(os.path.join(c, "sesdf")):
+            return os.path.abspath(c)
+    return None
 
 _lib = None
 
 
 def build_cubin(force: bool = False) -> bool:
     """Compiles the reference kernels when the reference checkout is present."""
-    if not os.path.isdir(REFERENCE):
+    ref = reference_checkout()
+    if ref is None:
         return os.path.exists(CUBIN)
     if force and os.path.exists(CUBIN):
         os.remove(CUBIN)
-    subprocess.run(["make", "-s", "-C", HERE, "ref-cubin", f"REF={REFERENCE}"], check=True)
+    subprocess.run(["make", "-s", "-C", HERE, "ref-cubin", f"REF={ref}"], check=True)
     return True
 
 

@@ -1,26 +1,27 @@
 // sesgb_noalloc.cu -- reference-grid atom sort that allocates no memory.
 //
 // Some callers cannot allocate device memory at the time they need the sort:
-// code that runs while its host application forbids new allocations (for
-// example between the start and end of a CUDA stream capture, inside a plugin
-// whose host owns a fixed device-memory budget, or in a real-time loop that
-// must not enter the allocator). For them, sesgb_sort_atoms_noalloc sorts
-// atoms into the order of the build's `atoms` output (the reference grid's
-// stable cell order, the order getAtomIndices() describes) using only the
-// buffers the caller passes plus one fixed scratch array that lives in this
-// library's device image.
+// a plugin whose host application owns a fixed device-memory budget and hands
+// it every buffer, or a real-time loop that must never enter the allocator
+// (cudaMalloc can synchronise the device and take milliseconds). For them,
+// sesgb_sort_atoms_noalloc sorts atoms into the order of the build's `atoms`
+// output (the reference grid's stable cell order, the order getAtomIndices()
+// describes) using only the buffers the caller passes plus one fixed scratch
+// array that lives in this library's device image.
 //
 // The scratch array below is a file-scope __device__ array: every GPU that
 // loads the library keeps its SESGB_NOALLOC_MAX_ATOMS-sized copy (about 3.3 MB)
 // until the process exits. Host code must not use the array's symbol as a
 // device address; the device address is fetched once per device with
 // cudaGetSymbolAddress (the first call of the entry point on a device does it,
-// with that device current) and passed to the kernels. Every call on a device
-// shares the one array and leaves its contents behind: two calls whose work
-// overlaps on the GPU (different streams, or different host threads on one
-// device) race on it and must be serialised by the caller. No part of the
-// scratch has to start at zero (every pass writes the whole histogram and key
-// arrays it reads afterwards).
+// with that device current) and passed to the kernels. The stored address
+// belongs to the device's context of that moment: resetting the device
+// (cudaDeviceReset) while the library is loaded is not supported. Every call
+// on a device shares the one array and leaves its contents behind: two calls
+// whose work overlaps on the GPU (different streams, or different host threads
+// on one device) race on it and must be serialised by the caller. No part of
+// the scratch has to start at zero (every pass writes the whole histogram and
+// key arrays it reads afterwards).
 #include <cstring>
 #include <mutex>
 
@@ -103,6 +104,10 @@ extern "C" int sesgb_sort_atoms_noalloc( const void * device_atoms, uint32_t n, 
         return SESGB_ERR_CUDA;
     if ( n == 0 )
         return SESGB_OK;
+    // a launch error left pending on this thread by earlier work is returned here, before anything
+    // is launched, so that the check after the launches below judges only this call's own
+    if ( cudaGetLastError() != cudaSuccess )
+        return SESGB_ERR_CUDA;
 
     // reference grid of Sesdf::Sesdf (sesdf/src/sesdf/sesdf.cu:23-33)
     GridRef        grid;

@@ -20,12 +20,21 @@ import numpy as np
 from . import _build
 
 _lib = None
+_path = None
+
+
+def use_library(path: str) -> None:
+    """Takes the generator from another library that exports the same sesgb_synth_*
+    functions (the reference harness links synth.c in, so that a process timing the
+    reference loads nothing of this package's native code)."""
+    global _lib, _path
+    _lib, _path = None, path
 
 
 def _load():
     global _lib
     if _lib is None:
-        path = _build.build_synth()
+        path = _path or _build.build_synth()
         lib = ctypes.CDLL(path)
         lib.sesgb_synth_globule.argtypes = [ctypes.c_uint32, ctypes.c_uint64, ctypes.c_void_p]
         lib.sesgb_synth_globule.restype = ctypes.c_int

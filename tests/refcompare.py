@@ -274,3 +274,208 @@ def compare(atoms_in: np.ndarray, rp: float, mode: str, ref: dict, o: dict) -> d
                 if np.all(np.isfinite(tm_o[k])) and np.all(np.isfinite(tm_r[k]))]
         rep["tori_max_err"] = float(max(errs, default=0.0))
     return rep
+
+
+# ---------------------------------------------------------------------------------------------------------
+# GPU build against the reference's kernels, in sorted-id space (vectorised, for 10^5 - 10^6 atoms)
+
+
+def _probe_keys_sorted(atoms, ids, pos, n):
+    """int64 key per probe: sorted triplet of sorted ids and the side of the centres' plane."""
+    trip = np.sort(np.asarray(ids)[:, :3].astype(np.int64), axis=1)
+    a = np.asarray(atoms, np.float64)
+    ca, cb, cc = (a[trip[:, m], :3] for m in range(3))
+    d = np.einsum("ij,ij->i", np.cross(cb - ca, cc - ca), np.asarray(pos, np.float64)[:, :3] - ca)
+    side = np.sign(d).astype(np.int64) + 1
+    return ((trip[:, 0] * n + trip[:, 1]) * n + trip[:, 2]) * 4 + side
+
+
+def _decode_probe_key(key, n):
+    side = int(key % 4) - 1
+    t = key // 4
+    c = int(t % n)
+    t //= n
+    return (int(t // n), int(t % n), c), side
+
+
+def _slot_keys(nbr_ids, nbr_count, n):
+    cap = nbr_ids.shape[1]
+    live = np.arange(cap)[None, :] < np.asarray(nbr_count)[:, None]
+    i, s = np.nonzero(live)
+    j = nbr_ids[i, s].astype(np.int64)
+    return i.astype(np.int64) * n + j, i, s
+
+
+def compare_sorted(ref: dict, gpu: dict, rp: float, mode: str) -> dict:
+    """GPU build (SesBuild.fetch) against the reference's kernels (RefBuild.fetch) on the same atoms.
+
+    Both sort the atoms with the same fast-math reference-grid division, so every id is compared in
+    sorted-id space. Each difference is checked against the float32 band of the predicate that decides
+    it (module docstring; margins in double precision from the float32 atoms) and counted as explained
+    when inside it, with the cases that follow from it (statuses of circles whose neighbour pair
+    differs, probes on such circles, segments of such probes)."""
+    rpd = _f(rp)
+    rep = {"perm_mismatch": int(np.count_nonzero(ref["perm"] != gpu["perm"])),
+           "atoms_mismatch": int(np.count_nonzero(np.any(ref["atoms"] != gpu["atoms"], axis=1)))}
+    if rep["perm_mismatch"] or rep["atoms_mismatch"]:
+        return rep
+    atoms = gpu["atoms"]
+    n = atoms.shape[0]
+    pos = atoms[:, :3].astype(np.float64)
+    rad = atoms[:, 3].astype(np.float64)
+    ext = mode == "exterior"
+
+    # neighbour pairs
+    kr, ir, sr_ = _slot_keys(ref["nbr_ids"], ref["nbr_count"], n)
+    kg, ig, sg_ = _slot_keys(gpu["nbr_ids"], gpu["nbr_count"], n)
+    diff = np.setxor1d(kr, kg)
+    a, b = diff // n, diff % n
+    d2 = np.einsum("ij,ij->i", pos[a] - pos[b], pos[a] - pos[b])
+    R = (rad[a] + rpd) + (rad[b] + rpd)
+    m = np.abs(d2 - R * R - _f(1e-4))
+    bad_pairs = set(zip(np.minimum(a, b).tolist(), np.maximum(a, b).tolist()))
+    rep["pairs"] = int(len(kg))
+    rep["nbr_mismatch"] = len(bad_pairs)
+    rep["nbr_unexplained"] = int(np.count_nonzero(m >= 64 * EPS32 * (d2 + R * R)))
+
+    def nbrs_of(i):
+        return [int(x) for x in gpu["nbr_ids"][i, :gpu["nbr_count"][i]]]
+
+    # statuses of the directed circles both sides hold
+    common, xr, xg = np.intersect1d(kr, kg, return_indices=True)
+    str_ = ref["status"][ir[xr], sr_[xr]]
+    stg = gpu["status"][ig[xg], sg_[xg]]
+    ci_, cj_ = common // n, common % n
+    keep = ci_ < cj_ if ext else np.ones(len(common), bool)
+    bad = np.nonzero(keep & (str_ != stg))[0]
+    # exterior statuses are read after the probes promoted their circles to status 2, so there a
+    # circle is a cause for its probes only when its own visibility margin is inside the band
+    tainted = set()
+    out_of_band = []
+    for q in bad.tolist():
+        i, j = int(ci_[q]), int(cj_[q])
+        c = (min(i, j), max(i, j))
+        inband = status_margin(pos, rad, i, j, nbrs_of(i), rpd) < WIDE
+        if inband or not ext:
+            tainted.add(c)
+        if not inband:
+            out_of_band.append(c)
+    rep["status_mismatch"] = int(len(bad))
+    rep["status_unexplained"] = len(out_of_band)
+
+    # probes
+    pkr = _probe_keys_sorted(atoms, ref["probe_ids"], ref["probe_pos"], n)
+    pkg = _probe_keys_sorted(atoms, gpu["probe_ids"], gpu["probe_pos"], n)
+    pdiff = np.setxor1d(pkr, pkg)
+    bad_probe_circles = set()
+    pr_unexp = 0
+    for key in pdiff.tolist():
+        trip, side = _decode_probe_key(key, n)
+        circles = [(trip[0], trip[1]), (trip[0], trip[2]), (trip[1], trip[2])]
+        bad_probe_circles |= set(circles)
+        if any(c in tainted or c in bad_pairs for c in circles):
+            continue
+        explained = False
+        for owner in trip:
+            others = [t for t in trip if t != owner]
+            sol, tnorm = probe_solutions(pos, rad, owner, others[0], others[1], rpd)
+            if sol is None or abs(tnorm) < WIDE:
+                explained = True
+                break
+            for x in sol:
+                if canon.side(atoms, trip, x) != side:
+                    continue
+                if occlusion_margin(pos, rad, x, owner, set(trip), nbrs_of(owner), rpd) < WIDE:
+                    explained = True
+        if not explained:
+            pr_unexp += 1
+    rep["probes"] = int(len(pkg))
+    rep["probe_mismatch"] = int(len(pdiff))
+    rep["probe_unexplained"] = pr_unexp
+    if ext:
+        # a probe found on one side only changes the statuses of its three circles
+        rep["status_unexplained"] = len([c for c in out_of_band if c not in bad_probe_circles and c not in bad_pairs])
+    _, qr, qg = np.intersect1d(pkr, pkg, return_indices=True)
+    if len(qr):
+        err = np.abs(ref["probe_pos"][qr, :3].astype(np.float64) - gpu["probe_pos"][qg, :3].astype(np.float64))
+        rep["probe_pos_max_diff"] = float(err.max())
+        rep["probe_pos_over_1e-4"] = int(np.count_nonzero(err.max(axis=1) > 1e-4))
+        if ext:
+            rs, gs = qr < ref["counts"]["Q"], qg < gpu["counts"]["singular_probes"]
+        else:
+            rs, gs = np.abs(ref["probe_pos"][qr, 3]) == 2, np.abs(gpu["probe_pos"][qg, 3]) == 2
+        rep["singular_mismatch"] = int(np.count_nonzero(rs != gs))
+    else:
+        rep["probe_pos_max_diff"], rep["probe_pos_over_1e-4"], rep["singular_mismatch"] = 0.0, 0, 0
+
+    def circle_tainted(i, j):
+        c = (min(i, j), max(i, j))
+        return c in tainted or c in bad_pairs or c in bad_probe_circles
+
+    if not ext:
+        # sectors of the visible circles both sides hold, by slot
+        def sector_index(side):
+            cap = side["nbr_ids"].shape[1]
+            live = np.arange(cap)[None, :] < side["nbr_count"][:, None]
+            vis = live & (side["status"] != 0)
+            idx = np.full(vis.shape, -1, np.int64)
+            idx[vis] = np.arange(int(vis.sum()))
+            return idx
+        sxr, sxg = sector_index(ref), sector_index(gpu)
+        a_r, a_g = sxr[ir[xr], sr_[xr]], sxg[ig[xg], sg_[xg]]
+        both = (a_r >= 0) & (a_g >= 0)
+        sr_v = ref["sectors"][a_r[both]].astype(np.float64)
+        sg_v = gpu["sectors"][a_g[both]].astype(np.float64)
+        rep["sector_axis_max_diff"] = float(np.abs(sr_v[:, :3] - sg_v[:, :3]).max()) if both.any() else 0.0
+        rep["sector_cos_max_diff"] = float(np.abs(np.cos(sr_v[:, 3]) - np.cos(sg_v[:, 3])).max()) if both.any() else 0.0
+        # complete circles
+        fr = np.sort(ref["full"].astype(np.int64), axis=1)
+        fg = np.sort(gpu["full"].astype(np.int64), axis=1)
+        fdiff = np.setxor1d(fr[:, 0] * n + fr[:, 1], fg[:, 0] * n + fg[:, 1])
+        rep["full_mismatch"] = int(len(fdiff))
+        rep["full_unexplained"] = int(sum(1 for k in fdiff.tolist() if not circle_tainted(k // n, k % n)))
+
+        # segments: circle and the unordered pair of probe keys
+        def seg_rows(side, pk):
+            s = side["segments"].astype(np.int64)
+            if len(s) == 0:
+                return np.zeros((0, 4), np.int64)
+            c = np.sort(s[:, :2], axis=1)
+            p = np.sort(np.stack([pk[s[:, 2]], pk[s[:, 3]]], 1), axis=1)
+            return np.ascontiguousarray(np.concatenate([c, p], 1))
+        rows_r, rows_g = seg_rows(ref, pkr), seg_rows(gpu, pkg)
+        vt = np.dtype((np.void, 32))
+        sdiff = np.setxor1d(rows_r.view(vt).ravel(), rows_g.view(vt).ravel())
+        bad_probe_keys = set(pdiff.tolist())
+        unexp = 0
+        for v in sdiff:
+            r = np.frombuffer(v.tobytes(), np.int64)
+            if circle_tainted(int(r[0]), int(r[1])) or int(r[2]) in bad_probe_keys or int(r[3]) in bad_probe_keys:
+                continue
+            unexp += 1
+        rep["segments"] = int(len(rows_g))
+        rep["segment_mismatch"] = int(len(sdiff))
+        rep["segment_unexplained"] = unexp
+    else:
+        # tori of the circles with status 2 (i < j) both sides hold, by slot
+        def tori_index(side):
+            cap = side["nbr_ids"].shape[1]
+            live = np.arange(cap)[None, :] < side["nbr_count"][:, None]
+            t = live & (side["status"] == 2)
+            idx = np.full(t.shape, -1, np.int64)
+            idx[t] = np.arange(int(t.sum()))
+            return idx
+        txr, txg = tori_index(ref), tori_index(gpu)
+        a_r, a_g = txr[ir[xr], sr_[xr]], txg[ig[xg], sg_[xg]]
+        both = (a_r >= 0) & (a_g >= 0) & keep
+        tr = np.concatenate([ref["tori_pos"], ref["tori_axis"], ref["tori_vs"]], 1)[a_r[both]].astype(np.float64)
+        tg = np.concatenate([gpu["tori_pos"], gpu["tori_axis"], gpu["tori_vs"]], 1)[a_g[both]].astype(np.float64)
+        fin = np.isfinite(tr).all(axis=1) & np.isfinite(tg).all(axis=1)
+        rep["tori_max_diff"] = float(np.abs(tr[fin] - tg[fin]).max()) if fin.any() else 0.0
+        only = keep & ((a_r >= 0) != (a_g >= 0))
+        rep["tori_mismatch"] = int(np.count_nonzero(only))
+        rep["tori_unexplained"] = int(sum(1 for q in np.nonzero(only)[0].tolist()
+                                          if not circle_tainted(int(ci_[q]), int(cj_[q]))))
+    rep["unexplained"] = int(sum(v for k, v in rep.items() if k.endswith("_unexplained")))
+    rep["band_cases"] = int(sum(v for k, v in rep.items() if k.endswith("_mismatch")))
+    return rep

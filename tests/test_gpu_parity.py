@@ -31,7 +31,7 @@ def compare(atoms, out, o, mode):
     n = atoms.shape[0]
     c = out["counts"]
     assert c["atoms"] == n
-    assert c["truncated_atoms"] == 0
+    assert c["truncated_atoms"] == o["counters"]["nbr_truncated"]
     assert c["outside_atoms"] == 0
     # stable reference-grid order: same permutation
     assert np.array_equal(out["perm"], o["perm"]), "sorted order differs"
@@ -129,6 +129,20 @@ def test_probe_radius_24():
         out = g.fetch()
     o = oracle.run(atoms, 2.4, "full", max_nbr=288)
     compare(atoms, out, o, "full")
+
+
+@pytest.mark.parametrize("mode", ["full", "exterior"])
+def test_neighbor_truncation(mode):
+    # 32 neighbour slots per atom where most atoms of the globule have 35-42: rows keep their first 32
+    # neighbours in visit order (sorted id), as the reference's neighbour search does when its slots are
+    # full (sesdf/src/sesdf/operations.cu:111-116), and the truncated atoms are counted
+    atoms = synth.globule(2000, 1000)
+    with SesBuild(atoms, RP, mode, max_neighbor_per_atom=32) as g:
+        g.build()
+        out = g.fetch()
+    o = oracle.run(atoms, RP, mode, max_nbr=32)
+    assert o["counters"]["nbr_truncated"] > 500
+    compare(atoms, out, o, mode)
 
 
 @pytest.mark.slow

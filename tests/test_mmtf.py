@@ -13,7 +13,7 @@ import struct
 import numpy as np
 import pytest
 
-from oracle.refharness import REFERENCE
+from oracle.refharness import reference_checkout
 from sesdf_gb300 import mmtf
 
 HERE = os.path.dirname(os.path.abspath(__file__))
@@ -177,7 +177,11 @@ def test_structure_fixture():
     assert sizes == {"1AGA": (126, 4), "101M": (1413, 4), "1VIS": (2531, 4), "7SC0": (11638, 4)}
 
 
-@pytest.mark.skipif(not os.path.isdir(os.path.join(REFERENCE, "samples")), reason="reference checkout absent")
+REFERENCE = reference_checkout()
+
+
+@pytest.mark.skipif(REFERENCE is None or not os.path.isdir(os.path.join(REFERENCE, "samples")),
+                    reason="reference checkout absent")
 def test_against_reference_checkout():
     # the radius table, as the reference states it
     src = open(os.path.join(REFERENCE, "sesdf/src/core/molecule.cpp")).read()
