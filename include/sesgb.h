@@ -28,7 +28,7 @@ extern "C" {
 #define SESGB_ERR_NOT_BUILT -4 /* results requested before a build */
 #define SESGB_ERR_TIMEOUT -5   /* a bounded device wait gave up */
 #define SESGB_ERR_MODE -6      /* request does not match the context's mode */
-#define SESGB_ERR_TOO_LARGE -7 /* input larger than the no-allocation entry point's fixed scratch holds */
+#define SESGB_ERR_TOO_LARGE -7 /* input beyond a fixed limit: the no-allocation sort's scratch, the cavity grid's size */
 
 #define SESGB_MODE_FULL 0     /* bcs::Sesdf */
 #define SESGB_MODE_EXTERIOR 1 /* bcs::Ssesdf */
@@ -48,6 +48,12 @@ typedef struct sesgb_options
 #define SESGB_FLAG_GRAPH 1u
 /* Record CUDA events between the stages of each build (see sesgb_stage_times). */
 #define SESGB_FLAG_PROFILE 2u
+/* Start the count-dependent output capacities at their minimum instead of at
+ * protein-like multiples of the atom count: the first build then overflows, and
+ * sesgb_build regrows every buffer to the counts it met (plus a quarter) and
+ * builds again (sesgb_counts.rebuilds). For callers that want buffers sized to
+ * their molecule rather than to the default estimate. */
+#define SESGB_FLAG_MIN_CAPACITY 4u
 
 /* Output buffers of the full-surface build: field for field the reference's
  * bcs::sesdf::SesdfData (sesdf/include/bcs/sesdf/graphics.hpp:39-66). Device pointers,
@@ -255,6 +261,66 @@ int sesgb_sdf( sesgb_ctx * ctx, const float * device_queries, uint32_t m, float 
  * sphere constraints, a circle point by the Lagrange rule on its two. */
 int sesgb_sdf_backward( sesgb_ctx * ctx, const float * device_queries, uint32_t m, const float * device_grad_sdf,
                         float * device_grad_atoms, void * stream );
+
+/* Headless image of the SES of the last full-surface build of one molecule (no
+ * counterpart in the reference, which draws its primitives through OpenGL): every
+ * pixel's ray from a pinhole camera is sphere-traced against sesgb_sdf's signed
+ * distance on the device, in one launch. Ray of pixel (ix, iy), row-major from the
+ * top left: d = normalise(forward + xs right + ys up), xs = (2 (ix + 0.5) / width - 1)
+ * tan_half_fov width / height, ys = (1 - 2 (iy + 0.5) / height) tan_half_fov; points
+ * eye + t d from t_near. Steps never cross the surface (inside the SAS the value
+ * bounds the distance to the SES, outside value - rp bounds the distance to the SAS)
+ * and are at least eps / 4; a ray stops at the first point inside the SAS whose value
+ * is below eps (or deeper than the band), at t_far, or after max_steps evaluations.
+ * device_depth: float[width * height], t of the hit or +inf; device_normals (may be
+ * NULL): float3 per pixel, the normalised central difference of the signed distance
+ * (step normal_step) at the hit, 0 for a miss. Ray arithmetic is in double precision. */
+typedef struct sesgb_camera
+{
+    double   eye[ 3 ];
+    double   forward[ 3 ]; /* unit vectors: view direction, image right, image up */
+    double   right[ 3 ];
+    double   up[ 3 ];
+    double   tan_half_fov; /* tangent of half the vertical field of view */
+    double   t_near, t_far;
+    double   eps;          /* hit threshold, A */
+    double   normal_step;  /* central-difference step of the normals, A */
+    uint32_t width, height, max_steps;
+} sesgb_camera;
+int sesgb_render( sesgb_ctx * ctx, const sesgb_camera * camera, float * device_depth, float * device_normals,
+                  void * stream );
+
+/* Exterior and cavities (no counterpart in the reference, whose exterior-only build
+ * keeps every probe, cavities included). E = probe-centre positions outside every
+ * SAS sphere (radius r_i + rp) of the last build of one molecule; its component
+ * that touches the border of a box around the SAS is the exterior, every other one
+ * a cavity. E is sampled at voxel centres of spacing `voxel` (A, >= 0.05): origin =
+ * min(c - R) - 2 voxel, dims = ceil((max(c + R) + 2 voxel - origin) / voxel) + 1 per
+ * axis, at most 2^28 voxels (SESGB_ERR_TOO_LARGE otherwise), voxel (ix, iy, iz) at
+ * index (ix * ny + iy) * nz + iz, accessible when ((dx^2 + dy^2) + dz^2) < R^2 holds
+ * for no atom (double precision). Components are 6-connected and numbered 1..n in
+ * the order of their first voxel. device_probe_component (may be NULL): int32 per
+ * probe of the build, the component of the nearest accessible voxel centre among
+ * the 5^3 around the probe's nearest voxel, 0 when none is accessible (E is thinner
+ * than a voxel there). Synchronises `stream`; the grid stays with the context until
+ * the next call. */
+typedef struct sesgb_cavity_info
+{
+    double   origin[ 3 ]; /* centre of voxel (0, 0, 0) */
+    double   voxel;
+    uint32_t dims[ 3 ];
+    uint32_t components; /* labels 1..components */
+    uint32_t exterior;   /* components touching the grid's border */
+    uint32_t cavities;   /* the others */
+    uint32_t probes;     /* probes classified */
+} sesgb_cavity_info;
+int sesgb_cavities( sesgb_ctx * ctx, double voxel, sesgb_cavity_info * info, int32_t * device_probe_component,
+                    void * stream );
+/* The label grid of the last sesgb_cavities (device int32 per voxel, 0 = not accessible). */
+int sesgb_cavity_labels( sesgb_ctx * ctx, const int32_t ** device_labels, uint64_t * voxels );
+/* Per component k (0..components, 0 unused): voxel count and border flag (1 = exterior);
+ * capacity >= components + 1. */
+int sesgb_cavity_components( sesgb_ctx * ctx, uint32_t * host_voxels, uint8_t * host_border, uint32_t capacity );
 
 /* Solvent-excluded surface area of the primitives of the last full-surface build
  * of one molecule (no counterpart in the reference): the convex patches (the

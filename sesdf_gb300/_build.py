@@ -21,7 +21,8 @@ INCLUDE = os.path.join(ROOT, "include")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-std=c++17", "-O3", "-lineinfo", "-Xcompiler", "-fPIC", "-I", INCLUDE, "-I", CSRC]
-CUDA_UNITS = ["sesgb_sort.cu", "sesgb_stages.cu", "sesgb_area.cu", "sesgb_api.cu", "sesgb_noalloc.cu"]
+CUDA_UNITS = ["sesgb_sort.cu", "sesgb_stages.cu", "sesgb_area.cu", "sesgb_api.cu", "sesgb_noalloc.cu",
+              "sesgb_cavities.cu"]
 CXX_UNITS = ["bcs_sesdf.cpp", "bcs_loader.cpp"]
 
 LIB = os.path.join(LIBDIR, "libsesgb.so")

@@ -20,6 +20,7 @@ MODE_FULL = 0
 MODE_EXTERIOR = 1
 FLAG_GRAPH = 1
 FLAG_PROFILE = 2
+FLAG_MIN_CAPACITY = 4
 
 BUF_ATOM_INDICES, BUF_NEIGHBOR_COUNT, BUF_NEIGHBOR_IDS, BUF_VISIBILITY_STATUS, BUF_GLOBAL_TO_TRIMMED = range(5)
 
@@ -32,7 +33,7 @@ EXPORTS = [
     "sesgb_launch_count", "sesgb_build_async", "sesgb_finish", "sesgb_sort_atoms_noalloc",
     "sesgb_create_batch", "sesgb_batch_molecules", "sesgb_molecule_record", "sesgb_get_full_molecule",
     "sesgb_get_exterior_molecule", "sesgb_sdf", "sesgb_sdf_backward", "sesgb_ses_area", "sesgb_ses_area_backward",
-    "sesgb_load_mmtf",
+    "sesgb_load_mmtf", "sesgb_render", "sesgb_cavities", "sesgb_cavity_labels", "sesgb_cavity_components",
 ]
 SDF_BAND = 3.0
 MOL_FIELDS = ["atoms", "sectors", "full_circles", "partial_circles", "probes", "singular_probes", "segments", "tori",
@@ -48,6 +49,19 @@ class SesgbError(RuntimeError):
 class Options(ctypes.Structure):
     _fields_ = [("max_neighbor_per_atom", ctypes.c_uint32), ("max_intersections_per_circle", ctypes.c_uint32),
                 ("device", ctypes.c_int32), ("flags", ctypes.c_uint32)]
+
+
+class Camera(ctypes.Structure):
+    _fields_ = [("eye", ctypes.c_double * 3), ("forward", ctypes.c_double * 3), ("right", ctypes.c_double * 3),
+                ("up", ctypes.c_double * 3), ("tan_half_fov", ctypes.c_double), ("t_near", ctypes.c_double),
+                ("t_far", ctypes.c_double), ("eps", ctypes.c_double), ("normal_step", ctypes.c_double),
+                ("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("max_steps", ctypes.c_uint32)]
+
+
+class CavityInfo(ctypes.Structure):
+    _fields_ = [("origin", ctypes.c_double * 3), ("voxel", ctypes.c_double), ("dims", ctypes.c_uint32 * 3),
+                ("components", ctypes.c_uint32), ("exterior", ctypes.c_uint32), ("cavities", ctypes.c_uint32),
+                ("probes", ctypes.c_uint32)]
 
 
 class FullData(ctypes.Structure):
@@ -133,6 +147,10 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         lib.sesgb_sdf_backward.argtypes = [P, P, U32, P, P, P]
         lib.sesgb_ses_area.argtypes = [P, P, P, P]
         lib.sesgb_ses_area_backward.argtypes = [P, P, P, P]
+        lib.sesgb_render.argtypes = [P, ctypes.POINTER(Camera), P, P, P]
+        lib.sesgb_cavities.argtypes = [P, ctypes.c_double, ctypes.POINTER(CavityInfo), P, P]
+        lib.sesgb_cavity_labels.argtypes = [P, ctypes.POINTER(P), ctypes.POINTER(ctypes.c_uint64)]
+        lib.sesgb_cavity_components.argtypes = [P, P, P, U32]
         _lib = lib
     return _lib
 
@@ -182,14 +200,14 @@ class SesBuild:
 
     def __init__(self, atoms: np.ndarray, probe_radius: float = 1.4, mode: str = "full", box=None,
                  max_neighbor_per_atom: int = 0, max_intersections_per_circle: int = 0, graph: bool = True,
-                 device: int = -1, profile: bool = False):
+                 device: int = -1, profile: bool = False, min_capacity: bool = False):
         self._lib = load_library()
         self.atoms = np.ascontiguousarray(np.asarray(atoms, np.float32).reshape(-1, 4))
         self.mode = mode
         self.probe_radius = float(probe_radius)
         bx = None if box is None else np.ascontiguousarray(box, np.float32)
         self.box = aabb(self.atoms) if bx is None else bx
-        flags = (FLAG_GRAPH if graph else 0) | (FLAG_PROFILE if profile else 0)
+        flags = (FLAG_GRAPH if graph else 0) | (FLAG_PROFILE if profile else 0) | (FLAG_MIN_CAPACITY if min_capacity else 0)
         opt = Options(max_neighbor_per_atom, max_intersections_per_circle, device, flags)
         h = ctypes.c_void_p()
         st = self._lib.sesgb_create(self.atoms.ctypes.data if self.atoms.size else None, self.atoms.shape[0],
@@ -287,6 +305,42 @@ class SesBuild:
         g = np.ascontiguousarray(np.broadcast_to(np.asarray(grad_parts, np.float32), (3,)))
         self._check(self._lib.sesgb_ses_area_backward(self._h, g.ctypes.data, grad_atoms_ptr, stream), "ses_area_backward")
 
+    def render(self, camera: dict, depth_ptr: int, normals_ptr: int | None = None, stream: int | None = None):
+        """Sphere-traced depth (device float[w*h]) and normals (device float3[w*h], optional) of the last
+        full-surface build (sesgb_render); camera: the fields of sesgb_camera."""
+        c = Camera()
+        for k in ("eye", "forward", "right", "up"):
+            getattr(c, k)[:] = [float(x) for x in camera[k]]
+        for k in ("tan_half_fov", "t_near", "t_far", "eps", "normal_step", "width", "height", "max_steps"):
+            setattr(c, k, camera[k])
+        self._check(self._lib.sesgb_render(self._h, ctypes.byref(c), depth_ptr, normals_ptr, stream), "render")
+
+    def cavities(self, voxel: float, probe_component_ptr: int | None = None, stream: int | None = None) -> dict:
+        """Components of the probe-accessible space on the device (sesgb_cavities): the grid, the
+        component count, exterior and cavity counts; probe_component_ptr (device int32[probes]) receives
+        each probe's component. Synchronises."""
+        info = CavityInfo()
+        self._check(self._lib.sesgb_cavities(self._h, float(voxel), ctypes.byref(info), probe_component_ptr, stream),
+                    "cavities")
+        return {"origin": np.array(info.origin[:], np.float64), "voxel": info.voxel, "dims": tuple(info.dims[:]),
+                "components": info.components, "exterior": info.exterior, "cavities": info.cavities,
+                "probes": info.probes}
+
+    def cavity_labels(self) -> np.ndarray:
+        """Host copy (int32, flat) of the label grid of the last cavities() call."""
+        p = ctypes.c_void_p()
+        v = ctypes.c_uint64()
+        self._check(self._lib.sesgb_cavity_labels(self._h, ctypes.byref(p), ctypes.byref(v)), "cavity_labels")
+        return self._copy(p, v.value, np.int32)
+
+    def cavity_components(self, components: int):
+        """(voxel count uint32 [components + 1], border flag uint8 [components + 1]) of the last cavities()."""
+        vox = np.zeros(components + 1, np.uint32)
+        bor = np.zeros(components + 1, np.uint8)
+        self._check(self._lib.sesgb_cavity_components(self._h, vox.ctypes.data, bor.ctypes.data, components + 1),
+                    "cavity_components")
+        return vox, bor
+
     @property
     def max_neighbor_per_atom(self) -> int:
         return int(self._lib.sesgb_max_neighbor_per_atom(self._h))
@@ -347,7 +401,8 @@ class SesBatch(SesBuild):
     the whole batch, molecule m's slice equal to its own SesBuild."""
 
     def __init__(self, molecules, probe_radius: float = 1.4, mode: str = "full", max_neighbor_per_atom: int = 0,
-                 max_intersections_per_circle: int = 0, graph: bool = True, device: int = -1, profile: bool = False):
+                 max_intersections_per_circle: int = 0, graph: bool = True, device: int = -1, profile: bool = False,
+                 min_capacity: bool = False):
         self._lib = load_library()
         mols = [np.ascontiguousarray(np.asarray(m, np.float32).reshape(-1, 4)) for m in molecules]
         self.starts = np.zeros(len(mols) + 1, np.uint32)
@@ -355,7 +410,7 @@ class SesBatch(SesBuild):
         self.atoms = np.ascontiguousarray(np.concatenate(mols) if mols else np.zeros((0, 4), np.float32))
         self.mode = mode
         self.probe_radius = float(probe_radius)
-        flags = (FLAG_GRAPH if graph else 0) | (FLAG_PROFILE if profile else 0)
+        flags = (FLAG_GRAPH if graph else 0) | (FLAG_PROFILE if profile else 0) | (FLAG_MIN_CAPACITY if min_capacity else 0)
         opt = Options(max_neighbor_per_atom, max_intersections_per_circle, device, flags)
         h = ctypes.c_void_p()
         st = self._lib.sesgb_create_batch(self.atoms.ctypes.data if self.atoms.size else None, self.starts.ctypes.data,

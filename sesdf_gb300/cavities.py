@@ -14,6 +14,11 @@ thinner than the grid, which it splits off as one-voxel components or misses (ab
 a 2,000-atom globule change class between h = 0.25 and 0.2 A). A probe position lies on the boundary of
 E (it touches three SAS spheres), so it takes the component of the nearest accessible voxel centre within
 two voxels; "probe_resolved" is false where there is none.
+
+``classify_gpu`` is the same classification on the device (``sesgb_cavities``: SAS spheres rasterised
+into an occupancy bit grid, lock-free union-find over the accessible voxels, components numbered in the
+order of their first voxel, probes of the build assigned by the same nearest-voxel rule); its labels
+equal this module's, voxel for voxel, for the same atoms, probe radius and spacing.
 """
 from __future__ import annotations
 
@@ -98,4 +103,28 @@ def classify(atoms: np.ndarray, probe_radius: float, probes: np.ndarray | None =
         # 0: no accessible voxel centre near the probe (E is thinner than h there)
         out["probe_resolved"] = comp > 0
         out["probe_in_cavity"] = np.isin(comp, cav)
+    return out
+
+
+def classify_gpu(build, h: float = 0.25, with_labels: bool = True) -> dict:
+    """classify() of a built SesBuild (one molecule, either mode) on the device: the same keys, the
+    probes being the build's own (its concave-patch positions). The grid uses the build's float32
+    probe radius."""
+    import torch
+
+    k = build.counts()["probes"]
+    comp = torch.zeros(max(k, 1), dtype=torch.int32, device="cuda")
+    info = build.cavities(h, comp.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    n = info["components"]
+    vox, bor = build.cavity_components(n)
+    ext = {int(x) for x in np.flatnonzero(bor[1:]) + 1}
+    cav = [x for x in range(1, n + 1) if x not in ext]
+    out = {"origin": info["origin"], "h": h, "exterior": ext, "cavities": cav,
+           "cavity_volume": [float(vox[x]) * h ** 3 for x in cav], "dims": info["dims"], "voxels": vox}
+    if with_labels:
+        out["labels"] = build.cavity_labels().reshape(info["dims"])
+    pc = comp.cpu().numpy()[:k]
+    out["probe_component"] = pc
+    out["probe_resolved"] = pc > 0
+    out["probe_in_cavity"] = np.isin(pc, cav)
     return out

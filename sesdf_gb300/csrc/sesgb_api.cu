@@ -46,6 +46,15 @@ struct sesgb_ctx
     void *   areaScratch = nullptr;
     size_t   areaScratchBytes = 0;
 
+    // cavities (sesgb_cavities): one grow-only allocation carved into the grid's parts
+    void *   cavMem = nullptr;
+    size_t   cavBytes = 0;
+    int32_t * cavLabels = nullptr;
+    uint32_t * cavVoxels = nullptr;
+    uint8_t *  cavBorder = nullptr;
+    uint64_t   cavV = 0;
+    uint32_t   cavComponents = 0;
+
     Build          b {};
     DeviceCounts * hCounts = nullptr;
     void *         scanScratch = nullptr;
@@ -79,7 +88,9 @@ struct sesgb_ctx
 namespace
 {
     const char * kStatusNames[] = { "ok", "invalid argument", "CUDA error", "capacity overflow", "not built", "timeout",
-                                    "wrong mode", "input exceeds the no-allocation limit (SESGB_NOALLOC_MAX_ATOMS)" };
+                                    "wrong mode",
+                                    "input exceeds a fixed limit (the no-allocation limit SESGB_NOALLOC_MAX_ATOMS, or 2^28 "
+                                    "cavity-grid voxels)" };
 
     bool cuda_ok( sesgb_ctx * c, cudaError_t e, const char * what )
     {
@@ -357,6 +368,22 @@ namespace
         mark( 10 );
     }
 
+    // first capacities: protein-like ratios to the atom count (regrown on demand), or the
+    // minimum with SESGB_FLAG_MIN_CAPACITY
+    void initial_capacities( sesgb_ctx * c )
+    {
+        Build &        b   = c->b;
+        const uint64_t n   = ( c->flags & SESGB_FLAG_MIN_CAPACITY ) ? 0 : c->n;
+        b.capSectors       = grow( 40ull * n );
+        b.capFull          = grow( 4ull * n );
+        b.capC1            = grow( 24ull * n );
+        b.capProbes        = grow( 8ull * n );
+        b.capVisBand       = grow( n ? std::max<uint64_t>( 1u << 16, n / 2 ) : 0 );
+        b.capPairs         = grow( 40ull * n );
+        b.capSeg           = grow( 8ull * n );
+        b.capTori          = grow( 16ull * n );
+    }
+
     // regrows the buffers whose counts exceeded their capacity; true if any
     bool regrow( sesgb_ctx * c )
     {
@@ -560,14 +587,7 @@ extern "C"
 
         // first capacities from protein-like ratios; regrown on demand
         Build & b    = c->b;
-        b.capSectors = grow( 40ull * n );
-        b.capFull    = grow( 4ull * n );
-        b.capC1      = grow( 24ull * n );
-        b.capProbes  = grow( 8ull * n );
-        b.capVisBand = grow( std::max<uint64_t>( 1u << 16, n / 2 ) );
-        b.capPairs   = grow( 40ull * n );
-        b.capSeg     = grow( 8ull * n );
-        b.capTori    = grow( 16ull * n );
+        initial_capacities( c );
         if ( !allocate_fixed( c ) || !allocate_dynamic( c ) || !cuda_ok( c, configure_kernels( c->b ), "configure" ) )
         {
             const int st = SESGB_ERR_CUDA;
@@ -810,6 +830,8 @@ extern "C"
             cudaFree( c->areaParts );
         if ( c->areaScratch )
             cudaFree( c->areaScratch );
+        if ( c->cavMem )
+            cudaFree( c->cavMem );
         delete c;
     }
 
@@ -871,6 +893,181 @@ extern "C"
         launch_sdf_backward( c->b, device_queries, m, SESGB_SDF_BAND, device_grad_sdf, c->gradSorted, device_grad_atoms,
                              c->sdfScratch, s );
         return cuda_ok( c, cudaGetLastError(), "sdf backward" ) ? SESGB_OK : SESGB_ERR_CUDA;
+    }
+
+    int sesgb_render( sesgb_ctx * c, const sesgb_camera * cam, float * device_depth, float * device_normals, void * stream )
+    {
+        if ( !c || !cam || !device_depth || !cam->width || !cam->height || (uint64_t)cam->width * cam->height > ( 1ull << 28 )
+             || cam->max_steps > ( 1u << 20 ) || !( cam->eps > 0.0 ) || !( cam->normal_step > 0.0 ) )
+            return SESGB_ERR_INVALID;
+        cudaStream_t s  = static_cast<cudaStream_t>( stream );
+        int          st = sdf_prepare( c, 0, s );
+        if ( st != SESGB_OK )
+            return st;
+        TraceParams p;
+        for ( int a = 0; a < 3; a++ )
+        {
+            p.eye[ a ]     = cam->eye[ a ];
+            p.forward[ a ] = cam->forward[ a ];
+            p.right[ a ]   = cam->right[ a ];
+            p.up[ a ]      = cam->up[ a ];
+        }
+        p.tanHalfFov = cam->tan_half_fov;
+        p.tNear      = cam->t_near;
+        p.tFar       = cam->t_far;
+        p.eps        = cam->eps;
+        p.normalStep = cam->normal_step;
+        p.width      = cam->width;
+        p.height     = cam->height;
+        p.maxSteps   = cam->max_steps;
+        launch_trace( c->b, p, SESGB_SDF_BAND, device_depth, device_normals, s );
+        return cuda_ok( c, cudaGetLastError(), "render" ) ? SESGB_OK : SESGB_ERR_CUDA;
+    }
+
+    // ---- exterior and cavities ---------------------------------------------------
+    int sesgb_cavities( sesgb_ctx * c, double voxel, sesgb_cavity_info * info, int32_t * device_probe_component, void * stream )
+    {
+        if ( !c || !info || !( voxel >= 0.05 ) || !( voxel <= 100.0 ) )
+            return SESGB_ERR_INVALID;
+        if ( !c->built )
+            return SESGB_ERR_NOT_BUILT;
+        if ( c->nMol != 1 || c->n == 0 )
+        {
+            c->err = "cavities need a build of one molecule with atoms";
+            return SESGB_ERR_MODE;
+        }
+        cudaStream_t s   = static_cast<cudaStream_t>( stream );
+        const double rp  = (double)c->rp;
+        const double h   = voxel;
+        // grid: bounds of the SAS spheres on the device, then the grid shape on the host
+        auto carve = []( char *& p, size_t bytes ) {
+            char * q = p;
+            p += ( bytes + 255 ) & ~(size_t)255;
+            return q;
+        };
+        const size_t small = 256;
+        if ( c->cavBytes < small )
+        {
+            if ( c->cavMem )
+                cudaFree( c->cavMem );
+            c->cavMem   = nullptr;
+            c->cavBytes = 0;
+            if ( !cuda_ok( c, cudaMalloc( &c->cavMem, small ), "cudaMalloc" ) )
+                return SESGB_ERR_CUDA;
+            c->cavBytes = small;
+        }
+        double bounds[ 6 ];
+        launch_cavity_bounds( c->b, rp, static_cast<double *>( c->cavMem ), s );
+        if ( !cuda_ok( c, cudaMemcpyAsync( bounds, c->cavMem, sizeof( bounds ), cudaMemcpyDeviceToHost, s ), "bounds" )
+             || !cuda_ok( c, cudaStreamSynchronize( s ), "bounds" ) )
+            return SESGB_ERR_CUDA;
+        CavGrid  g;
+        uint64_t V = 1;
+        for ( int a = 0; a < 3; a++ )
+        {
+            const double lo = bounds[ a ] - 2.0 * h, hi = bounds[ 3 + a ] + 2.0 * h;
+            const double d  = std::ceil( ( hi - lo ) / h ) + 1.0;
+            if ( !( d >= 1.0 ) || d > (double)( 1u << 28 ) )
+            {
+                c->err = "the cavity grid is too large for this voxel size";
+                return SESGB_ERR_TOO_LARGE;
+            }
+            g.lo[ a ]   = lo;
+            g.dims[ a ] = (uint32_t)d;
+            V *= g.dims[ a ];
+        }
+        g.h  = h;
+        g.rp = rp;
+        if ( V > ( 1ull << 28 ) )
+        {
+            c->err = "the cavity grid exceeds 2^28 voxels: use a larger voxel size";
+            return SESGB_ERR_TOO_LARGE;
+        }
+        const uint32_t rootCap = (uint32_t)std::min<uint64_t>( V, 1u << 22 );
+        const size_t   need    = small + ( ( ( V + 31 ) / 32 * 4 + 255 ) & ~(size_t)255 ) + ( ( V * 4 + 255 ) & ~(size_t)255 )
+                            + 2 * ( ( (size_t)rootCap * 4 + 255 ) & ~(size_t)255 ) + ( ( ( rootCap + 1ull ) * 4 + 255 ) & ~(size_t)255 )
+                            + ( ( rootCap + 1ull + 255 ) & ~(size_t)255 ) + radix_scratch_bytes( rootCap ) + 256;
+        if ( need > c->cavBytes )
+        {
+            cudaFree( c->cavMem );
+            c->cavMem   = nullptr;
+            c->cavBytes = 0;
+            if ( !cuda_ok( c, cudaMalloc( &c->cavMem, need ), "cudaMalloc" ) )
+                return SESGB_ERR_CUDA;
+            c->cavBytes = need;
+        }
+        char *     p       = static_cast<char *>( c->cavMem );
+        uint32_t * scalars = reinterpret_cast<uint32_t *>( carve( p, small ) );
+        uint32_t * bits    = reinterpret_cast<uint32_t *>( carve( p, ( V + 31 ) / 32 * 4 ) );
+        int32_t *  labels  = reinterpret_cast<int32_t *>( carve( p, V * 4 ) );
+        uint32_t * roots   = reinterpret_cast<uint32_t *>( carve( p, (size_t)rootCap * 4 ) );
+        uint32_t * order   = reinterpret_cast<uint32_t *>( carve( p, (size_t)rootCap * 4 ) );
+        uint32_t * voxels  = reinterpret_cast<uint32_t *>( carve( p, ( rootCap + 1ull ) * 4 ) );
+        uint8_t *  border  = reinterpret_cast<uint8_t *>( carve( p, rootCap + 1ull ) );
+        void *     radix   = carve( p, radix_scratch_bytes( rootCap ) );
+        launch_cavity_labels( c->b, g, bits, labels, roots, rootCap, scalars, s );
+        uint32_t hs[ 2 ];
+        if ( !cuda_ok( c, cudaMemcpyAsync( hs, scalars, sizeof( hs ), cudaMemcpyDeviceToHost, s ), "labels" )
+             || !cuda_ok( c, cudaStreamSynchronize( s ), "labels" ) )
+            return SESGB_ERR_CUDA;
+        if ( hs[ 1 ] )
+        {
+            c->err = ( hs[ 1 ] & 4u ) ? "more than 2^22 components in the cavity grid" : "cavity labelling did not converge";
+            return SESGB_ERR_OVERFLOW;
+        }
+        const uint32_t nRoots = hs[ 0 ];
+        radix_sort( roots, order, nRoots, 28, radix, s ); // voxel indices are below 2^28
+        const uint32_t nProbes = device_probe_component ? c->hCounts->I : 0u;
+        launch_cavity_relabel( g, labels, roots, nRoots, voxels, border, c->b.probePos, nProbes, device_probe_component, s );
+        std::vector<uint8_t> hb( nRoots + 1ull );
+        if ( !cuda_ok( c, cudaMemcpyAsync( hb.data(), border, hb.size(), cudaMemcpyDeviceToHost, s ), "components" )
+             || !cuda_ok( c, cudaStreamSynchronize( s ), "components" ) )
+            return SESGB_ERR_CUDA;
+        uint32_t ext = 0;
+        for ( uint32_t k = 1; k <= nRoots; k++ )
+            ext += hb[ k ] != 0;
+        c->cavLabels     = labels;
+        c->cavVoxels     = voxels;
+        c->cavBorder     = border;
+        c->cavV          = V;
+        c->cavComponents = nRoots;
+        for ( int a = 0; a < 3; a++ )
+        {
+            info->origin[ a ] = g.lo[ a ];
+            info->dims[ a ]   = g.dims[ a ];
+        }
+        info->voxel      = h;
+        info->components = nRoots;
+        info->exterior   = ext;
+        info->cavities   = nRoots - ext;
+        info->probes     = nProbes;
+        return SESGB_OK;
+    }
+
+    int sesgb_cavity_labels( sesgb_ctx * c, const int32_t ** device_labels, uint64_t * voxels )
+    {
+        if ( !c || !device_labels || !voxels )
+            return SESGB_ERR_INVALID;
+        if ( !c->cavLabels )
+            return SESGB_ERR_NOT_BUILT;
+        *device_labels = c->cavLabels;
+        *voxels        = c->cavV;
+        return SESGB_OK;
+    }
+
+    int sesgb_cavity_components( sesgb_ctx * c, uint32_t * host_voxels, uint8_t * host_border, uint32_t capacity )
+    {
+        if ( !c )
+            return SESGB_ERR_INVALID;
+        if ( !c->cavLabels )
+            return SESGB_ERR_NOT_BUILT;
+        if ( capacity < c->cavComponents + 1u )
+            return SESGB_ERR_OVERFLOW;
+        if ( host_voxels && !cuda_ok( c, cudaMemcpy( host_voxels, c->cavVoxels, 4ull * ( c->cavComponents + 1ull ), cudaMemcpyDeviceToHost ), "components" ) )
+            return SESGB_ERR_CUDA;
+        if ( host_border && !cuda_ok( c, cudaMemcpy( host_border, c->cavBorder, c->cavComponents + 1ull, cudaMemcpyDeviceToHost ), "components" ) )
+            return SESGB_ERR_CUDA;
+        return SESGB_OK;
     }
 
     // ---- SES area of the primitives ---------------------------------------------
@@ -1016,14 +1213,7 @@ extern "C"
         host_aabb( atoms, n, c->aabb );
 
         Build & b    = c->b;
-        b.capSectors = grow( 40ull * n );
-        b.capFull    = grow( 4ull * n );
-        b.capC1      = grow( 24ull * n );
-        b.capProbes  = grow( 8ull * n );
-        b.capVisBand = grow( std::max<uint64_t>( 1u << 16, n / 2 ) );
-        b.capPairs   = grow( 40ull * n );
-        b.capSeg     = grow( 8ull * n );
-        b.capTori    = grow( 16ull * n );
+        initial_capacities( c );
         if ( !allocate_fixed( c ) || !allocate_dynamic( c ) || !cuda_ok( c, configure_kernels( c->b ), "configure" ) )
         {
             const int st = SESGB_ERR_CUDA;

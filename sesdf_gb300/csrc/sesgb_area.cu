@@ -785,7 +785,11 @@ namespace sesgb
         }
 
         // probe positions follow their atoms: M^T lambda = g with rows p - c_a;
-        // d/dc_a = lambda_a (p - c_a), d/dR_a = lambda_a R_a
+        // d/dc_a = lambda_a (p - c_a), d/dR_a = lambda_a R_a. The 3x3 solve is in double
+        // precision: for a probe near the plane of its three centres (its mirror probe about to
+        // merge with it) M is nearly singular and lambda grows as 1 / det, so float32 rounding of
+        // the rows and of det would show in the atoms' gradients. One solve per probe: the FP64
+        // pipe's rate does not matter here.
         __global__ void k_area_probe_back( Build b, const float4 * probeGrad, float * gradSorted )
         {
             const uint32_t I = min( b.counts->I, b.capProbes );
@@ -794,25 +798,28 @@ namespace sesgb
                 const float4 g4 = probeGrad[ p ];
                 if ( g4.x == 0.f && g4.y == 0.f && g4.z == 0.f )
                     continue;
-                const f3     g  = F3( g4.x, g4.y, g4.z );
+                const d3     g  = D3( (double)g4.x, (double)g4.y, (double)g4.z );
                 const int4   id = b.probeIds[ p ];
                 const float4 pp = b.probePos[ p ];
                 const int    ia[ 3 ] = { id.x, id.y, id.z };
-                f3           r[ 3 ];
-                float        R[ 3 ];
+                d3           r[ 3 ];
+                double       R[ 3 ];
                 for ( int k = 0; k < 3; k++ )
                 {
                     const float4 c = b.atoms[ ia[ k ] ];
-                    r[ k ]         = F3( pp.x - c.x, pp.y - c.y, pp.z - c.z );
-                    R[ k ]         = c.w + b.rp;
+                    // differences of float32 values: exact in double
+                    r[ k ] = D3( (double)pp.x - (double)c.x, (double)pp.y - (double)c.y, (double)pp.z - (double)c.z );
+                    R[ k ] = (double)c.w + (double)b.rp;
                 }
-                const float det = dot( r[ 0 ], cross( r[ 1 ], r[ 2 ] ) );
-                if ( !( fabsf( det ) > 0.f ) )
+                const double det = ddot( r[ 0 ], dcross( r[ 1 ], r[ 2 ] ) );
+                if ( !( fabs( det ) > 0.0 ) )
                     continue;
-                const float lam[ 3 ] = { dot( g, cross( r[ 1 ], r[ 2 ] ) ) / det, dot( r[ 0 ], cross( g, r[ 2 ] ) ) / det,
-                                         dot( r[ 0 ], cross( r[ 1 ], g ) ) / det };
+                const double lam[ 3 ] = { ddot( g, dcross( r[ 1 ], r[ 2 ] ) ) / det, ddot( r[ 0 ], dcross( g, r[ 2 ] ) ) / det,
+                                          ddot( r[ 0 ], dcross( r[ 1 ], g ) ) / det };
                 for ( int k = 0; k < 3; k++ )
-                    add4( gradSorted, (uint32_t)ia[ k ], r[ k ] * lam[ k ], lam[ k ] * R[ k ] );
+                    add4( gradSorted, (uint32_t)ia[ k ],
+                          F3( (float)( r[ k ].x * lam[ k ] ), (float)( r[ k ].y * lam[ k ] ), (float)( r[ k ].z * lam[ k ] ) ),
+                          (float)( lam[ k ] * R[ k ] ) );
             }
         }
 

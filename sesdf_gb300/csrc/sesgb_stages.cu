@@ -1468,7 +1468,12 @@ namespace sesgb
                         m.full[ s ]       = cn[ h ] >= b.cap;
                         isP               = st[ h ] == 1 && i < j;
                         if ( isP && useMask )
-                            m.touch[ s ] = b.touch[ b.pairOff[ i ] + s ];
+                        {
+                            // past the touch buffer's capacity (a build that overflowed P and is built
+                            // again) every neighbour counts as touching
+                            const uint32_t at = b.pairOff[ i ] + s;
+                            m.touch[ s ]      = at < b.capPairs ? b.touch[ at ] : ~0ull;
+                        }
                         d2max = fmaxf( d2max, dd );
                         bmax  = fmaxf( bmax, Ri * Ri + dd + Rl * Rl );
                     }
@@ -1646,8 +1651,10 @@ namespace sesgb
                 if ( fp64 )
                     atomicAdd( &b.counts->fp64[ kFp64Neighbor ], fp64 );
             }
-            chunk           = __shfl_sync( 0xffffffffu, chunk, 0 );
-            const bool fits = chunk + kept <= b.capProbes;
+            chunk = __shfl_sync( 0xffffffffu, chunk, 0 );
+            // an atom with more entries than the warp holds (an error of the build) places none, so
+            // that the probe offsets stay within the staged ones
+            const bool fits = chunk + kept <= b.capProbes && nEnt <= (uint32_t)kProbeBuf;
             // jobs: a fill entry is one job (counted up from the bottom of the job array); a
             // band candidate's two entries are one job on its first entry (counted down
             // from the top), so that each kind runs with full warps
@@ -1930,9 +1937,14 @@ namespace sesgb
                 b.probeIds[ dst ] = b.stageIds[ chunk + m ];
                 if ( b.mode == 0 )
                 {
-                    atomicAdd( &b.ccount[ cid.x ], 1u );
-                    atomicAdd( &b.ccount[ cid.y ], 1u );
-                    atomicAdd( &b.ccount[ cid.z ], 1u );
+                    // partial-circle numbers beyond the capacity exist only in a build that overflowed
+                    // C1 (flagged by k_emit) and is built again after regrowing
+                    if ( (uint32_t)cid.x < b.capC1 )
+                        atomicAdd( &b.ccount[ cid.x ], 1u );
+                    if ( (uint32_t)cid.y < b.capC1 )
+                        atomicAdd( &b.ccount[ cid.y ], 1u );
+                    if ( (uint32_t)cid.z < b.capC1 )
+                        atomicAdd( &b.ccount[ cid.z ], 1u );
                 }
                 else
                 {
@@ -1957,7 +1969,9 @@ namespace sesgb
                 const uint32_t t3[ 3 ] = { (uint32_t)cid.x, (uint32_t)cid.y, (uint32_t)cid.z };
                 for ( int e = 0; e < 3; e++ )
                 {
-                    const uint32_t t   = t3[ e ];
+                    const uint32_t t = t3[ e ];
+                    if ( t >= b.capC1 ) // only in a build that overflowed C1 (see k_place)
+                        continue;
                     const uint32_t pos = b.cstart[ t ] + atomicAdd( &b.ccursor[ t ], 1u );
                     b.clist[ pos ]     = q;
                 }
@@ -2360,8 +2374,10 @@ namespace sesgb
                     o[ kMolSectorBase ]  = b.visOff[ a0 ];
                     o[ kMolFull ]        = b.fullOff[ a1 ] - b.fullOff[ a0 ];
                     o[ kMolFullBase ]    = b.fullOff[ a0 ];
-                    o[ kMolSegments ]    = b.segOff[ b.partOff[ a1 ] ] - b.segOff[ b.partOff[ a0 ] ];
-                    o[ kMolSegmentBase ] = b.segOff[ b.partOff[ a0 ] ];
+                    // segOff holds min(C1, capC1) + 1 entries (larger C1: a build that is done again)
+                    const uint32_t t0    = min( b.partOff[ a0 ], b.capC1 ), t1 = min( b.partOff[ a1 ], b.capC1 );
+                    o[ kMolSegments ]    = b.segOff[ t1 ] - b.segOff[ t0 ];
+                    o[ kMolSegmentBase ] = b.segOff[ t0 ];
                     o[ kMolTori ] = o[ kMolToriBase ] = 0;
                 }
                 else
@@ -3203,6 +3219,112 @@ namespace sesgb
                     gradInput[ 4 * (size_t)i + k ] = gradSorted[ 4 * (size_t)s + k ];
             }
         }
+
+        // ---- headless image: sphere tracing of the signed distance ------------------
+        // Every pixel's ray x(t) = eye + t d advances by a step that never crosses the SES:
+        // inside the SAS (kinds 3-5) the value rp - dist(x, E) bounds the distance to the SES
+        // (every SES point lies at rp from E); outside (kinds 1, 2) value - rp bounds the distance
+        // to the SAS, which holds the SES. A ray stops when an inside value falls below eps (a hit
+        // at t), when it reaches a point deeper than the band (kind 0, taken as a hit), or when t
+        // passes tFar; it advances by at least eps / 4. Directions, ray points and the depth are
+        // evaluated in double precision with explicit rounding, in the order a host tracer writes
+        // them, so that the image does not depend on contraction choices. The normal of a hit is
+        // the normalised central difference of the signed distance (step normalStep).
+        __device__ __forceinline__ double trace_step( const SdfHit & h, double rp, double eps, bool & stop )
+        {
+            const bool   inside = h.kind == kSdfSphere || h.kind == kSdfCircle || h.kind == kSdfProbe;
+            const double v      = (double)h.value;
+            stop                = ( inside && v < eps ) || h.kind == kSdfClampInside;
+            const double step   = inside ? v : __dsub_rn( v, rp );
+            return fmax( step, __dmul_rn( 0.25, eps ) );
+        }
+
+        __device__ __forceinline__ float3 ray_point( const double eye[ 3 ], d3 d, double t )
+        {
+            return make_float3( (float)__dadd_rn( eye[ 0 ], __dmul_rn( t, d.x ) ), (float)__dadd_rn( eye[ 1 ], __dmul_rn( t, d.y ) ),
+                                (float)__dadd_rn( eye[ 2 ], __dmul_rn( t, d.z ) ) );
+        }
+
+        __global__ void __launch_bounds__( 32 * kSdfWarps, 8 ) k_trace( Build b, TraceParams p, float band, float * depth,
+                                                                       float * normals )
+        {
+            __shared__ SdfSmem smem[ kSdfWarps ];
+            const uint32_t     warp = threadIdx.x >> 5, lane = lane_id();
+            uint32_t           overflow = 0;
+            const uint32_t     pixels   = p.width * p.height;
+            const double       rp       = (double)b.rp;
+            const d3           f        = D3( p.forward[ 0 ], p.forward[ 1 ], p.forward[ 2 ] );
+            const d3           r        = D3( p.right[ 0 ], p.right[ 1 ], p.right[ 2 ] );
+            const d3           u        = D3( p.up[ 0 ], p.up[ 1 ], p.up[ 2 ] );
+            for ( uint32_t px = blockIdx.x * kSdfWarps + warp; px < pixels; px += gridDim.x * kSdfWarps )
+            {
+                const uint32_t iy = px / p.width, ix = px - iy * p.width;
+                // pinhole ray through the pixel centre, row-major from the top left
+                const double xs = __dmul_rn( __dmul_rn( __dsub_rn( __ddiv_rn( __dmul_rn( 2.0, __dadd_rn( (double)ix, 0.5 ) ),
+                                                                              (double)p.width ), 1.0 ), p.tanHalfFov ),
+                                             (double)p.width );
+                const double xsw = __ddiv_rn( xs, (double)p.height );
+                const double ys  = __dmul_rn( __dsub_rn( 1.0, __ddiv_rn( __dmul_rn( 2.0, __dadd_rn( (double)iy, 0.5 ) ),
+                                                                         (double)p.height ) ), p.tanHalfFov );
+                d3           d   = dadd( dadd( f, dmul( r, xsw ) ), dmul( u, ys ) );
+                const double len = __dsqrt_rn( ddot( d, d ) );
+                d                = D3( __ddiv_rn( d.x, len ), __ddiv_rn( d.y, len ), __ddiv_rn( d.z, len ) );
+                double t   = p.tNear;
+                double hit = __longlong_as_double( 0x7ff0000000000000ll ); // +inf: background
+                for ( uint32_t step = 0; step < p.maxSteps && t <= p.tFar; step++ )
+                {
+                    const SdfHit h = sdf_query( b, ray_point( p.eye, d, t ), smem[ warp ], band, overflow );
+                    bool         stop;
+                    const double adv = trace_step( h, rp, p.eps, stop );
+                    if ( stop )
+                    {
+                        hit = t;
+                        break;
+                    }
+                    t = __dadd_rn( t, adv );
+                }
+                float3 nrm = make_float3( 0.f, 0.f, 0.f );
+                if ( normals && hit < 1e300 )
+                {
+                    const d3 x = D3( __dadd_rn( p.eye[ 0 ], __dmul_rn( hit, d.x ) ), __dadd_rn( p.eye[ 1 ], __dmul_rn( hit, d.y ) ),
+                                     __dadd_rn( p.eye[ 2 ], __dmul_rn( hit, d.z ) ) );
+                    double g[ 3 ];
+                    for ( int a = 0; a < 3; a++ )
+                    {
+                        double v2[ 2 ];
+                        for ( int sg = 0; sg < 2; sg++ )
+                        {
+                            const double e = sg == 0 ? p.normalStep : -p.normalStep;
+                            float3       q = make_float3( (float)x.x, (float)x.y, (float)x.z );
+                            if ( a == 0 )
+                                q.x = (float)__dadd_rn( x.x, e );
+                            else if ( a == 1 )
+                                q.y = (float)__dadd_rn( x.y, e );
+                            else
+                                q.z = (float)__dadd_rn( x.z, e );
+                            v2[ sg ] = (double)sdf_query( b, q, smem[ warp ], band, overflow ).value;
+                        }
+                        g[ a ] = __ddiv_rn( __dsub_rn( v2[ 0 ], v2[ 1 ] ), __dmul_rn( 2.0, p.normalStep ) );
+                    }
+                    const double gl = __dsqrt_rn( __dadd_rn( __dadd_rn( __dmul_rn( g[ 0 ], g[ 0 ] ), __dmul_rn( g[ 1 ], g[ 1 ] ) ),
+                                                             __dmul_rn( g[ 2 ], g[ 2 ] ) ) );
+                    const double inv = gl > 0.0 ? gl : 1.0;
+                    nrm = make_float3( (float)__ddiv_rn( g[ 0 ], inv ), (float)__ddiv_rn( g[ 1 ], inv ), (float)__ddiv_rn( g[ 2 ], inv ) );
+                }
+                if ( lane == 0 )
+                {
+                    depth[ px ] = (float)hit;
+                    if ( normals )
+                    {
+                        normals[ 3 * (size_t)px ]     = nrm.x;
+                        normals[ 3 * (size_t)px + 1 ] = nrm.y;
+                        normals[ 3 * (size_t)px + 2 ] = nrm.z;
+                    }
+                }
+            }
+            if ( lane == 0 && overflow )
+                atomicOr( &b.counts->overflow, (uint32_t)kOverflowSdfList );
+        }
     } // namespace
 
     size_t sdf_scratch_bytes( uint32_t m ) { return 2 * ( ( (size_t)m * 4 + 255 ) & ~(size_t)255 ) + radix_scratch_bytes( m ); }
@@ -3230,6 +3352,16 @@ namespace sesgb
         k_sdf<false><<<blocks, 32 * kSdfWarps, 0, s>>>( b, queries, m, band, sdf, nullptr, nullptr, kind, order );
         counted();
     }
+    void launch_trace( const Build & b, const TraceParams & p, float band, float * depth, float * normals, cudaStream_t s )
+    {
+        const uint32_t pixels = p.width * p.height;
+        if ( !pixels )
+            return;
+        const uint32_t blocks = min( persistent_blocks( 32 * kSdfWarps ) * 2, ( pixels + kSdfWarps - 1 ) / kSdfWarps );
+        k_trace<<<blocks, 32 * kSdfWarps, 0, s>>>( b, p, band, depth, normals );
+        counted();
+    }
+
     void launch_sdf_backward( const Build & b, const float * queries, uint32_t m, float band, const float * gradSdf,
                               float * gradSorted, float * gradInput, void * scratch, cudaStream_t s )
     {

@@ -130,6 +130,32 @@ namespace sesgb
                        cudaStream_t s );
     void   launch_sdf_backward( const Build & b, const float * queries, uint32_t m, float band, const float * gradSdf,
                                 float * gradSorted, float * gradInput, void * scratch, cudaStream_t s );
+    // headless image: every pixel's ray sphere-traced against the signed distance (same grid as the SDF)
+    struct TraceParams
+    {
+        double   eye[ 3 ], forward[ 3 ], right[ 3 ], up[ 3 ];
+        double   tanHalfFov, tNear, tFar, eps, normalStep;
+        uint32_t width, height, maxSteps;
+    };
+    void launch_trace( const Build & b, const TraceParams & p, float band, float * depth, float * normals, cudaStream_t s );
+    // components of the probe-accessible space on a voxel grid (sesgb_cavities.cu)
+    struct CavGrid
+    {
+        double   lo[ 3 ]; // centre of voxel (0, 0, 0)
+        double   h;
+        double   rp;
+        uint32_t dims[ 3 ];
+    };
+    // out (device double[6]): min and max of c -+ (r + rp) over the build's atoms
+    void launch_cavity_bounds( const Build & b, double rp, double * out, cudaStream_t s );
+    // occupancy bits, union-find labels (root = smallest voxel index), roots collected into roots
+    // (scalars[0] = count, scalars[1] = error bits)
+    void launch_cavity_labels( const Build & b, const CavGrid & g, uint32_t * bits, int32_t * labels, uint32_t * roots,
+                               uint32_t rootCap, uint32_t * scalars, cudaStream_t s );
+    // labels 1..nRoots by the rank of their root in the sorted roots; voxel counts and border flags
+    // per label; the label of each of k probes (probeLabel may be null)
+    void launch_cavity_relabel( const CavGrid & g, int32_t * labels, const uint32_t * roots, uint32_t nRoots, uint32_t * voxels,
+                                uint8_t * border, const float4 * probes, uint32_t k, int32_t * probeLabel, cudaStream_t s );
     // SES area of the primitives of a full-surface build (sesgb_area.cu): parts (device
     // double[3]: convex, toroidal, concave), atomArea (optional, float[n], input order)
     size_t area_scratch_bytes( const Build & b );

@@ -14,7 +14,9 @@ A ray stops when an inside-SAS value falls below ``eps`` (a hit at depth t) or t
 Normals are the normalised central differences of the signed distance at the hit points.
 
 The tracer takes the signed distance as a function of (m, 3) float32 points, so the same code runs on
-the GPU build (``gpu_sdf_fn``) and, in the tests, on the FP64 oracle.
+the GPU build (``gpu_sdf_fn``) and, in the tests, on the FP64 oracle. ``gpu_depth_image`` is the same
+image from one device launch (``sesgb_render``: a warp per ray, the signed distance evaluated in the
+kernel, no host round trip per step); its ray arithmetic follows this module's operation for operation.
 """
 from __future__ import annotations
 
@@ -23,14 +25,20 @@ import numpy as np
 INSIDE_SAS = (3, 4, 5)
 
 
-def camera_rays(eye, target, up, fov_deg: float, width: int, height: int):
-    """Unit ray directions (height*width, 3) float64 of a pinhole camera, row-major from the top left."""
+def camera_basis(eye, target, up):
+    """Unit forward, right and up vectors (float64) of a camera at eye looking at target."""
     eye = np.asarray(eye, np.float64)
     f = np.asarray(target, np.float64) - eye
     f /= np.linalg.norm(f)
     r = np.cross(f, np.asarray(up, np.float64))
     r /= np.linalg.norm(r)
     u = np.cross(r, f)
+    return f, r, u
+
+
+def camera_rays(eye, target, up, fov_deg: float, width: int, height: int):
+    """Unit ray directions (height*width, 3) float64 of a pinhole camera, row-major from the top left."""
+    f, r, u = camera_basis(eye, target, up)
     h = np.tan(np.radians(fov_deg) / 2.0)
     xs = (2.0 * (np.arange(width) + 0.5) / width - 1.0) * h * width / height
     ys = (1.0 - 2.0 * (np.arange(height) + 0.5) / height) * h
@@ -44,6 +52,7 @@ def sphere_trace(sdf_fn, origin, dirs, probe_radius: float, t_near: float, t_far
     """Depth t (float64 [m], inf where the ray misses) of the first SES point along origin + t * dirs.
     sdf_fn(points float32 [k, 3]) -> (value [k], kind [k]) as numpy arrays."""
     m = dirs.shape[0]
+    probe_radius = float(np.float32(probe_radius))  # the build's float32 probe radius
     t = np.full(m, float(t_near))
     depth = np.full(m, np.inf)
     live = np.arange(m)
@@ -81,10 +90,8 @@ def normals(sdf_fn, points, h: float = 1e-2):
     return g / np.where(n > 0, n, 1.0)
 
 
-def depth_image(sdf_fn, atoms, probe_radius: float, width: int = 128, height: int = 128, view=(0.3, -1.0, 0.5),
-                fov_deg: float = 40.0, eps: float = 1e-3, with_normals: bool = True):
-    """Depth (height, width) float32 (inf = background) and normals (height, width, 3) float32 (0 where
-    the ray misses) of the SES of atoms seen from the direction view, the camera framing the SAS bounds."""
+def framing(atoms, probe_radius: float, view=(0.3, -1.0, 0.5), fov_deg: float = 40.0):
+    """Camera framing the SAS bounds of atoms from the direction view: (eye, centre, up, t_near, t_far)."""
     a = np.asarray(atoms, np.float64)
     lo = (a[:, :3] - a[:, 3:4] - probe_radius).min(axis=0)
     hi = (a[:, :3] + a[:, 3:4] + probe_radius).max(axis=0)
@@ -95,13 +102,39 @@ def depth_image(sdf_fn, atoms, probe_radius: float, width: int = 128, height: in
     dist = radius / np.sin(np.radians(fov_deg) / 2.0)
     eye = centre - dist * v
     up = (0.0, 0.0, 1.0) if abs(v[2]) < 0.9 else (0.0, 1.0, 0.0)
+    return eye, centre, up, max(dist - radius, 0.0), dist + radius
+
+
+def depth_image(sdf_fn, atoms, probe_radius: float, width: int = 128, height: int = 128, view=(0.3, -1.0, 0.5),
+                fov_deg: float = 40.0, eps: float = 1e-3, with_normals: bool = True):
+    """Depth (height, width) float32 (inf = background) and normals (height, width, 3) float32 (0 where
+    the ray misses) of the SES of atoms seen from the direction view, the camera framing the SAS bounds."""
+    eye, centre, up, t_near, t_far = framing(atoms, probe_radius, view, fov_deg)
     dirs = camera_rays(eye, centre, up, fov_deg, width, height)
-    depth = sphere_trace(sdf_fn, eye, dirs, probe_radius, max(dist - radius, 0.0), dist + radius, eps)
+    depth = sphere_trace(sdf_fn, eye, dirs, probe_radius, t_near, t_far, eps)
     nrm = np.zeros((width * height, 3))
     hit = np.isfinite(depth)
     if with_normals and hit.any():
         nrm[hit] = normals(sdf_fn, eye[None, :] + depth[hit, None] * dirs[hit])
     return depth.reshape(height, width).astype(np.float32), nrm.reshape(height, width, 3).astype(np.float32)
+
+
+def gpu_depth_image(build, width: int = 128, height: int = 128, view=(0.3, -1.0, 0.5), fov_deg: float = 40.0,
+                    eps: float = 1e-3, with_normals: bool = True, max_steps: int = 256, normal_step: float = 1e-2):
+    """depth_image of a built full-surface SesBuild in one device launch (sesgb_render)."""
+    import torch
+    eye, centre, up, t_near, t_far = framing(build.atoms, build.probe_radius, view, fov_deg)
+    f, r, u = camera_basis(eye, centre, up)
+    cam = dict(eye=eye, forward=f, right=r, up=u, tan_half_fov=float(np.tan(np.radians(fov_deg) / 2.0)),
+               t_near=float(t_near), t_far=float(t_far), eps=float(eps), normal_step=float(normal_step),
+               width=width, height=height, max_steps=max_steps)
+    depth = torch.empty(width * height, dtype=torch.float32, device="cuda")
+    nrm = torch.zeros(width * height * 3, dtype=torch.float32, device="cuda") if with_normals else None
+    build.render(cam, depth.data_ptr(), nrm.data_ptr() if nrm is not None else None,
+                 torch.cuda.current_stream().cuda_stream)
+    d = depth.cpu().numpy().reshape(height, width)
+    n = nrm.cpu().numpy().reshape(height, width, 3) if nrm is not None else np.zeros((height, width, 3), np.float32)
+    return d, n
 
 
 def gpu_sdf_fn(build):

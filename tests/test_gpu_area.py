@@ -92,6 +92,8 @@ def test_gradient_matches_oracle():
     err = np.abs(g - go)
     rel = np.linalg.norm(g - go) / np.linalg.norm(go)
     frac = np.mean(err <= 1e-3 * scale)
+    print(f"area adjoint, 2,000 atoms: GPU vs oracle {rel:.2e} relative (Frobenius), {frac:.4f} of components within "
+          f"1e-3 of the largest, worst {err.max() / scale:.2e}")
     assert rel <= 5e-3 and frac >= 0.995, (rel, frac, err.max(), scale, np.unravel_index(np.argmax(err), err.shape))
 
 
@@ -116,4 +118,6 @@ def test_sdf_workload_globule():
     for k, key in enumerate(("convex", "toroidal", "concave")):
         assert got[key] == pytest.approx(want[k], rel=1e-4), (key, got, want)
     assert np.mean(np.abs(per - wper) <= 1e-3 + 1e-4 * np.abs(wper)) >= 0.999
-    assert np.linalg.norm(g - go) <= 5e-3 * np.linalg.norm(go)
+    rel = np.linalg.norm(g - go) / np.linalg.norm(go)
+    print(f"area adjoint, 20,000 atoms: GPU vs oracle {rel:.2e} relative (Frobenius)")
+    assert rel <= 5e-3

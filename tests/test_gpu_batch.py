@@ -69,3 +69,14 @@ def test_batch_graph_replay_and_frames():
         b.build()
         b.build()  # replay
         compare(b, frames, "full")
+
+
+@pytest.mark.parametrize("mode", ["full", "exterior"])
+def test_batch_regrow_from_minimal_capacities(mode):
+    # the first batch build overflows every count-dependent buffer; after the regrow and the
+    # second build each molecule's slice still equals its own build
+    mols = molecules()
+    with SesBatch(mols, RP, mode, min_capacity=True) as b:
+        b.build()
+        assert b.counts()["rebuilds"] >= 1
+        compare(b, mols, mode)

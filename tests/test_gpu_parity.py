@@ -145,6 +145,30 @@ def test_neighbor_truncation(mode):
     compare(atoms, out, o, mode)
 
 
+@pytest.mark.parametrize("mode", ["full", "exterior"])
+def test_regrow_from_minimal_capacities(mode):
+    # every count-dependent buffer starts at its minimum: the first build overflows them all, the
+    # library regrows each to the counts it met and builds again; the result must be the default
+    # build's, and a second build must fit without another rebuild
+    atoms = synth.globule(20000, 1500)
+    with SesBuild(atoms, RP, mode) as g:
+        g.build()
+        want = g.fetch()
+    with SesBuild(atoms, RP, mode, min_capacity=True) as g:
+        g.build()
+        got = g.fetch()
+        first = g.counts()["rebuilds"]
+        g.build()
+        again = g.fetch()
+        second = g.counts()["rebuilds"]
+    assert first >= 1 and second == first
+    assert want["counts"]["rebuilds"] == 0
+    for k in want:
+        if k != "counts":
+            assert np.array_equal(got[k], want[k], equal_nan=True), k
+            assert np.array_equal(again[k], want[k], equal_nan=True), k
+
+
 @pytest.mark.slow
 @pytest.mark.parametrize("mode", ["full", "exterior"])
 def test_assembly_100k(mode):

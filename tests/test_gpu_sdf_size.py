@@ -1,0 +1,126 @@
+"""The SDF adjoint at its workload's size: a 20,000-atom globule (seed 1500), probe 1.4 A, 1,000,000
+query points within 3 A of its vdW surface (seed 1501), upstream weights g_q ~ N(0, 1).
+
+* The GPU adjoint of sum_q g_q sdf_q with respect to every atom's (x, y, z, r) against the oracle's
+  FP64 analytic gradient over all 1M queries.
+* FP64 central finite differences of the oracle (h = 1e-4 A) on 512 random atoms (seed 1502). The
+  signed distance of a query depends on atom a only within r_a + 2 rp + 3 A of it, and the surface
+  there only on atoms within ~23 A, so each atom's differences are taken on the oracle built from
+  the atoms within 28 A and the queries within reach (identical values to the whole molecule's).
+  A query whose signed distance is not differentiable within +-h (its active primitive changes: the
+  forward and backward one-sided slopes differ by more than 1e-3) is left out of both sides -- the
+  GPU side by subtracting the adjoint of exactly those queries -- and counted. The atoms are drawn
+  among those with accessible surface (an atom whose circles are all buried moves no query's
+  signed distance: its gradient is 0 on both sides). Tolerance: per atom, the gradient 4-vector
+  within 1e-3 of the finite-difference vector's norm.
+"""
+import multiprocessing
+import os
+
+import numpy as np
+import pytest
+
+from oracle import oracle
+from sesdf_gb300 import SesBuild, synth
+
+pytestmark = [pytest.mark.gpu, pytest.mark.slow]
+RP = 1.4
+H = 1e-4
+SUBSET = 28.0
+KINK = 1e-3  # forward and backward slopes further apart than this: not differentiable within +-h
+_W = {}
+
+
+def _init_worker():
+    atoms, q = synth.sdf_workload()
+    rng = np.random.default_rng(1502)
+    _W["atoms"], _W["q"] = atoms, q
+    _W["q64"] = q.astype(np.float64)
+    _W["gq"] = rng.standard_normal(q.shape[0])
+
+
+def _fd_atom(a):
+    """Central differences of sum_q g_q sdf_q for atom a, and the queries left out (not smooth)."""
+    atoms, q, q64, gq = _W["atoms"], _W["q"], _W["q64"], _W["gq"]
+    c = atoms[:, :3].astype(np.float64)
+    sel = np.flatnonzero(np.linalg.norm(c - c[a], axis=1) < SUBSET)
+    ia = int(np.flatnonzero(sel == a)[0])
+    reach = float(atoms[a, 3]) + 2 * RP + 3.0 + 0.1
+    qi = np.flatnonzero(np.linalg.norm(q64 - c[a], axis=1) <= reach)
+    ql = q[qi]
+    sub = atoms[sel]
+
+    def s(at):
+        return oracle.sdf(oracle.run(at, RP, "full", threads=1), ql, threads=1)[0]
+    s0 = s(sub)
+    kinks = np.zeros(len(qi), bool)
+    diffs = []
+    for comp in range(4):
+        ap = sub.astype(np.float64)
+        am = ap.copy()
+        ap[ia, comp] += H
+        am[ia, comp] -= H
+        ap32, am32 = ap.astype(np.float32), am.astype(np.float32)
+        # the float32 coordinates actually taken (not exactly +-h around the base)
+        up = float(ap32[ia, comp]) - float(sub[ia, comp])
+        dn = float(sub[ia, comp]) - float(am32[ia, comp])
+        sp, sm = s(ap32), s(am32)
+        kinks |= np.abs((sp - s0) / up - (s0 - sm) / dn) > KINK
+        diffs.append((sp - sm) / (up + dn))
+    g = gq[qi]
+    fd = np.array([np.sum(g[~kinks] * d[~kinks]) for d in diffs])
+    return a, fd, qi[kinks], len(qi)
+
+
+def gpu_backward(g, q, gq):
+    import torch
+    m = q.shape[0]
+    ga = torch.zeros((g.atoms.shape[0], 4), dtype=torch.float32, device="cuda")
+    if m:
+        dq = torch.from_numpy(np.ascontiguousarray(q, np.float32)).cuda()
+        dg = torch.from_numpy(np.ascontiguousarray(gq, np.float32)).cuda()
+        g.sdf_backward(dq.data_ptr(), m, dg.data_ptr(), ga.data_ptr())
+    torch.cuda.synchronize()
+    return ga.cpu().numpy().astype(np.float64)
+
+
+def test_sdf_adjoint_20k_atoms_1m_queries():
+    # the oracle's finite differences run in a spawned pool, started before this process uses the GPU
+    ctx = multiprocessing.get_context("spawn")
+    workers = max(1, min(os.cpu_count() or 1, 32))
+    atoms, q = synth.sdf_workload()
+    rng = np.random.default_rng(1502)
+    gq = rng.standard_normal(q.shape[0])
+    # FP64 analytic gradient of the oracle over all queries (input order)
+    o = oracle.run(atoms, RP, "full")
+    _, _, go = oracle.sdf(o, q, gq=gq)
+    want = np.zeros_like(go)
+    want[o["perm"]] = go
+    # atoms with accessible surface: a visible circle in the oracle's build
+    vis = np.zeros(atoms.shape[0], bool)
+    slot_atom = np.repeat(np.arange(atoms.shape[0]), np.diff(o["noff"]).astype(np.int64))
+    vis[o["perm"][np.unique(slot_atom[o["status"] != 0])]] = True
+    pick = rng.choice(np.flatnonzero(vis), 512, replace=False)
+    with ctx.Pool(workers, initializer=_init_worker) as pool:
+        pending = pool.map_async(_fd_atom, [int(a) for a in pick], chunksize=4)
+        with SesBuild(atoms, RP, "full") as g:
+            g.build()
+            full = gpu_backward(g, q, gq)
+            assert np.abs(full - want).max() <= 1e-3 * np.abs(want).max()
+            per_atom = np.linalg.norm(full - want, axis=1) / np.maximum(np.linalg.norm(want, axis=1), 1e-12)
+            live = np.linalg.norm(want, axis=1) > 0
+            assert np.quantile(per_atom[live], 0.99) <= 1e-3
+            results = pending.get(timeout=1800)
+            worst, left_out, queries = 0.0, 0, 0
+            for a, fd, kq, nq in results:
+                got = full[a] - (gpu_backward(g, q[kq], gq[kq])[a] if len(kq) else 0.0)
+                err = np.linalg.norm(got - fd)
+                norm = np.linalg.norm(fd)
+                assert err <= 1e-3 * norm + 1e-9, (a, got, fd, len(kq))
+                if norm > 0:
+                    worst = max(worst, err / norm)
+                left_out += len(kq)
+                queries += nq
+    print(f"sdf adjoint vs FP64 central differences: 512 atoms, worst relative error {worst:.2e}, "
+          f"{left_out} of {queries} query terms not differentiable within +-h left out")
+    assert left_out <= 0.01 * queries
