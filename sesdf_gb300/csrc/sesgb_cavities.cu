@@ -12,10 +12,12 @@
 //                  per 32-voxel word. The voxel test is ((dx^2 + dy^2) + dz^2) < R^2 in double
 //                  precision, dx = (lo_x + ix h) - c_x, evaluated exactly for the voxels next to the
 //                  run's ends; voxels two or more inside the ends are well inside the sphere.
-//   k_cav_init     label[v] = v for an accessible voxel, -1 otherwise
-//   k_cav_union    every accessible voxel with its +x, +y, +z accessible neighbours: lock-free union-find
-//                  in which a root is only ever linked under a smaller one (atomicMin), so the root of a
-//                  component ends as its smallest voxel index
+//   k_cav_init     label[v] = the first voxel of v's run of accessible voxels along z (-1 when v is
+//                  not accessible): every run starts as a tree of depth one
+//   k_cav_union    runs joined across y and x: lock-free union-find (one merge per pair of overlapping
+//                  runs, at the first voxel of their overlap) in which a root is only ever linked under a
+//                  smaller one (atomicMin), with path halving in every find, so the root of a component
+//                  ends as its smallest voxel index
 //   k_cav_flatten  label[v] = root of v; roots are collected
 //   k_cav_relabel  label[v] = 1 + rank of its root among the sorted roots: components numbered in the
 //                  order of their first voxel in index order (the numbering of a raster-order labelling);
@@ -160,20 +162,48 @@ namespace sesgb
 
         __device__ __forceinline__ bool cav_free( const uint32_t * bits, uint64_t v ) { return !( ( bits[ v >> 5 ] >> ( v & 31u ) ) & 1u ); }
 
-        __global__ void k_cav_init( const uint32_t * bits, uint64_t V, int32_t * L )
+        // largest occupied bit index in [lo, v), or lo - 1 when there is none
+        __device__ __forceinline__ int64_t cav_last_occupied( const uint32_t * bits, uint64_t lo, uint64_t v )
         {
-            for ( uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < V; v += (uint64_t)gridDim.x * blockDim.x )
-                L[ v ] = cav_free( bits, v ) ? (int32_t)v : -1;
+            int64_t w = (int64_t)( v >> 5 );
+            uint32_t x = bits[ w ] & ( ( v & 31u ) ? ( 0xffffffffu >> ( 32u - ( v & 31u ) ) ) : 0u );
+            const int64_t wlo = (int64_t)( lo >> 5 );
+            while ( !x && w > wlo )
+                x = bits[ --w ];
+            if ( !x )
+                return (int64_t)lo - 1;
+            const int64_t at = w * 32 + ( 31 - __clz( x ) );
+            return at >= (int64_t)lo ? at : (int64_t)lo - 1;
         }
 
-        __device__ __forceinline__ int32_t cav_find( const int32_t * L, int32_t v, uint32_t * err )
+        __global__ void k_cav_init( const uint32_t * bits, CavGrid g, int32_t * L )
+        {
+            const uint64_t nz = g.dims[ 2 ], V = nz * g.dims[ 1 ] * g.dims[ 0 ];
+            for ( uint64_t v = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; v < V; v += (uint64_t)gridDim.x * blockDim.x )
+            {
+                if ( !cav_free( bits, v ) )
+                {
+                    L[ v ] = -1;
+                    continue;
+                }
+                const uint64_t row = v - v % nz;
+                L[ v ]             = (int32_t)( cav_last_occupied( bits, row, v ) + 1 );
+            }
+        }
+
+        // root of v, halving the path on the way (labels only decrease: every write keeps an ancestor)
+        __device__ __forceinline__ int32_t cav_find( int32_t * L, int32_t v, uint32_t * err )
         {
             for ( uint32_t s = 0; s < kCavMaxFind; s++ )
             {
-                const int32_t p = L[ v ];
+                const int32_t p = __ldcg( L + v );
                 if ( p == v )
                     return v;
-                v = p;
+                const int32_t gp = __ldcg( L + p );
+                if ( gp == p )
+                    return p;
+                atomicMin( L + v, gp );
+                v = gp;
             }
             atomicOr( err, 1u );
             return v;
@@ -210,11 +240,11 @@ namespace sesgb
                 if ( !cav_free( bits, v ) )
                     continue;
                 const uint64_t iz = v % nz, iy = ( v / nz ) % g.dims[ 1 ], ix = v / nyz;
-                if ( iz + 1 < nz && cav_free( bits, v + 1 ) )
-                    cav_merge( L, (int32_t)v, (int32_t)( v + 1 ), err );
-                if ( iy + 1 < g.dims[ 1 ] && cav_free( bits, v + nz ) )
+                const bool     prev = iz > 0 && cav_free( bits, v - 1 );
+                // a neighbouring run is joined once, where its overlap with v's run begins
+                if ( iy + 1 < g.dims[ 1 ] && cav_free( bits, v + nz ) && !( prev && cav_free( bits, v + nz - 1 ) ) )
                     cav_merge( L, (int32_t)v, (int32_t)( v + nz ), err );
-                if ( ix + 1 < g.dims[ 0 ] && cav_free( bits, v + nyz ) )
+                if ( ix + 1 < g.dims[ 0 ] && cav_free( bits, v + nyz ) && !( prev && cav_free( bits, v + nyz - 1 ) ) )
                     cav_merge( L, (int32_t)v, (int32_t)( v + nyz ), err );
             }
         }
@@ -326,7 +356,7 @@ namespace sesgb
         cudaMemsetAsync( scalars, 0, sizeof( uint32_t ) * 2, s );
         if ( b.n )
             k_cav_raster<<<cav_blocks( (uint64_t)b.n * 32, 256 ), 256, 0, s>>>( b.atoms, b.n, g, bits );
-        k_cav_init<<<cav_blocks( V, 256 ), 256, 0, s>>>( bits, V, labels );
+        k_cav_init<<<cav_blocks( V, 256 ), 256, 0, s>>>( bits, g, labels );
         k_cav_union<<<cav_blocks( V, 256 ), 256, 0, s>>>( bits, g, labels, scalars + 1 );
         k_cav_flatten<<<cav_blocks( V, 256 ), 256, 0, s>>>( V, labels, roots, rootCap, scalars, scalars + 1 );
         count_launches( b.n ? 4 : 3 );
