@@ -309,6 +309,7 @@ def sdf_extra(flush):
         res[f"{name}_queries_per_s"] = round(m / (float(np.median(ms)) * 1e-3), 1)
     res["queries"] = int(m)
     res["atoms"] = int(atoms.shape[0])
+    res["probes"] = int(g.counts()["probes"])
     res["band_A"] = 3.0
     # SES area of the primitives (sesgb_ses_area synchronises: host wall clock around the call)
     # and its adjoint (device events)
@@ -337,6 +338,38 @@ def sdf_extra(flush):
         torch.cuda.synchronize()
         ms.append(t0.elapsed_time(t1))
     res["area_backward_ms"] = round(float(np.median(ms)), 4)
+    # headless image: 512 x 512 rays sphere-traced on the device in one launch (sesgb_render)
+    from sesdf_gb300 import render
+    w = h = 512
+    eye, centre, up, t_near, t_far = render.framing(atoms, RP)
+    f, r, u = render.camera_basis(eye, centre, up)
+    cam = dict(eye=eye, forward=f, right=r, up=u, tan_half_fov=float(np.tan(np.radians(20.0))), t_near=float(t_near),
+               t_far=float(t_far), eps=1e-3, normal_step=1e-2, width=w, height=h, max_steps=256)
+    depth = torch.empty(w * h, dtype=torch.float32, device="cuda")
+    nrm = torch.empty(3 * w * h, dtype=torch.float32, device="cuda")
+    for _ in range(2):
+        g.render(cam, depth.data_ptr(), nrm.data_ptr(), stream.cuda_stream)
+    ms = []
+    for _ in range(5):
+        t0, t1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0.record(stream)
+        g.render(cam, depth.data_ptr(), nrm.data_ptr(), stream.cuda_stream)
+        t1.record(stream)
+        torch.cuda.synchronize()
+        ms.append(t0.elapsed_time(t1))
+    res["render_512x512_ms"] = round(float(np.median(ms)), 4)
+    res["render_hit_pixels"] = int(torch.isfinite(depth).sum().item())
+    # exterior and cavities on a 0.5 A voxel grid (sesgb_cavities synchronises: host wall clock)
+    g.cavities(0.5)
+    ms = []
+    for _ in range(5):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        info = g.cavities(0.5)
+        ms.append((time.perf_counter() - t0) * 1e3)
+    res["cavities_0.5A_ms"] = round(float(np.median(ms)), 4)
+    res["cavities_0.5A"] = {"voxels": int(np.prod(info["dims"])), "components": info["components"],
+                            "exterior": info["exterior"], "cavities": info["cavities"]}
     g.close()
     return res
 
@@ -349,7 +382,7 @@ def profiled(kernel: str, workload: str = "assembly100k") -> dict:
     out = {}
     keys = {"dram_bytes_per_launch:": "traffic", "issue active %": "issue_active", "ALU pipe %": "alu_pipe",
             "FMA pipe %": "fma_pipe", "threads per instruction": "threads_per_instruction",
-            "warp instructions": "warp_instructions"}
+            "warp instructions": "warp_instructions", "duration (one launch, cold)": "duration_us"}
     try:
         with open(path) as f:
             for line in f:
@@ -488,6 +521,23 @@ def run_ours(args, rank, world, local):
         del shell
         extra.update(batch_extras(args, flush, rank, world))
         extra["sdf_20k_1m"] = sdf_extra(flush)
+        sx = extra["sdf_20k_1m"]
+        # issue-rate rooflines of the on-demand kernels (their ncu summaries: profiles/<kernel>_<workload>.txt);
+        # the SDF call's time is k_sdf's to within its sort of the query keys, the area call's is the sum of
+        # k_area_atoms and k_area_probes (split by the launch list's shares)
+        n20, m = sx["atoms"], sx["queries"]
+        extra["rooflines"] = {
+            "k_sdf": issue_roofline("k_sdf", sx["forward_ms"], clocks.get("sm_mhz"), 16.0 * m + 16.0 * n20,
+                                    "globule20k_1m"),
+        }
+        prof_a, prof_p = profiled("k_area_atoms", "globule20k"), profiled("k_area_probes", "globule20k")
+        if prof_a.get("duration_us") and prof_p.get("duration_us"):
+            share = prof_a["duration_us"] / (prof_a["duration_us"] + prof_p["duration_us"])
+            extra["rooflines"]["k_area_atoms"] = issue_roofline("k_area_atoms", sx["area_ms"] * share, clocks.get("sm_mhz"),
+                                                                16.0 * n20, "globule20k")
+            extra["rooflines"]["k_area_probes"] = issue_roofline("k_area_probes", sx["area_ms"] * (1 - share),
+                                                                 clocks.get("sm_mhz"), 64.0 * sx.get("probes", 0),
+                                                                 "globule20k")
 
     roof = roofline(stages, counts, n, clocks.get("sm_mhz"))
     line = {
@@ -522,6 +572,45 @@ REF_D2H_BYTES_FULL = 5 * 4 + 3 * 8
 # exterior build (sesdf/src/ssesdf/ssesdf.cu:133-187): one 4-byte counter read, the results of four
 # thrust::count_if calls and one thrust::copy_if
 REF_D2H_BYTES_EXTERIOR = 4 + 5 * 8
+
+
+def run_profile_case(args):
+    """One on-demand workload of the 20,000-atom globule, args.steps times after args.warmup, for
+    profiler runs (no JSON line): sdf (forward and adjoint at 200,000 of the 1M queries), area
+    (SES area and its adjoint), render (512 x 512 image), cavities (0.5 A voxels)."""
+    import torch
+    from sesdf_gb300 import SesBuild, render, synth
+    atoms, q = synth.sdf_workload()
+    q = np.ascontiguousarray(q[:200_000])
+    stream = torch.cuda.current_stream()
+    g = SesBuild(atoms, RP, "full")
+    g.build()
+    m = q.shape[0]
+    dq = torch.from_numpy(q).cuda()
+    out = torch.empty(m, dtype=torch.float32, device="cuda")
+    gs = torch.ones(m, dtype=torch.float32, device="cuda")
+    ga = torch.empty((atoms.shape[0], 4), dtype=torch.float32, device="cuda")
+    depth = torch.empty(512 * 512, dtype=torch.float32, device="cuda")
+    eye, centre, up, t_near, t_far = render.framing(atoms, RP)
+    f, r, u = render.camera_basis(eye, centre, up)
+    cam = dict(eye=eye, forward=f, right=r, up=u, tan_half_fov=float(np.tan(np.radians(20.0))), t_near=float(t_near),
+               t_far=float(t_far), eps=1e-3, normal_step=1e-2, width=512, height=512, max_steps=256)
+
+    def once():
+        if args.profile_case == "sdf":
+            g.sdf(dq.data_ptr(), m, out.data_ptr(), None, stream.cuda_stream)
+            g.sdf_backward(dq.data_ptr(), m, gs.data_ptr(), ga.data_ptr(), stream.cuda_stream)
+        elif args.profile_case == "area":
+            g.ses_area(None, stream.cuda_stream)
+            g.ses_area_backward(ga.data_ptr(), (1.0, 1.0, 1.0), stream.cuda_stream)
+        elif args.profile_case == "render":
+            g.render(cam, depth.data_ptr(), None, stream.cuda_stream)
+        elif args.profile_case == "cavities":
+            g.cavities(0.5)
+    for _ in range(args.warmup + args.steps):
+        once()
+    torch.cuda.synchronize()
+    g.close()
 
 
 def run_reference(args, rank, world, local):
@@ -619,6 +708,8 @@ def main():
     ap.add_argument("--impl", choices=["ours", "reference"], default="ours")
     ap.add_argument("--no-extras", action="store_true")
     ap.add_argument("--no-error-report", action="store_true", help="skip the FP64 error report of the 1M builds")
+    ap.add_argument("--profile-case", choices=["sdf", "area", "render", "cavities"], default=None,
+                    help="run one on-demand workload of the 20k-atom globule for a profiler (no JSON line)")
     ap.add_argument("--kernels-only", action="store_true",
                     help="only the device-timed builds (for profiler runs): no e2e, extras, stage profile or CPU baseline")
     args = ap.parse_args()
@@ -632,7 +723,9 @@ def main():
         from oracle import refharness
         refharness.build_cubin()
     barrier(world)
-    if args.impl == "reference":
+    if args.profile_case:
+        run_profile_case(args)
+    elif args.impl == "reference":
         run_reference(args, rank, world, local)
     else:
         run_ours(args, rank, world, local)

@@ -3098,7 +3098,7 @@ namespace sesgb
         }
 
         // d sdf / d (c, r) of the active primitive, scaled by gs, into g (sorted order)
-        __device__ void sdf_gradient( const Build & b, const SdfHit & h, float3 x, float gs, float * g )
+        __device__ __noinline__ void sdf_gradient( const Build & b, const SdfHit & h, float3 x, float gs, float * g )
         {
             if ( h.kind == kSdfAtom || h.kind == kSdfSphere )
             {
@@ -3117,33 +3117,40 @@ namespace sesgb
             }
             if ( h.kind != kSdfCircle && h.kind != kSdfProbe )
                 return;
-            const float3 p = h.q;
-            const float  dx = x.x - p.x, dy = x.y - p.y, dz = x.z - p.z;
-            const float  D  = sqrtf( dx * dx + dy * dy + dz * dz );
-            if ( !( D > 0.f ) )
+            // The multipliers of the constraints |p - c_k|^2 = R_k^2 that hold the point p: a 2x2
+            // (circle) or 3x3 (probe) system that is nearly singular when the constraint normals
+            // are nearly parallel (two circle centres nearly aligned with p, a probe near the plane
+            // of its three centres), where float32 would show in the gradient. Solved in double
+            // precision from the float32 values (their differences are exact in double); one lane
+            // per query, so the FP64 pipe's rate does not matter.
+            const float3 pf = h.q;
+            const d3     p  = D3( (double)pf.x, (double)pf.y, (double)pf.z );
+            const d3     dv = D3( (double)x.x - p.x, (double)x.y - p.y, (double)x.z - p.z );
+            const double D  = sqrt( dv.x * dv.x + dv.y * dv.y + dv.z * dv.z );
+            if ( !( D > 0.0 ) )
                 return;
-            const float3 u = make_float3( dx / D, dy / D, dz / D );
-            const int    m = h.kind == kSdfCircle ? 2 : 3;
-            const int    ids[ 3 ] = { h.a, h.b, h.c };
-            float3       a[ 3 ];
-            float        R[ 3 ];
+            const d3  u = D3( dv.x / D, dv.y / D, dv.z / D );
+            const int m = h.kind == kSdfCircle ? 2 : 3;
+            const int ids[ 3 ] = { h.a, h.b, h.c };
+            d3        a[ 3 ];
+            double    R[ 3 ];
             for ( int k = 0; k < m; k++ )
             {
                 const float4 c = b.atoms[ ids[ k ] ];
-                a[ k ]         = make_float3( 2.f * ( p.x - c.x ), 2.f * ( p.y - c.y ), 2.f * ( p.z - c.z ) );
-                R[ k ]         = c.w + b.rp;
+                a[ k ]         = D3( 2.0 * ( p.x - (double)c.x ), 2.0 * ( p.y - (double)c.y ), 2.0 * ( p.z - (double)c.z ) );
+                R[ k ]         = (double)c.w + (double)b.rp;
             }
             // multipliers w: sum_k w_k a_k = u (least squares for the circle, exact for the probe)
-            float w[ 3 ] = { 0.f, 0.f, 0.f };
+            double w[ 3 ] = { 0.0, 0.0, 0.0 };
             if ( m == 2 )
             {
-                const float g00 = a[ 0 ].x * a[ 0 ].x + a[ 0 ].y * a[ 0 ].y + a[ 0 ].z * a[ 0 ].z;
-                const float g01 = a[ 0 ].x * a[ 1 ].x + a[ 0 ].y * a[ 1 ].y + a[ 0 ].z * a[ 1 ].z;
-                const float g11 = a[ 1 ].x * a[ 1 ].x + a[ 1 ].y * a[ 1 ].y + a[ 1 ].z * a[ 1 ].z;
-                const float r0  = a[ 0 ].x * u.x + a[ 0 ].y * u.y + a[ 0 ].z * u.z;
-                const float r1  = a[ 1 ].x * u.x + a[ 1 ].y * u.y + a[ 1 ].z * u.z;
-                const float det = g00 * g11 - g01 * g01;
-                if ( !( fabsf( det ) > 0.f ) )
+                const double g00 = a[ 0 ].x * a[ 0 ].x + a[ 0 ].y * a[ 0 ].y + a[ 0 ].z * a[ 0 ].z;
+                const double g01 = a[ 0 ].x * a[ 1 ].x + a[ 0 ].y * a[ 1 ].y + a[ 0 ].z * a[ 1 ].z;
+                const double g11 = a[ 1 ].x * a[ 1 ].x + a[ 1 ].y * a[ 1 ].y + a[ 1 ].z * a[ 1 ].z;
+                const double r0  = a[ 0 ].x * u.x + a[ 0 ].y * u.y + a[ 0 ].z * u.z;
+                const double r1  = a[ 1 ].x * u.x + a[ 1 ].y * u.y + a[ 1 ].z * u.z;
+                const double det = g00 * g11 - g01 * g01;
+                if ( !( fabs( det ) > 0.0 ) )
                     return;
                 w[ 0 ] = ( r0 * g11 - r1 * g01 ) / det;
                 w[ 1 ] = ( r1 * g00 - r0 * g01 ) / det;
@@ -3151,22 +3158,18 @@ namespace sesgb
             else
             {
                 // columns a_0, a_1, a_2: Cramer's rule
-                const float3 c01 = make_float3( a[ 1 ].y * a[ 2 ].z - a[ 1 ].z * a[ 2 ].y, a[ 1 ].z * a[ 2 ].x - a[ 1 ].x * a[ 2 ].z,
-                                                a[ 1 ].x * a[ 2 ].y - a[ 1 ].y * a[ 2 ].x );
-                const float det = a[ 0 ].x * c01.x + a[ 0 ].y * c01.y + a[ 0 ].z * c01.z;
-                if ( !( fabsf( det ) > 0.f ) )
+                const d3     c12 = dcross( a[ 1 ], a[ 2 ] );
+                const double det = ddot( a[ 0 ], c12 );
+                if ( !( fabs( det ) > 0.0 ) )
                     return;
-                const float3 cu1 = make_float3( u.y * a[ 2 ].z - u.z * a[ 2 ].y, u.z * a[ 2 ].x - u.x * a[ 2 ].z, u.x * a[ 2 ].y - u.y * a[ 2 ].x );
-                const float3 c0v = make_float3( a[ 0 ].y * a[ 1 ].z - a[ 0 ].z * a[ 1 ].y, a[ 0 ].z * a[ 1 ].x - a[ 0 ].x * a[ 1 ].z,
-                                                a[ 0 ].x * a[ 1 ].y - a[ 0 ].y * a[ 1 ].x );
-                w[ 0 ] = ( u.x * c01.x + u.y * c01.y + u.z * c01.z ) / det;                 // det[u, a1, a2]
-                w[ 1 ] = ( a[ 0 ].x * cu1.x + a[ 0 ].y * cu1.y + a[ 0 ].z * cu1.z ) / det;  // det[a0, u, a2]
-                w[ 2 ] = ( c0v.x * u.x + c0v.y * u.y + c0v.z * u.z ) / det;                 // det[a0, a1, u]
+                w[ 0 ] = ddot( u, c12 ) / det;                    // det[u, a1, a2]
+                w[ 1 ] = ddot( a[ 0 ], dcross( u, a[ 2 ] ) ) / det; // det[a0, u, a2]
+                w[ 2 ] = ddot( dcross( a[ 0 ], a[ 1 ] ), u ) / det; // det[a0, a1, u]
             }
             // sdf = rp - D: d sdf / d c_k = w_k a_k, d sdf / d r_k = 2 w_k R_k
             for ( int k = 0; k < m; k++ )
-                add_grad( g, (uint32_t)ids[ k ], gs * w[ k ] * a[ k ].x, gs * w[ k ] * a[ k ].y, gs * w[ k ] * a[ k ].z,
-                          gs * 2.f * w[ k ] * R[ k ] );
+                add_grad( g, (uint32_t)ids[ k ], (float)( gs * w[ k ] * a[ k ].x ), (float)( gs * w[ k ] * a[ k ].y ),
+                          (float)( gs * w[ k ] * a[ k ].z ), (float)( gs * 2.0 * w[ k ] * R[ k ] ) );
         }
 
         // grid cell of each query (sort key) and its index

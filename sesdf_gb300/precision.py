@@ -12,7 +12,9 @@ the build stores and reports how far the stored float32 values are from it:
 * convex sectors: the axis c_ij (unit vector from i to j) and the half angle
   acos(c_ij . (x - c_i) / R_i) of each visible circle, x the circle point along the
   reference's orthogonal vector (operations.inl:175-228, math.cuh:32-38); the angle
-  is compared through its cosine, which is well conditioned next to 0 and pi.
+  is compared through its cosine, which is well conditioned next to 0 and pi;
+* exterior tori: circle centre and radius, axis, visibility sphere
+  (sesdf/src/ssesdf/operations.cu:246-285).
 
 Together with the per-predicate counts of double-precision decisions the build
 reports (`fp64_decisions`), this is the error statement of one build.
@@ -90,12 +92,59 @@ def sector_error(atoms: np.ndarray, nbr_ids: np.ndarray, nbr_count: np.ndarray, 
             "cos_max_err": float(np.abs(np.cos(s[:, 3]) - cos).max())}
 
 
+def tori_error(atoms: np.ndarray, nbr_ids: np.ndarray, nbr_count: np.ndarray, status: np.ndarray,
+               tori_pos: np.ndarray, tori_axis: np.ndarray, tori_vs: np.ndarray, rp: float) -> dict:
+    """Max error of the stored exterior tori (fillCircles, sesdf/src/ssesdf/operations.cu:246-285: circle
+    centre and radius, axis and probe radius, visibility sphere) against FP64, over the circles with
+    status 2 in slot order; tori whose axis is parallel to z (no reference frame, counted by the build as
+    degenerate) are left out."""
+    a = np.asarray(atoms, np.float64)
+    n, cap = nbr_ids.shape
+    live = np.arange(cap)[None, :] < np.asarray(nbr_count)[:, None]
+    sel = live & (status == 2)
+    i = np.nonzero(sel)[0].astype(np.int64)
+    j = nbr_ids[sel].astype(np.int64)
+    if len(i) == 0:
+        return {"tori": 0, "max_err": 0.0, "degenerate": 0}
+    rpd = float(np.float32(rp))
+    ci, cj, ri = a[i, :3], a[j, :3], a[i, 3]
+    Ri, Rj = ri + rpd, a[j, 3] + rpd
+    d = ci - cj
+    dd = np.einsum("ij,ij->i", d, d)
+    t = (Ri * Ri - Rj * Rj + dd) / (2 * dd)
+    tc = ci + (cj - ci) * t[:, None]
+    radius = np.sqrt(np.maximum(Ri * Ri - np.einsum("ij,ij->i", ci - tc, ci - tc), 0.0))
+
+    def nrm(v):
+        return v / np.linalg.norm(v, axis=1, keepdims=True)
+    with np.errstate(invalid="ignore", divide="ignore"):
+        ta = nrm(tc - ci)
+        cz = np.cross(ta, np.array([0.0, 0.0, 1.0]))
+        degenerate = np.einsum("ij,ij->i", cz, cz) < 1e-12
+        ortho = nrm(cz)
+        P = tc + ortho * radius[:, None]
+        X = nrm(P - ci) * ri[:, None]
+        lpi = np.linalg.norm(P - ci, axis=1)
+        lpj = np.linalg.norm(P - cj, axis=1)
+        C = (cj - ci) * (lpi / (lpj + lpi))[:, None]
+        dist = np.linalg.norm(X - C, axis=1)
+        C = C + ci - tc
+    want = np.concatenate([tc, radius[:, None], ta, np.full((len(i), 1), rpd), C, dist[:, None]], axis=1)
+    got = np.concatenate([tori_pos, tori_axis, tori_vs], axis=1).astype(np.float64)
+    ok = ~degenerate & np.isfinite(want).all(axis=1)
+    err = np.abs(got[ok] - want[ok])
+    return {"tori": int(len(i)), "max_err": float(err.max()) if err.size else 0.0, "degenerate": int(degenerate.sum())}
+
+
 def error_report(out: dict, rp: float, mode: str) -> dict:
     """Error of one build against FP64 from SesBuild.fetch(analysis=True) output, with the build's
     double-precision decision counts (the degeneracy band) per predicate."""
     rep = {"probes": probe_error(out["atoms"], out["probe_ids"], out["probe_pos"], rp)}
     if mode == "full":
         rep["sectors"] = sector_error(out["atoms"], out["nbr_ids"], out["nbr_count"], out["status"], out["sectors"], rp)
+    else:
+        rep["tori"] = tori_error(out["atoms"], out["nbr_ids"], out["nbr_count"], out["status"], out["tori_pos"],
+                                 out["tori_axis"], out["tori_vs"], rp)
     rep["fp64_decisions"] = dict(zip(FP64_PREDICATES, out["counts"]["fp64_decisions"]))
     rep["band_cases"] = int(sum(out["counts"]["fp64_decisions"]))
     return rep

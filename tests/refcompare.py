@@ -20,6 +20,7 @@ from __future__ import annotations
 import numpy as np
 
 import canon
+from sesdf_gb300 import precision
 
 EPS32 = 2.0 ** -23
 WIDE = 2.0 ** -10
@@ -348,20 +349,29 @@ def compare_sorted(ref: dict, gpu: dict, rp: float, mode: str) -> dict:
     ci_, cj_ = common // n, common % n
     keep = ci_ < cj_ if ext else np.ones(len(common), bool)
     bad = np.nonzero(keep & (str_ != stg))[0]
+    # a circle's status depends on every neighbour of its atom: an atom whose neighbour list differs
+    # between the two sides (a neighbour decided inside the band) explains all of its circles
+    bad_atoms = {x for pr in bad_pairs for x in pr}
     # exterior statuses are read after the probes promoted their circles to status 2, so there a
     # circle is a cause for its probes only when its own visibility margin is inside the band
     tainted = set()
     out_of_band = []
+    cases = []
     for q in bad.tolist():
         i, j = int(ci_[q]), int(cj_[q])
         c = (min(i, j), max(i, j))
-        inband = status_margin(pos, rad, i, j, nbrs_of(i), rpd) < WIDE
+        margin = 0.0 if i in bad_atoms else status_margin(pos, rad, i, j, nbrs_of(i), rpd)
+        inband = margin < WIDE
         if inband or not ext:
             tainted.add(c)
         if not inband:
             out_of_band.append(c)
+            if len(cases) < 20:
+                cases.append({"i": int(gpu["perm"][i]), "j": int(gpu["perm"][j]), "ref": int(str_[q]), "gpu": int(stg[q]),
+                              "margin": float(margin)})
     rep["status_mismatch"] = int(len(bad))
     rep["status_unexplained"] = len(out_of_band)
+    rep["status_cases"] = cases
 
     # probes
     pkr = _probe_keys_sorted(atoms, ref["probe_ids"], ref["probe_pos"], n)
@@ -395,6 +405,7 @@ def compare_sorted(ref: dict, gpu: dict, rp: float, mode: str) -> dict:
     if ext:
         # a probe found on one side only changes the statuses of its three circles
         rep["status_unexplained"] = len([c for c in out_of_band if c not in bad_probe_circles and c not in bad_pairs])
+    rep["ref_probe_vs_fp64"] = precision.probe_error(atoms, ref["probe_ids"], ref["probe_pos"], rp)
     _, qr, qg = np.intersect1d(pkr, pkg, return_indices=True)
     if len(qr):
         err = np.abs(ref["probe_pos"][qr, :3].astype(np.float64) - gpu["probe_pos"][qg, :3].astype(np.float64))
@@ -477,5 +488,5 @@ def compare_sorted(ref: dict, gpu: dict, rp: float, mode: str) -> dict:
         rep["tori_unexplained"] = int(sum(1 for q in np.nonzero(only)[0].tolist()
                                           if not circle_tainted(int(ci_[q]), int(cj_[q]))))
     rep["unexplained"] = int(sum(v for k, v in rep.items() if k.endswith("_unexplained")))
-    rep["band_cases"] = int(sum(v for k, v in rep.items() if k.endswith("_mismatch")))
+    rep["band_cases"] = int(sum(v for k, v in rep.items() if k.endswith("_mismatch") and k != "perm_mismatch"))
     return rep
