@@ -62,3 +62,11 @@ def segment_set(perm, segments, keys) -> set:
 
 def pair_set(perm, pairs) -> set:
     return {frozenset((int(perm[p[0]]), int(perm[p[1]]))) for p in pairs}
+
+
+def written_probe_nbrs(probe_nbrs, probe_ids, q_count) -> np.ndarray:
+    """The written entries of the singular probes' 32-entry neighbour blocks (probe q's first
+    probe_ids[q, 3] entries, q < q_count), concatenated; the rest of a block is never written."""
+    blocks = np.asarray(probe_nbrs, np.float32).reshape(-1, 32, 4)
+    rows = [blocks[q, :max(0, min(32, int(probe_ids[q, 3])))] for q in range(int(q_count))]
+    return np.concatenate(rows) if rows else np.zeros((0, 4), np.float32)

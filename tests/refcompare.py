@@ -11,6 +11,7 @@ its FP64 margin lies inside it, together with the cases that depend on it
 Band widths (|FP64 margin| below which a disagreement is explained):
   neighbour   |d^2 - R^2 - 1e-4|            < 64 eps32 (d^2 + R^2)
   visibility  |complete - R_k^2 - 1e-4|      < 2^-10 (complete + R_k^2)     (float32 sqrt(1-cos^2) amplifies)
+  circle      |R_i^2 - |c_i - c|^2|          < 2^-10 R_i^2                  (tangent SAS spheres: radius^2 ~ 0)
   occlusion   ||c_l - x|^2 - R_l^2|          < 2^-10 (|c_l - x|^2 + R_l^2)  (float32 triplet solve)
   singular    |d^2 - rp^2 + 1e-4|            < 2^-10 (d^2 + rp^2)
   probe pair  |t| (x1 = x2)                  < 2^-10 R_i^2
@@ -41,7 +42,16 @@ def circle_geometry(ci, ri, cj, rj, rp):
 
 
 def status_margin(pos, rad, i, j, nbrs, rp):
-    """Smallest |margin| over k of the two visibility predicates of circle (i, j)."""
+    """Smallest |margin| over k of the two visibility predicates of circle (i, j); 0 when the circle
+    itself hangs on the band (SAS spheres of i and j tangent: its radius is the root of a difference
+    of nearly equal numbers, NaN on one side and a tiny circle on the other)."""
+    R1, R2 = rad[i] + rp, rad[j] + rp
+    dij = np.dot(pos[i] - pos[j], pos[i] - pos[j])
+    t = (R1 * R1 - R2 * R2 + dij) / (2 * dij)
+    cc = pos[i] + (pos[j] - pos[i]) * t
+    r2 = R1 * R1 - np.dot(pos[i] - cc, pos[i] - cc)
+    if abs(r2) < WIDE * R1 * R1:
+        return 0.0
     c, n, r = circle_geometry(pos[i], rad[i], pos[j], rad[j], rp)
     best = np.inf
     for k in nbrs:

@@ -10,6 +10,7 @@ import subprocess
 import numpy as np
 import pytest
 
+import canon
 from sesdf_gb300 import SesBuild, _build, synth
 
 pytestmark = pytest.mark.gpu
@@ -179,7 +180,9 @@ def test_dropin_classes_match_binding(program, tmp_path, mode):
     assert np.array_equal(read(out, "atoms", np.float32, 4), want["atoms"])
     assert np.array_equal(read(out, "probe_pos", np.float32, 4), want["probe_pos"])
     assert np.array_equal(read(out, "probe_ids", np.int32, 4), want["probe_ids"])
-    assert np.array_equal(read(out, "probe_nbrs", np.float32, 4), want["probe_nbrs"])
+    Q = c["singular_probes"]
+    assert np.array_equal(canon.written_probe_nbrs(read(out, "probe_nbrs", np.float32, 4), want["probe_ids"], Q),
+                          canon.written_probe_nbrs(want["probe_nbrs"], want["probe_ids"], Q))
     assert np.array_equal(read(out, "indices", np.uint32), want["perm"])
     assert np.array_equal(read(out, "d_indices", np.uint32), want["perm"])
     assert np.array_equal(read(out, "d_nbr_count", np.uint32)[: atoms.shape[0]], want["nbr_count"])
