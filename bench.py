@@ -35,7 +35,7 @@ sys.path.insert(0, ROOT)
 METRIC = "SES build ms & atoms/s at 100k/1M atoms; batched+adjoint vs plain, ≤1e-4 Å"
 RP = 1.4
 L2_FLUSH_BYTES = 256 << 20
-COUNTS_BYTES = 128  # sesgb DeviceCounts read back per build
+COUNTS_BYTES = 132  # sesgb DeviceCounts read back per build
 FP32_LANES = 152 * 128  # SMs x FP32 lanes of a GB300
 
 
@@ -224,11 +224,13 @@ def time_plain_loop(mols, mode, repeats, flush):
     return out
 
 
-def time_batched(mols, mode, repeats, flush, cap, graph):
+def time_batched(mols, mode, repeats, flush, cap, graph, tuning=None):
     import torch
     from sesdf_gb300 import SesBatch
     stream = torch.cuda.current_stream()
     b = SesBatch(mols, RP, mode, max_neighbor_per_atom=cap, graph=graph)
+    if tuning:
+        b.set_tuning(**tuning)
     d = torch.from_numpy(b.atoms).cuda()
     for _ in range(2):
         b.build_async(d.data_ptr(), stream.cuda_stream)
@@ -263,7 +265,7 @@ def batch_extras(args, flush, rank=0, world=1):
         a, b = split_by_atoms([m.shape[0] for m in all_mols], world)[rank]
         mols = all_mols[a:b] if b > a else all_mols[:1]
         tuned = tune_batch(mols, RP, "full")
-        bm, c = time_batched(mols, "full", 5, flush, tuned["max_neighbor_per_atom"], tuned["graph"])
+        bm, c = time_batched(mols, "full", 5, flush, tuned["max_neighbor_per_atom"], tuned["graph"], tuned["tuning"])
         pm = time_plain_loop(mols, "full", 3, flush)
         bmed = max_over_ranks(float(np.median(bm)), world)
         pmed = max_over_ranks(float(np.median(pm)), world)
@@ -271,7 +273,7 @@ def batch_extras(args, flush, rank=0, world=1):
         res[name] = {"molecules": len(all_mols), "atoms": atoms, "batched_ms": round(bmed, 3),
                      "plain_loop_ms": round(pmed, 3), "speedup": round(pmed / bmed, 2),
                      "batched_atoms_per_s": round(atoms / (bmed * 1e-3), 1),
-                     "tuned": {k: tuned[k] for k in ("max_neighbor_per_atom", "graph", "max_neighbors")},
+                     "tuned": {k: tuned[k] for k in ("max_neighbor_per_atom", "graph", "max_neighbors", "tuning")},
                      "probes_rank0": c["probes"], "split": "molecules by atoms over ranks" if world > 1 else None}
     return res
 

@@ -54,6 +54,34 @@ typedef struct sesgb_options
  * builds again (sesgb_counts.rebuilds). For callers that want buffers sized to
  * their molecule rather than to the default estimate. */
 #define SESGB_FLAG_MIN_CAPACITY 4u
+/* Neighbour search on a grid whose cells are the largest pair cutoff (the 27
+ * cells around an atom) instead of the default cells of half that cutoff (the
+ * 125 cells around an atom, each row cut to the atom's reach: about half the
+ * candidate pairs, for a grid eight times finer). Same neighbour lists either
+ * way; for very sparse molecules, whose fine grid would be mostly empty cells. */
+#define SESGB_FLAG_CUTOFF_CELLS 8u
+
+/* Tuning knobs of a context (no counterpart in the reference): the neighbour
+ * search grid and the block shapes of the three heaviest kernels. None of them
+ * changes any result; sesdf_gb300/autotune.py times them on the caller's
+ * molecules. Values: neighbor_cell_span 1 (cells of the largest pair cutoff) or
+ * 2 (cells of half of it, the default); neighbor_warps 2, 4, 8 (default) or 16
+ * warps per block of the neighbour search; visibility_warps and probe_warps 1
+ * (default), 2 or 4 atoms (warps) per block of the visibility pass and the probe
+ * screen; probe_queue 1 runs the probe screen as a persistent grid whose warps take
+ * atoms from a work counter in sorted order (molecule by molecule, reference-grid
+ * cell by cell), 0 (default) as one block per atom group. A change takes effect at
+ * the next build (a captured graph is captured again). */
+typedef struct sesgb_tuning
+{
+    uint32_t neighbor_cell_span;
+    uint32_t neighbor_warps;
+    uint32_t visibility_warps;
+    uint32_t probe_warps;
+    uint32_t probe_queue;
+} sesgb_tuning;
+int sesgb_set_tuning( sesgb_ctx * ctx, const sesgb_tuning * tuning );
+int sesgb_get_tuning( const sesgb_ctx * ctx, sesgb_tuning * tuning );
 
 /* Output buffers of the full-surface build: field for field the reference's
  * bcs::sesdf::SesdfData (sesdf/include/bcs/sesdf/graphics.hpp:39-66). Device pointers,

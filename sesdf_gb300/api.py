@@ -21,6 +21,8 @@ MODE_EXTERIOR = 1
 FLAG_GRAPH = 1
 FLAG_PROFILE = 2
 FLAG_MIN_CAPACITY = 4
+FLAG_CUTOFF_CELLS = 8
+TUNING_FIELDS = ["neighbor_cell_span", "neighbor_warps", "visibility_warps", "probe_warps", "probe_queue"]
 
 BUF_ATOM_INDICES, BUF_NEIGHBOR_COUNT, BUF_NEIGHBOR_IDS, BUF_VISIBILITY_STATUS, BUF_GLOBAL_TO_TRIMMED = range(5)
 
@@ -34,6 +36,7 @@ EXPORTS = [
     "sesgb_create_batch", "sesgb_batch_molecules", "sesgb_molecule_record", "sesgb_get_full_molecule",
     "sesgb_get_exterior_molecule", "sesgb_sdf", "sesgb_sdf_backward", "sesgb_ses_area", "sesgb_ses_area_backward",
     "sesgb_load_mmtf", "sesgb_render", "sesgb_cavities", "sesgb_cavity_labels", "sesgb_cavity_components",
+    "sesgb_set_tuning", "sesgb_get_tuning",
 ]
 SDF_BAND = 3.0
 MOL_FIELDS = ["atoms", "sectors", "full_circles", "partial_circles", "probes", "singular_probes", "segments", "tori",
@@ -56,6 +59,10 @@ class Camera(ctypes.Structure):
                 ("up", ctypes.c_double * 3), ("tan_half_fov", ctypes.c_double), ("t_near", ctypes.c_double),
                 ("t_far", ctypes.c_double), ("eps", ctypes.c_double), ("normal_step", ctypes.c_double),
                 ("width", ctypes.c_uint32), ("height", ctypes.c_uint32), ("max_steps", ctypes.c_uint32)]
+
+
+class Tuning(ctypes.Structure):
+    _fields_ = [(f, ctypes.c_uint32) for f in TUNING_FIELDS]
 
 
 class CavityInfo(ctypes.Structure):
@@ -151,6 +158,8 @@ def load_library(path: str | None = None) -> ctypes.CDLL:
         lib.sesgb_cavities.argtypes = [P, ctypes.c_double, ctypes.POINTER(CavityInfo), P, P]
         lib.sesgb_cavity_labels.argtypes = [P, ctypes.POINTER(P), ctypes.POINTER(ctypes.c_uint64)]
         lib.sesgb_cavity_components.argtypes = [P, P, P, U32]
+        lib.sesgb_set_tuning.argtypes = [P, ctypes.POINTER(Tuning)]
+        lib.sesgb_get_tuning.argtypes = [P, ctypes.POINTER(Tuning)]
         _lib = lib
     return _lib
 
@@ -314,6 +323,22 @@ class SesBuild:
         for k in ("tan_half_fov", "t_near", "t_far", "eps", "normal_step", "width", "height", "max_steps"):
             setattr(c, k, camera[k])
         self._check(self._lib.sesgb_render(self._h, ctypes.byref(c), depth_ptr, normals_ptr, stream), "render")
+
+    def tuning(self) -> dict:
+        """The context's tuning knobs (sesgb_get_tuning)."""
+        t = Tuning()
+        self._check(self._lib.sesgb_get_tuning(self._h, ctypes.byref(t)), "get_tuning")
+        return {f: int(getattr(t, f)) for f in TUNING_FIELDS}
+
+    def set_tuning(self, **knobs):
+        """Changes tuning knobs (sesgb_set_tuning); the others keep their values."""
+        cur = self.tuning()
+        unknown = set(knobs) - set(TUNING_FIELDS)
+        if unknown:
+            raise ValueError(f"unknown tuning knobs {sorted(unknown)}")
+        cur.update({k: int(v) for k, v in knobs.items()})
+        t = Tuning(*[cur[f] for f in TUNING_FIELDS])
+        self._check(self._lib.sesgb_set_tuning(self._h, ctypes.byref(t)), "set_tuning")
 
     def cavities(self, voxel: float, probe_component_ptr: int | None = None, stream: int | None = None) -> dict:
         """Components of the probe-accessible space on the device (sesgb_cavities): the grid, the

@@ -9,6 +9,7 @@
 // buffers are regrown to the exact counts (plus a margin) and the build is
 // run again, so the first build of a new molecule may run twice.
 #include <algorithm>
+#include <initializer_list>
 #include <cmath>
 #include <cstdio>
 #include <cstring>
@@ -206,7 +207,8 @@ namespace
             b.gridM    = grids;
         }
         else
-            b.capCells = (uint32_t)std::max<size_t>( 1u << 16, 4 * n );
+            // a half-cutoff grid over a sparse molecule needs room: cells are coarsened until they fit
+            b.capCells = (uint32_t)std::min<size_t>( std::max<size_t>( 1u << 16, ( b.nbrSpan == 2 ? 16 : 4 ) * n ), 1u << 28 );
         b.cellCount       = dalloc<uint32_t>( c, L, b.capCells + 1ull, ok );
         b.cellStart       = dalloc<uint32_t>( c, L, b.capCells + 1ull, ok );
         b.cellCursor      = dalloc<uint32_t>( c, L, b.capCells + 1ull, ok );
@@ -307,7 +309,7 @@ namespace
         mark( 0 );
         launch_hash( b, s );
         radix_sort( b.keys, b.perm, n, c->gridBits, c->radixScratch, s );
-        launch_fine_params( b, -1.f, n, s );
+        launch_fine_params( b, -1.f, n, s, b.nbrSpan );
         launch_gather( b, s );
         launch_cells( b, 0, n, nullptr, sc, s );
         mark( 1 );
@@ -565,6 +567,10 @@ extern "C"
         c->b.cap         = o.max_neighbor_per_atom ? o.max_neighbor_per_atom : 128u;
         c->b.segCap      = o.max_intersections_per_circle ? o.max_intersections_per_circle : 32u;
         c->flags         = o.flags;
+        c->b.nbrSpan    = ( o.flags & SESGB_FLAG_CUTOFF_CELLS ) ? 1 : 2;
+        c->b.nbrWarps   = 8;
+        c->b.visWarps   = 1;
+        c->b.probeWarps = 1;
         c->b.mode        = mode;
         c->b.rp          = probe_radius;
         c->b.n           = n;
@@ -595,6 +601,44 @@ extern "C"
             return st;
         }
         *out = c;
+        return SESGB_OK;
+    }
+
+    int sesgb_set_tuning( sesgb_ctx * c, const sesgb_tuning * t )
+    {
+        if ( !c || !t )
+            return SESGB_ERR_INVALID;
+        auto one_of = []( uint32_t v, std::initializer_list<uint32_t> ok ) {
+            for ( uint32_t x : ok )
+                if ( v == x )
+                    return true;
+            return false;
+        };
+        if ( !one_of( t->neighbor_cell_span, { 1, 2 } ) || !one_of( t->neighbor_warps, { 2, 4, 8, 16 } )
+             || !one_of( t->visibility_warps, { 1, 2, 4 } ) || !one_of( t->probe_warps, { 1, 2, 4 } ) || t->probe_queue > 1 )
+        {
+            c->err = "tuning value out of range";
+            return SESGB_ERR_INVALID;
+        }
+        Build & b          = c->b;
+        b.nbrSpan          = (int)t->neighbor_cell_span;
+        b.nbrWarps         = (int)t->neighbor_warps;
+        b.visWarps         = (int)t->visibility_warps;
+        b.probeWarps       = (int)t->probe_warps;
+        b.probeQueueBlocks = t->probe_queue ? probe_queue_blocks( b, b.probeWarps ) : 0u;
+        destroy_graph( c );
+        return SESGB_OK;
+    }
+
+    int sesgb_get_tuning( const sesgb_ctx * c, sesgb_tuning * t )
+    {
+        if ( !c || !t )
+            return SESGB_ERR_INVALID;
+        t->neighbor_cell_span = (uint32_t)c->b.nbrSpan;
+        t->neighbor_warps     = (uint32_t)c->b.nbrWarps;
+        t->visibility_warps   = (uint32_t)c->b.visWarps;
+        t->probe_warps        = (uint32_t)c->b.probeWarps;
+        t->probe_queue        = c->b.probeQueueBlocks ? 1u : 0u;
         return SESGB_OK;
     }
 
@@ -1163,6 +1207,10 @@ extern "C"
         c->b.cap        = o.max_neighbor_per_atom ? o.max_neighbor_per_atom : 128u;
         c->b.segCap     = o.max_intersections_per_circle ? o.max_intersections_per_circle : 32u;
         c->flags        = o.flags;
+        c->b.nbrSpan    = ( o.flags & SESGB_FLAG_CUTOFF_CELLS ) ? 1 : 2;
+        c->b.nbrWarps   = 8;
+        c->b.visWarps   = 1;
+        c->b.probeWarps = 1;
         c->b.mode       = mode;
         c->b.rp         = probe_radius;
         c->b.n          = n;
@@ -1199,7 +1247,7 @@ extern "C"
             }
             c->molGrid[ m ].size = (int)gs;
             molShift             = std::max( molShift, 3 * (int)floor_log2( gs ) );
-            c->molCells[ m ]     = std::max<uint32_t>( 1024u, cnt );
+            c->molCells[ m ]     = std::max<uint32_t>( 1024u, 4u * cnt );
         }
         const int molBits = (int)floor_log2( molecules - 1 ) + 1;
         if ( molShift + molBits > 32 )

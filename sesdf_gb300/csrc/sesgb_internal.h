@@ -56,6 +56,7 @@ namespace sesgb
         uint32_t jobs;       // double-precision probe jobs
         uint32_t segCircles; // circles carrying at least two probes
         uint32_t visBand;    // visibility tests queued for double precision
+        uint32_t probeCursor; // work counter of the persistent probe screen
     };
 
     enum Overflow : uint32_t
@@ -96,6 +97,7 @@ namespace sesgb
         float    h;
         int3     dims;
         uint32_t cells;
+        int      span; // cells the search stencil reaches on each side: 1 (cell >= cutoff) or 2 (cell >= cutoff / 2)
     };
 
     // ---- primitives (sesgb_sort.cu) ------------------------------------------

@@ -199,7 +199,7 @@ namespace sesgb
         }
 
         // thread per molecule: neighbour-grid geometry from the molecule's reference grid box
-        __global__ void k_fine_params( Build b, float cutoff )
+        __global__ void k_fine_params( Build b, float cutoff, int span )
         {
             pdl_begin();
             if ( cutoff < 0.f )
@@ -209,7 +209,7 @@ namespace sesgb
                 const GridRef  gr  = grid_of( b, m );
                 const uint32_t cap = b.nMol > 1 ? b.cellBase[ m + 1 ] - b.cellBase[ m ] : b.capCells;
                 const float    ex = gr.cell.x * gr.size, ey = gr.cell.y * gr.size, ez = gr.cell.z * gr.size;
-                float          h  = cutoff;
+                float          h  = cutoff / (float)span;
                 int3           d;
                 for ( int it = 0; it < 200; it++ )
                 {
@@ -223,6 +223,7 @@ namespace sesgb
                 g.h         = h;
                 g.dims      = d;
                 g.cells     = (uint32_t)( (uint64_t)d.x * d.y * d.z );
+                g.span      = span;
                 b.fine[ m ] = g;
                 if ( m == 0 )
                 {
@@ -321,22 +322,95 @@ namespace sesgb
             return __dsqrt_rn( ddot( dd, dd ) ) < 2.0 * (double)rp;
         }
 
-        __global__ void __launch_bounds__( 32 * kWarpsPerBlock ) k_neighbors( Build b )
+        // The 25 rows of a span-2 stencil (cells of at least half the largest pair cutoff) around
+        // atom position p, each cut to the x-range that can hold a neighbour of the atom: a
+        // neighbour j lies within cut = R_i + R_max (+ margins) of p, so a row (y, z) whose cells
+        // keep |dy|, |dz| >= ey, ez from p only needs x within sqrt(cut^2 - ey^2 - ez^2) of p.
+        // Lane r < 25 computes row r; the rows' first items and exclusive prefixes go to shared
+        // memory (start[25], pre[26] with pre[25] = total), and the total is returned. A cell two
+        // beyond the atom's own along any axis starts at least 2h >= the largest pair cutoff away.
+        __device__ __forceinline__ uint32_t stencil_rows_span2( const FineGrid & g, const uint32_t * cellStart, float4 p,
+                                                                float cut, uint32_t * start, uint32_t * pre )
+        {
+            const uint32_t lane = lane_id();
+            const int3     c    = fine_cell( g, p.x, p.y, p.z );
+            uint32_t       st = 0, len = 0;
+            if ( lane < 25u )
+            {
+                const int y = c.y + (int)( lane % 5u ) - 2;
+                const int z = c.z + (int)( lane / 5u ) - 2;
+                if ( y >= 0 && z >= 0 && y < g.dims.y && z < g.dims.z )
+                {
+                    const float ylo = g.origin.y + (float)y * g.h, zlo = g.origin.z + (float)z * g.h;
+                    const float ey  = fmaxf( 0.f, fmaxf( ylo - p.y, p.y - ( ylo + g.h ) ) );
+                    const float ez  = fmaxf( 0.f, fmaxf( zlo - p.z, p.z - ( zlo + g.h ) ) );
+                    const float w2  = cut * cut - ey * ey - ez * ez;
+                    if ( w2 >= 0.f )
+                    {
+                        const float w  = sqrtf( w2 ) + 0.01f;
+                        int         x0 = (int)floorf( ( p.x - w - g.origin.x ) / g.h );
+                        int         x1 = (int)floorf( ( p.x + w - g.origin.x ) / g.h );
+                        x0             = max( x0, max( c.x - 2, 0 ) );
+                        x1             = min( x1, min( c.x + 2, g.dims.x - 1 ) );
+                        if ( x0 <= x1 )
+                        {
+                            st  = cellStart[ fine_key( g, make_int3( x0, y, z ) ) ];
+                            len = cellStart[ fine_key( g, make_int3( x1, y, z ) ) + 1 ] - st;
+                        }
+                    }
+                }
+            }
+            uint32_t       total;
+            const uint32_t ex = warp_exclusive_sum( len, total );
+            if ( lane < 25u )
+            {
+                start[ lane ] = st;
+                pre[ lane ]   = ex;
+            }
+            if ( lane == 0 )
+                pre[ 25 ] = total;
+            __syncwarp();
+            return total;
+        }
+        // cell-item index of stencil item f (f < total): the last row whose prefix is <= f
+        __device__ __forceinline__ uint32_t row_item_span2( const uint32_t * start, const uint32_t * pre, uint32_t f )
+        {
+            uint32_t r = 0;
+#pragma unroll
+            for ( uint32_t step = 16; step > 0; step >>= 1 )
+                if ( r + step < 25u && pre[ r + step ] <= f )
+                    r += step;
+            return start[ r ] + ( f - pre[ r ] );
+        }
+
+        template<int W>
+        __global__ void __launch_bounds__( 32 * W ) k_neighbors( Build b )
         {
             pdl_begin();
-            __shared__ uint32_t buf[ kWarpsPerBlock ][ kNbrBuf ];
+            __shared__ uint32_t buf[ W ][ kNbrBuf ];
+            __shared__ uint32_t rowStart[ W ][ 25 ], rowPre[ W ][ 26 ];
             const uint32_t      warp = threadIdx.x >> 5, lane = lane_id();
-            const uint32_t      i    = blockIdx.x * kWarpsPerBlock + warp;
+            const uint32_t      i    = blockIdx.x * W + warp;
             if ( i >= b.n )
                 return;
-            const uint32_t m  = mol_of( b, i );
-            const FineGrid g  = b.fine[ m ];
-            const float4   ai = b.atoms[ i ];
-            Rows           rows;
-            stencil_rows( g, b.cellStart + cell_base( b, m ), fine_cell( g, ai.x, ai.y, ai.z ), rows );
+            const uint32_t   m     = mol_of( b, i );
+            const FineGrid   g     = b.fine[ m ];
+            const float4     ai    = b.atoms[ i ];
+            const uint32_t * cells = b.cellStart + cell_base( b, m );
+            const bool       span2 = g.span == 2;
+            Rows             rows;
+            uint32_t         total;
+            if ( span2 )
+                total = stencil_rows_span2( g, cells, ai, ( ai.w + b.rp ) + ( b.counts->rmax + b.rp ) + 0.01f, rowStart[ warp ],
+                                            rowPre[ warp ] );
+            else
+            {
+                stencil_rows( g, cells, fine_cell( g, ai.x, ai.y, ai.z ), rows );
+                total = rows.total;
+            }
             const float Ri    = ai.w + b.rp;
             uint32_t    count = 0, fp64 = 0;
-            for ( uint32_t base0 = 0; base0 < rows.total; base0 += 64 )
+            for ( uint32_t base0 = 0; base0 < total; base0 += 64 )
             {
                 // two rows of 32 items: the loads of both issued before their use
                 uint32_t jj[ 2 ] = { 0u, 0u };
@@ -345,9 +419,9 @@ namespace sesgb
                 for ( int h = 0; h < 2; h++ )
                 {
                     const uint32_t f = base0 + 32 * h + lane;
-                    if ( f < rows.total )
+                    if ( f < total )
                     {
-                        const uint32_t idx = row_item( rows, f );
+                        const uint32_t idx = span2 ? row_item_span2( rowStart[ warp ], rowPre[ warp ], f ) : row_item( rows, f );
                         jj[ h ]            = b.cellItems[ idx ];
                         pp[ h ]            = b.cellPos[ idx ];
                     }
@@ -356,12 +430,12 @@ namespace sesgb
                 for ( int h = 0; h < 2; h++ )
                 {
                     const uint32_t base = base0 + 32 * h;
-                    if ( base >= rows.total )
+                    if ( base >= total )
                         break;
                     const uint32_t f    = base + lane;
                     bool           pass = false;
                     const uint32_t j    = jj[ h ];
-                    if ( f < rows.total && j != i )
+                    if ( f < total && j != i )
                     {
                         const float4 aj = pp[ h ];
                         const f3     dj = F3( aj.x - ai.x, aj.y - ai.y, aj.z - ai.z );
@@ -590,14 +664,14 @@ namespace sesgb
         };
         __device__ __forceinline__ uint32_t operator*( UnitStride, uint32_t u ) { return u; }
 
-        // one warp (one atom) per block, as k_probes: a slot is freed when its atom is done
-        constexpr int kVisWarps = 1;
-        __global__ void __launch_bounds__( 32 * kVisWarps, 32 / kVisWarps ) k_visibility( Build b )
+        // W warps (atoms) per block; one by default, as k_probes: a slot is freed when its atom is done
+        template<int W>
+        __global__ void __launch_bounds__( 32 * W, 32 / W ) k_visibility( Build b )
         {
             pdl_begin();
             extern __shared__ __align__( 16 ) unsigned char smemRaw[];
             const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
-            const uint32_t i    = blockIdx.x * kVisWarps + warp;
+            const uint32_t i    = blockIdx.x * W + warp;
             if ( i >= b.n )
                 return;
             const VisSmem  m   = vis_smem( smemRaw + warp * vis_smem_per_warp( b.cap ), b.cap );
@@ -890,7 +964,7 @@ namespace sesgb
             }
         }
 
-        __host__ inline size_t visibility_smem( uint32_t cap ) { return vis_smem_per_warp( cap ) * kVisWarps; }
+        __host__ inline size_t visibility_smem( uint32_t cap, int warps ) { return vis_smem_per_warp( cap ) * (size_t)warps; }
 
         // ---- sectors, complete circles, partial-circle numbering -----------
         // sector of buildConvexPatchesSectors (operations.inl:186-213) in
@@ -1190,7 +1264,6 @@ namespace sesgb
 
         // One warp per block: the work of an atom varies a lot, and a block's slot (its
         // registers and shared memory) is freed only when its last warp ends.
-        constexpr int kProbeWarps = 1;   // warps per block of k_probes
         constexpr int kCandBuf    = 64;  // candidates queued per warp
         constexpr int kProbeBuf   = 128; // probes of one atom (the reference's per-block buffer, operations.inl:248)
 
@@ -1404,15 +1477,10 @@ namespace sesgb
         // whose far atoms are neighbours. Entries of the atom's probe list are kept
         // in order (circle (i, j), then k, then x1 before x2) and written as one
         // chunk; positions and undecided flags are completed by k_probe_jobs.
-        __global__ void __launch_bounds__( 32 * kProbeWarps, 32 / kProbeWarps ) k_probes( Build b )
+        __device__ __forceinline__ void probes_of_atom( const Build & b, uint32_t i, unsigned char * smemWarp )
         {
-            pdl_begin();
-            extern __shared__ __align__( 16 ) unsigned char smemRaw[];
-            const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
-            const uint32_t i    = blockIdx.x * kProbeWarps + warp;
-            if ( i >= b.n )
-                return;
-            const ProbeSmem m   = probe_smem( smemRaw + warp * probe_smem_per_warp( b.cap ), b.cap );
+            const uint32_t  lane = lane_id();
+            const ProbeSmem m    = probe_smem( smemWarp, b.cap );
             const uint32_t  ni  = b.nbrCount[ i ];
             const float4    ai  = b.atoms[ i ];
             const float     Ri  = ai.w + b.rp;
@@ -1775,6 +1843,36 @@ namespace sesgb
                 b.chunkLen[ i ]   = fits ? kept : 0u;
                 b.singCnt[ i ]    = fits ? nSing : 0u;
                 b.regCnt[ i ]     = fits ? nReg : 0u;
+            }
+        }
+
+        // W warps per block; with kQueue the grid is persistent and its warps take atoms from a
+        // work counter (in sorted order: molecule by molecule, reference-grid cell by cell), else
+        // warp w of block k takes atom k W + w
+        template<int W, bool kQueue>
+        __global__ void __launch_bounds__( 32 * W, 32 / W ) k_probes( Build b )
+        {
+            pdl_begin();
+            extern __shared__ __align__( 16 ) unsigned char smemRaw[];
+            const uint32_t  warp = threadIdx.x >> 5, lane = lane_id();
+            unsigned char * mine = smemRaw + warp * probe_smem_per_warp( b.cap );
+            if ( !kQueue )
+            {
+                const uint32_t i = blockIdx.x * W + warp;
+                if ( i < b.n )
+                    probes_of_atom( b, i, mine );
+                return;
+            }
+            for ( uint32_t it = 0; it < b.n; it++ ) // bounded: every turn takes a new atom
+            {
+                uint32_t i = 0;
+                if ( lane == 0 )
+                    i = atomicAdd( &b.counts->probeCursor, 1u );
+                i = __shfl_sync( 0xffffffffu, i, 0 );
+                if ( i >= b.n )
+                    break;
+                probes_of_atom( b, i, mine );
+                __syncwarp();
             }
         }
 
@@ -2564,9 +2662,9 @@ namespace sesgb
         pdl_launch( k_hash, blocks_for( b.n, 256 ), 256, 0, s, b );
         counted();
     }
-    void launch_fine_params( const Build & b, float cutoff, uint32_t, cudaStream_t s )
+    void launch_fine_params( const Build & b, float cutoff, uint32_t, cudaStream_t s, int span )
     {
-        pdl_launch( k_fine_params, blocks_for( b.nMol, 128 ), 128, 0, s, b, cutoff );
+        pdl_launch( k_fine_params, blocks_for( b.nMol, 128 ), 128, 0, s, b, cutoff, span );
         counted();
     }
     void launch_zero2( uint32_t * a, uint32_t * c, uint32_t nHost, const uint32_t * nDevice, cudaStream_t s )
@@ -2616,14 +2714,25 @@ namespace sesgb
     {
         if ( !b.n )
             return;
-        pdl_launch( k_neighbors, blocks_for( b.n, kWarpsPerBlock ), 32 * kWarpsPerBlock, 0, s, b );
+        switch ( b.nbrWarps )
+        {
+        case 2: pdl_launch( k_neighbors<2>, blocks_for( b.n, 2 ), 64, 0, s, b ); break;
+        case 4: pdl_launch( k_neighbors<4>, blocks_for( b.n, 4 ), 128, 0, s, b ); break;
+        case 16: pdl_launch( k_neighbors<16>, blocks_for( b.n, 16 ), 512, 0, s, b ); break;
+        default: pdl_launch( k_neighbors<8>, blocks_for( b.n, 8 ), 256, 0, s, b ); break;
+        }
         counted();
     }
     void launch_visibility( const Build & b, cudaStream_t s )
     {
         if ( !b.n )
             return;
-        pdl_launch( k_visibility, blocks_for( b.n, kVisWarps ), 32 * kVisWarps, visibility_smem( b.cap ), s, b );
+        switch ( b.visWarps )
+        {
+        case 2: pdl_launch( k_visibility<2>, blocks_for( b.n, 2 ), 64, visibility_smem( b.cap, 2 ), s, b ); break;
+        case 4: pdl_launch( k_visibility<4>, blocks_for( b.n, 4 ), 128, visibility_smem( b.cap, 4 ), s, b ); break;
+        default: pdl_launch( k_visibility<1>, blocks_for( b.n, 1 ), 32, visibility_smem( b.cap, 1 ), s, b ); break;
+        }
         counted();
     }
     void launch_visibility_resolve( const Build & b, cudaStream_t s )
@@ -2645,8 +2754,17 @@ namespace sesgb
     {
         if ( !b.n )
             return;
-        const size_t smem = probe_smem_per_warp( b.cap ) * kProbeWarps;
-        pdl_launch( k_probes, blocks_for( b.n, kProbeWarps ), 32 * kProbeWarps, smem, s, b );
+        const size_t   smem  = probe_smem_per_warp( b.cap ) * (size_t)b.probeWarps;
+        const uint32_t queue = b.probeQueueBlocks; // resident blocks of the persistent variant (0: one warp per atom)
+        switch ( b.probeWarps * 2 + ( queue ? 1 : 0 ) )
+        {
+        case 3: pdl_launch( k_probes<1, true>, min( queue, blocks_for( b.n, 1 ) ), 32, smem, s, b ); break;
+        case 4: pdl_launch( k_probes<2, false>, blocks_for( b.n, 2 ), 64, smem, s, b ); break;
+        case 5: pdl_launch( k_probes<2, true>, min( queue, blocks_for( b.n, 2 ) ), 64, smem, s, b ); break;
+        case 8: pdl_launch( k_probes<4, false>, blocks_for( b.n, 4 ), 128, smem, s, b ); break;
+        case 9: pdl_launch( k_probes<4, true>, min( queue, blocks_for( b.n, 4 ) ), 128, smem, s, b ); break;
+        default: pdl_launch( k_probes<1, false>, blocks_for( b.n, 1 ), 32, smem, s, b ); break;
+        }
         counted();
     }
     void launch_probe_jobs( const Build & b, cudaStream_t s )
@@ -2705,11 +2823,36 @@ namespace sesgb
 
     cudaError_t configure_kernels( const Build & b )
     {
-        cudaError_t e = cudaFuncSetAttribute( k_visibility, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)visibility_smem( b.cap ) );
-        if ( e != cudaSuccess )
-            return e;
-        return cudaFuncSetAttribute( k_probes, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)( probe_smem_per_warp( b.cap ) * kProbeWarps ) );
+        const size_t vs = vis_smem_per_warp( b.cap ), ps = probe_smem_per_warp( b.cap );
+        cudaError_t  e  = cudaSuccess;
+        auto         set = [ & ]( const void * f, size_t bytes ) {
+            if ( e == cudaSuccess )
+                e = cudaFuncSetAttribute( f, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes );
+        };
+        set( (const void *)k_visibility<1>, vs );
+        set( (const void *)k_visibility<2>, 2 * vs );
+        set( (const void *)k_visibility<4>, 4 * vs );
+        set( (const void *)k_probes<1, false>, ps );
+        set( (const void *)k_probes<1, true>, ps );
+        set( (const void *)k_probes<2, false>, 2 * ps );
+        set( (const void *)k_probes<2, true>, 2 * ps );
+        set( (const void *)k_probes<4, false>, 4 * ps );
+        set( (const void *)k_probes<4, true>, 4 * ps );
+        return e;
+    }
+
+    uint32_t probe_queue_blocks( const Build & b, int warps )
+    {
+        // blocks of the persistent probe kernel that fit on the GPU at once
+        int          dev = 0, sms = 0, per = 0;
+        const void * f   = warps == 4 ? (const void *)k_probes<4, true>
+                                      : warps == 2 ? (const void *)k_probes<2, true> : (const void *)k_probes<1, true>;
+        cudaGetDevice( &dev );
+        cudaDeviceGetAttribute( &sms, cudaDevAttrMultiProcessorCount, dev );
+        if ( cudaOccupancyMaxActiveBlocksPerMultiprocessor( &per, f, 32 * warps, probe_smem_per_warp( b.cap ) * warps )
+             != cudaSuccess )
+            per = 1;
+        return (uint32_t)std::max( 1, sms * std::max( per, 1 ) );
     }
     void launch_reference_fill( const Build & b, uint32_t * globalToTrimmed, cudaStream_t s )
     {

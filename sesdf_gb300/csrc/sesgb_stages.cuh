@@ -27,6 +27,11 @@ namespace sesgb
         int      mode;   // 0 full surface, 1 exterior only
         float    rp;
         GridRef  grid;
+        int      nbrSpan; // neighbour-search grid: cells of the pair cutoff / nbrSpan (1 or 2)
+        // block shapes (warps per block) of the neighbour search, the visibility pass and the probe
+        // screen, and the resident blocks of the persistent probe screen (0: one block per atom group)
+        int      nbrWarps, visWarps, probeWarps;
+        uint32_t probeQueueBlocks;
 
         // batches: nMol molecules built together (nMol = 1 for a single molecule). Sort
         // keys carry the molecule above molShift, so every molecule keeps its own
@@ -114,7 +119,8 @@ namespace sesgb
 
     // ---- launchers (sesgb_stages.cu) ---------------------------------------
     void launch_hash( const Build & b, cudaStream_t s );
-    void launch_fine_params( const Build & b, float cutoff, uint32_t items, cudaStream_t s );
+    // neighbour-grid geometry: cells of cutoff / span (span 1 or 2), coarsened until they fit the capacity
+    void launch_fine_params( const Build & b, float cutoff, uint32_t items, cudaStream_t s, int span = 1 );
     void launch_gather( const Build & b, cudaStream_t s );
     // zeroes a[0, n] and c[0, n] (c may be null) with n = min(*nDevice, nHost), or nHost without nDevice
     void launch_zero2( uint32_t * a, uint32_t * c, uint32_t nHost, const uint32_t * nDevice, cudaStream_t s );
@@ -178,6 +184,7 @@ namespace sesgb
     void launch_tori( const Build & b, cudaStream_t s );
     void launch_tori_emit( const Build & b, cudaStream_t s );
     cudaError_t configure_kernels( const Build & b );
+    uint32_t    probe_queue_blocks( const Build & b, int warps );
     uint64_t    launch_count();
     void launch_reference_fill( const Build & b, uint32_t * globalToTrimmed, cudaStream_t s );
 } // namespace sesgb

@@ -243,3 +243,34 @@ def test_profiled_graph_stage_times():
         total = t0.elapsed_time(t1)
     assert all(v >= 0 for v in st.values())
     assert 0.5 * total <= sum(st.values()) <= 1.01 * total + 0.05
+
+
+@pytest.mark.parametrize("mode", ["full", "exterior"])
+def test_tuning_knobs_change_no_result(mode):
+    # every tuning knob (neighbour-grid cell size, block shapes, persistent probe screen) is a
+    # speed choice: each setting must give the default build's buffers exactly
+    from sesdf_gb300.autotune import KNOBS
+    atoms = synth.globule(5000, 81)
+    with SesBuild(atoms, RP, mode) as g:
+        g.build()
+        want = g.fetch()
+        default = g.tuning()
+        assert default == {"neighbor_cell_span": 2, "neighbor_warps": 8, "visibility_warps": 1, "probe_warps": 1,
+                           "probe_queue": 0}
+        for knob, values in KNOBS.items():
+            for v in values:
+                g.set_tuning(**dict(default, **{knob: v}))
+                g.build()
+                same_buffers(g.fetch(), want, (knob, v))
+        with pytest.raises(Exception):
+            g.set_tuning(neighbor_warps=3)
+
+
+def test_cutoff_cells_match_oracle():
+    # the 27-cell neighbour search (cells of the full pair cutoff) against the oracle
+    atoms = synth.globule(2000, 1000)
+    with SesBuild(atoms, RP, "full") as g:
+        g.set_tuning(neighbor_cell_span=1)
+        g.build()
+        out = g.fetch()
+    compare(atoms, out, oracle.run(atoms, RP, "full"), "full")
