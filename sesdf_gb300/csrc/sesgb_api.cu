@@ -353,7 +353,7 @@ namespace
 
         // G: neighbours of singular probes
         mark( 8 );
-        launch_fine_params( b, 2.f * c->rp + 0.01f, 0, s );
+        launch_fine_params( b, 2.f * c->rp + 0.01f, 0, s, b.nbrSpan );
         launch_cells( b, 1, b.capProbes, &d->Q, sc, s );
         launch_probe_neighbors( b, s );
 

@@ -2340,6 +2340,7 @@ namespace sesgb
         {
             pdl_begin();
             __shared__ unsigned long long buf[ kWarpsPerBlock ][ kSnbrBuf ];
+            __shared__ uint32_t           rowStart[ kWarpsPerBlock ][ 25 ], rowPre[ kWarpsPerBlock ][ 26 ];
             const uint32_t                warp = threadIdx.x >> 5, lane = lane_id();
             const uint32_t                Q    = min( b.counts->Q, b.capProbes );
             const float                   t2   = 2.f * b.rp;
@@ -2351,17 +2352,27 @@ namespace sesgb
                 const uint32_t m  = b.nMol > 1 ? mol_of( b, (uint32_t)b.probeIds[ pi ].x ) : 0u;
                 const FineGrid g  = b.fine[ m ];
                 const GridRef  gr = grid_of( b, m );
-                Rows           rows;
-                stencil_rows( g, b.cellStart + cell_base( b, m ), fine_cell( g, pq.x, pq.y, pq.z ), rows );
+                const uint32_t * cells = b.cellStart + cell_base( b, m );
+                const bool       span2 = g.span == 2;
+                Rows             rows;
+                uint32_t         total;
+                __syncwarp();
+                if ( span2 )
+                    total = stencil_rows_span2( g, cells, pq, t2 + 0.005f, rowStart[ warp ], rowPre[ warp ] );
+                else
+                {
+                    stencil_rows( g, cells, fine_cell( g, pq.x, pq.y, pq.z ), rows );
+                    total = rows.total;
+                }
                 uint32_t count = 0;
-                for ( uint32_t base = 0; base < rows.total; base += 32 )
+                for ( uint32_t base = 0; base < total; base += 32 )
                 {
                     const uint32_t     f    = base + lane;
                     bool               pass = false;
                     unsigned long long key  = 0;
-                    if ( f < rows.total )
+                    if ( f < total )
                     {
-                        const uint32_t idx = row_item( rows, f );
+                        const uint32_t idx = span2 ? row_item_span2( rowStart[ warp ], rowPre[ warp ], f ) : row_item( rows, f );
                         const uint32_t p   = b.cellItems[ idx ];
                         if ( p != q )
                         {
