@@ -2587,8 +2587,20 @@ namespace sesgb
                     const float    d   = dot( dj, dj );
                     const float    t   = ( Ri * Ri - Rj * Rj + d ) / ( 2.f * d );
                     const f3       c   = dj * t; // circle centre relative to atom i
-                    const float    r   = sqrtf( fmaxf( Ri * Ri - dot( c, c ), 0.f ) );
-                    const f3       ta  = normalize( c );
+                    float          r2  = Ri * Ri - dot( c, c );
+                    if ( r2 < 0.004f * Ri * Ri )
+                    {
+                        // nearly tangent SAS spheres: the radius is the root of a difference of nearly
+                        // equal numbers; taken in double precision from the float32 atoms
+                        const double Rid = (double)ai.w + (double)b.rp, Rjd = (double)aj.w + (double)b.rp;
+                        const double ex = (double)aj.x - (double)ai.x, ey = (double)aj.y - (double)ai.y,
+                                     ez = (double)aj.z - (double)ai.z;
+                        const double dd = ex * ex + ey * ey + ez * ez;
+                        const double td = ( Rid * Rid - Rjd * Rjd + dd ) / ( 2.0 * dd );
+                        r2              = (float)( Rid * Rid - td * td * dd );
+                    }
+                    const float r  = sqrtf( fmaxf( r2, 0.f ) );
+                    const f3    ta = normalize( c );
                     f3             cz  = cross( ta, F3( 0.f, 0.f, 1.f ) );
                     if ( dot( cz, cz ) < 1e-12f )
                     {
@@ -2946,10 +2958,82 @@ namespace sesgb
             }
         }
 
-        // one query, the whole warp; the hit is valid in every lane
-        __device__ SdfHit sdf_query( const Build & b, float3 x, SdfSmem & sm, float band, uint32_t & overflow )
+        // Float32 error bound of |q - c_k|^2 - R_k^2 for a point q computed in absolute float32
+        // coordinates: a few ulps of |q| on every coordinate, times 2 |q - c_k|, plus the rounding of
+        // the squares. Inside it the test is taken again in double precision.
+        __device__ __forceinline__ float hidden_band( float3 q, float d2, float Rk )
         {
-            const uint32_t lane = lane_id();
+            const float Q = fmaxf( fabsf( q.x ), fmaxf( fabsf( q.y ), fabsf( q.z ) ) );
+            return 3.8147e-6f * ( d2 + Rk * Rk + 4.f * Q * sqrtf( d2 ) + 1.f );
+        }
+
+        // point q (double) strictly inside the SAS sphere of atom k, in double precision
+        __device__ __noinline__ bool point_inside_d( const Build & b, d3 q, uint32_t k )
+        {
+            const float4 ck = b.atoms[ k ];
+            const double Rk = (double)ck.w + (double)b.rp;
+            const double dx = q.x - (double)ck.x, dy = q.y - (double)ck.y, dz = q.z - (double)ck.z;
+            return dx * dx + dy * dy + dz * dz < Rk * Rk;
+        }
+
+        // The radial projection of x on the SAS sphere of i, in double precision, strictly inside the
+        // SAS sphere of one of this lane's near neighbours (lanes take every 32nd)
+        __device__ __noinline__ bool sphere_point_hidden_d( const Build & b, const SdfSmem & sm, size_t row, uint32_t nn,
+                                                            uint32_t i, float3 x, uint32_t lane )
+        {
+            const float4 ci = b.atoms[ i ];
+            const d3     wd = D3( (double)x.x - (double)ci.x, (double)x.y - (double)ci.y, (double)x.z - (double)ci.z );
+            const double Rd = (double)ci.w + (double)b.rp;
+            const double sc = Rd / sqrt( wd.x * wd.x + wd.y * wd.y + wd.z * wd.z );
+            const d3     qd = D3( (double)ci.x + wd.x * sc, (double)ci.y + wd.y * sc, (double)ci.z + wd.z * sc );
+            bool         hd = false;
+            for ( uint32_t e = lane; e < nn; e += 32 )
+                hd = hd || point_inside_d( b, qd, b.nbr[ row + sm.near[ e ] ] );
+            return hd;
+        }
+
+        // The nearest point of circle (i, neighbour slot s) to x, in double precision, strictly inside
+        // the SAS sphere of a near neighbour of i other than that of slot s
+        __device__ __noinline__ bool circle_point_hidden_d( const Build & b, const SdfSmem & sm, size_t row, uint32_t nn,
+                                                            uint32_t i, uint32_t s, float3 x )
+        {
+            const float4 ai = b.atoms[ i ], aj = b.atoms[ b.nbr[ row + s ] ];
+            const double Ri = (double)ai.w + (double)b.rp, Rj = (double)aj.w + (double)b.rp;
+            const d3     d  = D3( (double)aj.x - (double)ai.x, (double)aj.y - (double)ai.y, (double)aj.z - (double)ai.z );
+            const double dd = d.x * d.x + d.y * d.y + d.z * d.z;
+            const double tt = ( Ri * Ri - Rj * Rj + dd ) / ( 2.0 * dd );
+            const double r2 = Ri * Ri - tt * tt * dd;
+            if ( !( r2 > 0.0 ) )
+                return false;
+            const double r   = sqrt( r2 );
+            const double inv = 1.0 / sqrt( dd );
+            const d3     n   = D3( d.x * inv, d.y * inv, d.z * inv );
+            const d3     c   = D3( (double)ai.x + d.x * tt, (double)ai.y + d.y * tt, (double)ai.z + d.z * tt );
+            const d3     w   = D3( (double)x.x - c.x, (double)x.y - c.y, (double)x.z - c.z );
+            const double h   = w.x * n.x + w.y * n.y + w.z * n.z;
+            const d3     v   = D3( w.x - h * n.x, w.y - h * n.y, w.z - h * n.z );
+            const double rho = sqrt( v.x * v.x + v.y * v.y + v.z * v.z );
+            if ( !( rho > 0.0 ) )
+                return false;
+            const d3 q = D3( c.x + v.x * ( r / rho ), c.y + v.y * ( r / rho ), c.z + v.z * ( r / rho ) );
+            for ( uint32_t e = 0; e < nn; e++ )
+            {
+                const uint32_t k = sm.near[ e ];
+                if ( k != s && point_inside_d( b, q, b.nbr[ row + k ] ) )
+                    return true;
+            }
+            return false;
+        }
+
+        // one query, the whole warp; the hit is valid in every lane. A point of dE within the float32
+        // error of another SAS sphere is decided in double precision with kExact; without it the
+        // query is only marked (exact set, in every lane), for a second pass that runs it with kExact.
+        template<bool kExact>
+        __device__ SdfHit sdf_query( const Build & b, float3 x, SdfSmem & sm, float band, uint32_t & overflow, bool & exact )
+        {
+            const uint32_t lane      = lane_id();
+            bool           exactLane = false;
+            exact                    = false;
             const float    T    = b.rp + band;
             const FineGrid g    = b.fine[ 0 ];
             Rows           rows;
@@ -3147,14 +3231,28 @@ namespace sesgb
                     if ( L > 0.f )
                     {
                         const float3 q = make_float3( ci.x + w.x * ( Ri / L ), ci.y + w.y * ( Ri / L ), ci.z + w.z * ( Ri / L ) );
-                        bool         hidden = false;
+                        bool         hidden = false, unsure = false;
                         for ( uint32_t e = lane; e < nn; e += 32 )
                         {
                             const float4 nk = sdf_nb( b, sm, row, sm.near[ e ] );
                             const float  dx = q.x - nk.x, dy = q.y - nk.y, dz = q.z - nk.z;
-                            hidden          = hidden || ( dx * dx + dy * dy + dz * dz < nk.w * nk.w );
+                            const float  d2 = dx * dx + dy * dy + dz * dz;
+                            const float  m  = d2 - nk.w * nk.w;
+                            const float  eb = hidden_band( q, d2, nk.w );
+                            hidden          = hidden || m < -eb;
+                            unsure          = unsure || !( fabsf( m ) > eb );
                         }
-                        if ( !__any_sync( 0xffffffffu, hidden ) && lane == 0 )
+                        bool hid = __any_sync( 0xffffffffu, hidden );
+                        if ( !hid && __any_sync( 0xffffffffu, unsure ) )
+                        {
+                            // a neighbour's sphere passes within the float32 error of the point:
+                            // the point and the test in double precision
+                            if ( kExact )
+                                hid = __any_sync( 0xffffffffu, sphere_point_hidden_d( b, sm, row, nn, i, x, lane ) );
+                            else
+                                exactLane = true;
+                        }
+                        if ( !hid && lane == 0 )
                         {
                             cand = dl;
                             ck   = kSdfSphere;
@@ -3197,7 +3295,7 @@ namespace sesgb
                         dist = sqrtf( h * h + ( rho - r ) * ( rho - r ) );
                         if ( !( dist < cand ) || !( dist < best ) )
                             continue;
-                        bool hidden = false;
+                        bool hidden = false, unsure = false;
                         for ( uint32_t e = 0; e < nn && !hidden; e++ )
                         {
                             const uint32_t k = sm.near[ e ];
@@ -3205,7 +3303,18 @@ namespace sesgb
                                 continue;
                             const float4 nk = sdf_nb( b, sm, row, k );
                             const float  dx = q.x - nk.x, dy = q.y - nk.y, dz = q.z - nk.z;
-                            hidden          = dx * dx + dy * dy + dz * dz < nk.w * nk.w;
+                            const float  d2 = dx * dx + dy * dy + dz * dz;
+                            const float  m  = d2 - nk.w * nk.w;
+                            const float  eb = hidden_band( q, d2, nk.w );
+                            hidden          = m < -eb;
+                            unsure          = unsure || !( fabsf( m ) > eb );
+                        }
+                        if ( !hidden && unsure )
+                        {
+                            if ( kExact )
+                                hidden = circle_point_hidden_d( b, sm, row, nn, i, s, x );
+                            else
+                                exactLane = true;
                         }
                         if ( hidden )
                             continue;
@@ -3240,6 +3349,7 @@ namespace sesgb
                 __syncwarp();
             }
             hit.value = b.rp - best;
+            exact     = __any_sync( 0xffffffffu, exactLane );
             return hit;
         }
 
@@ -3337,20 +3447,58 @@ namespace sesgb
             }
         }
 
+        // First pass over the queries (in grid-cell order: neighbouring warps read the same atoms);
+        // a query that needs a double-precision decision is listed for k_sdf_exact instead
         template<bool kBackward>
         __global__ void __launch_bounds__( 32 * kSdfWarps, 8 ) k_sdf( Build b, const float * queries, uint32_t m, float band,
                                                                    float * sdf, const float * gradSdf, float * gradSorted,
-                                                                   int * kind, const uint32_t * order )
+                                                                   int * kind, const uint32_t * order, uint32_t * exactList,
+                                                                   uint32_t * exactCount )
         {
             __shared__ SdfSmem smem[ kSdfWarps ];
             const uint32_t     warp = threadIdx.x >> 5, lane = lane_id();
             uint32_t           overflow = 0;
-            // queries in grid-cell order: neighbouring warps read the same atoms
             for ( uint32_t qs = blockIdx.x * kSdfWarps + warp; qs < m; qs += gridDim.x * kSdfWarps )
             {
                 const uint32_t qi = order[ qs ];
                 const float3 x = make_float3( queries[ 3 * (size_t)qi ], queries[ 3 * (size_t)qi + 1 ], queries[ 3 * (size_t)qi + 2 ] );
-                const SdfHit h = sdf_query( b, x, smem[ warp ], band, overflow );
+                bool         exact;
+                const SdfHit h = sdf_query<false>( b, x, smem[ warp ], band, overflow, exact );
+                if ( lane == 0 )
+                {
+                    if ( exact )
+                        exactList[ atomicAdd( exactCount, 1u ) ] = qi;
+                    else if ( kBackward )
+                        sdf_gradient( b, h, x, gradSdf[ qi ], gradSorted );
+                    else
+                    {
+                        sdf[ qi ] = h.value;
+                        if ( kind )
+                            kind[ qi ] = h.kind;
+                    }
+                }
+            }
+            if ( lane == 0 && overflow )
+                atomicOr( &b.counts->overflow, (uint32_t)kOverflowSdfList );
+        }
+
+        // Second pass: the listed queries, with every decision within the float32 band taken in
+        // double precision (few queries: a point of dE next to another SAS sphere's surface)
+        template<bool kBackward>
+        __global__ void __launch_bounds__( 32 * kSdfWarps ) k_sdf_exact( Build b, const float * queries, float band, float * sdf,
+                                                                      const float * gradSdf, float * gradSorted, int * kind,
+                                                                      const uint32_t * exactList, const uint32_t * exactCount )
+        {
+            __shared__ SdfSmem smem[ kSdfWarps ];
+            const uint32_t     warp = threadIdx.x >> 5, lane = lane_id();
+            const uint32_t     count = *exactCount;
+            uint32_t           overflow = 0;
+            for ( uint32_t e = blockIdx.x * kSdfWarps + warp; e < count; e += gridDim.x * kSdfWarps )
+            {
+                const uint32_t qi = exactList[ e ];
+                const float3 x = make_float3( queries[ 3 * (size_t)qi ], queries[ 3 * (size_t)qi + 1 ], queries[ 3 * (size_t)qi + 2 ] );
+                bool         exact;
+                const SdfHit h = sdf_query<true>( b, x, smem[ warp ], band, overflow, exact );
                 if ( lane == 0 )
                 {
                     if ( kBackward )
@@ -3402,7 +3550,7 @@ namespace sesgb
                                 (float)__dadd_rn( eye[ 2 ], __dmul_rn( t, d.z ) ) );
         }
 
-        __global__ void __launch_bounds__( 32 * kSdfWarps, 8 ) k_trace( Build b, TraceParams p, float band, float * depth,
+        __global__ void __launch_bounds__( 32 * kSdfWarps ) k_trace( Build b, TraceParams p, float band, float * depth,
                                                                        float * normals )
         {
             __shared__ SdfSmem smem[ kSdfWarps ];
@@ -3430,7 +3578,8 @@ namespace sesgb
                 double hit = __longlong_as_double( 0x7ff0000000000000ll ); // +inf: background
                 for ( uint32_t step = 0; step < p.maxSteps && t <= p.tFar; step++ )
                 {
-                    const SdfHit h = sdf_query( b, ray_point( p.eye, d, t ), smem[ warp ], band, overflow );
+                    bool         ex;
+                    const SdfHit h = sdf_query<true>( b, ray_point( p.eye, d, t ), smem[ warp ], band, overflow, ex );
                     bool         stop;
                     const double adv = trace_step( h, rp, p.eps, stop );
                     if ( stop )
@@ -3459,7 +3608,8 @@ namespace sesgb
                                 q.y = (float)__dadd_rn( x.y, e );
                             else
                                 q.z = (float)__dadd_rn( x.z, e );
-                            v2[ sg ] = (double)sdf_query( b, q, smem[ warp ], band, overflow ).value;
+                            bool ex;
+                            v2[ sg ] = (double)sdf_query<true>( b, q, smem[ warp ], band, overflow, ex ).value;
                         }
                         g[ a ] = __ddiv_rn( __dsub_rn( v2[ 0 ], v2[ 1 ] ), __dmul_rn( 2.0, p.normalStep ) );
                     }
@@ -3484,7 +3634,14 @@ namespace sesgb
         }
     } // namespace
 
-    size_t sdf_scratch_bytes( uint32_t m ) { return 2 * ( ( (size_t)m * 4 + 255 ) & ~(size_t)255 ) + radix_scratch_bytes( m ); }
+    // keys and order of the queries, the list of queries for the exact pass and its counter, radix scratch
+    size_t sdf_scratch_bytes( uint32_t m ) { return 3 * ( ( (size_t)m * 4 + 255 ) & ~(size_t)255 ) + 256 + radix_scratch_bytes( m ); }
+
+    // the list of queries for the exact pass (m entries, then its counter)
+    static uint32_t * sdf_exact_list( void * scratch, uint32_t m )
+    {
+        return reinterpret_cast<uint32_t *>( static_cast<char *>( scratch ) + 2 * ( ( (size_t)m * 4 + 255 ) & ~(size_t)255 ) );
+    }
 
     // queries sorted by grid cell into `order` (scratch: sdf_scratch_bytes)
     static const uint32_t * sdf_order( const Build & b, const float * queries, uint32_t m, void * scratch, cudaStream_t s )
@@ -3492,7 +3649,7 @@ namespace sesgb
         char *     p     = static_cast<char *>( scratch );
         uint32_t * keys  = reinterpret_cast<uint32_t *>( p );
         uint32_t * order = reinterpret_cast<uint32_t *>( p + ( ( (size_t)m * 4 + 255 ) & ~(size_t)255 ) );
-        void *     rad   = p + 2 * ( ( (size_t)m * 4 + 255 ) & ~(size_t)255 );
+        void *     rad   = p + 3 * ( ( (size_t)m * 4 + 255 ) & ~(size_t)255 ) + 256;
         k_sdf_keys<<<min( persistent_blocks( 256 ), blocks_for( m, 256 ) ), 256, 0, s>>>( b, queries, m, keys, order );
         counted();
         radix_sort( keys, order, m, 32, rad, s );
@@ -3505,9 +3662,14 @@ namespace sesgb
         if ( !m )
             return;
         const uint32_t * order  = sdf_order( b, queries, m, scratch, s );
+        uint32_t *       list   = sdf_exact_list( scratch, m );
+        uint32_t *       count  = list + ( ( (size_t)m * 4 + 255 ) & ~(size_t)255 ) / 4;
         const uint32_t   blocks = min( persistent_blocks( 32 * kSdfWarps ) * 2, ( m + kSdfWarps - 1 ) / kSdfWarps );
-        k_sdf<false><<<blocks, 32 * kSdfWarps, 0, s>>>( b, queries, m, band, sdf, nullptr, nullptr, kind, order );
-        counted();
+        cudaMemsetAsync( count, 0, sizeof( uint32_t ), s );
+        k_sdf<false><<<blocks, 32 * kSdfWarps, 0, s>>>( b, queries, m, band, sdf, nullptr, nullptr, kind, order, list, count );
+        k_sdf_exact<false><<<min( blocks, 152u * 4u ), 32 * kSdfWarps, 0, s>>>( b, queries, band, sdf, nullptr, nullptr, kind, list,
+                                                                              count );
+        counted( 2 );
     }
     void launch_trace( const Build & b, const TraceParams & p, float band, float * depth, float * normals, cudaStream_t s )
     {
@@ -3526,9 +3688,15 @@ namespace sesgb
         if ( m )
         {
             const uint32_t * order  = sdf_order( b, queries, m, scratch, s );
+            uint32_t *       list   = sdf_exact_list( scratch, m );
+            uint32_t *       count  = list + ( ( (size_t)m * 4 + 255 ) & ~(size_t)255 ) / 4;
             const uint32_t   blocks = min( persistent_blocks( 32 * kSdfWarps ) * 2, ( m + kSdfWarps - 1 ) / kSdfWarps );
-            k_sdf<true><<<blocks, 32 * kSdfWarps, 0, s>>>( b, queries, m, band, nullptr, gradSdf, gradSorted, nullptr, order );
-            counted();
+            cudaMemsetAsync( count, 0, sizeof( uint32_t ), s );
+            k_sdf<true><<<blocks, 32 * kSdfWarps, 0, s>>>( b, queries, m, band, nullptr, gradSdf, gradSorted, nullptr, order, list,
+                                                           count );
+            k_sdf_exact<true><<<min( blocks, 152u * 4u ), 32 * kSdfWarps, 0, s>>>( b, queries, band, nullptr, gradSdf, gradSorted,
+                                                                                 nullptr, list, count );
+            counted( 2 );
         }
         if ( b.n )
         {
