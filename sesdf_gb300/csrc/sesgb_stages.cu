@@ -3531,25 +3531,11 @@ namespace sesgb
         // (every SES point lies at rp from E); outside (kinds 1, 2) value - rp bounds the distance
         // to the SAS, which holds the SES. A ray stops when an inside value falls below eps (a hit
         // at t), when it reaches a point deeper than the band (kind 0, taken as a hit), or when t
-        // passes tFar; it advances by at least eps / 4. Directions, ray points and the depth are
-        // evaluated in double precision with explicit rounding, in the order a host tracer writes
-        // them, so that the image does not depend on contraction choices. The normal of a hit is
-        // the normalised central difference of the signed distance (step normalStep).
-        __device__ __forceinline__ double trace_step( const SdfHit & h, double rp, double eps, bool & stop )
-        {
-            const bool   inside = h.kind == kSdfSphere || h.kind == kSdfCircle || h.kind == kSdfProbe;
-            const double v      = (double)h.value;
-            stop                = ( inside && v < eps ) || h.kind == kSdfClampInside;
-            const double step   = inside ? v : __dsub_rn( v, rp );
-            return fmax( step, __dmul_rn( 0.25, eps ) );
-        }
-
-        __device__ __forceinline__ float3 ray_point( const double eye[ 3 ], d3 d, double t )
-        {
-            return make_float3( (float)__dadd_rn( eye[ 0 ], __dmul_rn( t, d.x ) ), (float)__dadd_rn( eye[ 1 ], __dmul_rn( t, d.y ) ),
-                                (float)__dadd_rn( eye[ 2 ], __dmul_rn( t, d.z ) ) );
-        }
-
+        // passes tFar; it advances by at least eps / 4. The direction of a pixel is computed once
+        // in double precision and rounded to float32; the march (points eye + t d, steps, t) is in
+        // float32 with explicitly rounded operations, in the order a host tracer writes them, so
+        // that the image does not depend on contraction choices. The normal of a hit is the
+        // normalised central difference of the signed distance (step normalStep, double precision).
         __global__ void __launch_bounds__( 32 * kSdfWarps ) k_trace( Build b, TraceParams p, float band, float * depth,
                                                                        float * normals )
         {
@@ -3557,10 +3543,12 @@ namespace sesgb
             const uint32_t     warp = threadIdx.x >> 5, lane = lane_id();
             uint32_t           overflow = 0;
             const uint32_t     pixels   = p.width * p.height;
-            const double       rp       = (double)b.rp;
             const d3           f        = D3( p.forward[ 0 ], p.forward[ 1 ], p.forward[ 2 ] );
             const d3           r        = D3( p.right[ 0 ], p.right[ 1 ], p.right[ 2 ] );
             const d3           u        = D3( p.up[ 0 ], p.up[ 1 ], p.up[ 2 ] );
+            const float3       ef       = make_float3( (float)p.eye[ 0 ], (float)p.eye[ 1 ], (float)p.eye[ 2 ] );
+            const float        eps      = (float)p.eps, tFar = (float)p.tFar;
+            const float        minStep  = __fmul_rn( 0.25f, eps );
             for ( uint32_t px = blockIdx.x * kSdfWarps + warp; px < pixels; px += gridDim.x * kSdfWarps )
             {
                 const uint32_t iy = px / p.width, ix = px - iy * p.width;
@@ -3574,26 +3562,30 @@ namespace sesgb
                 d3           d   = dadd( dadd( f, dmul( r, xsw ) ), dmul( u, ys ) );
                 const double len = __dsqrt_rn( ddot( d, d ) );
                 d                = D3( __ddiv_rn( d.x, len ), __ddiv_rn( d.y, len ), __ddiv_rn( d.z, len ) );
-                double t   = p.tNear;
-                double hit = __longlong_as_double( 0x7ff0000000000000ll ); // +inf: background
-                for ( uint32_t step = 0; step < p.maxSteps && t <= p.tFar; step++ )
+                const float3 df  = make_float3( (float)d.x, (float)d.y, (float)d.z );
+                float        t   = (float)p.tNear;
+                float        hit = __int_as_float( 0x7f800000 ); // +inf: background
+                for ( uint32_t step = 0; step < p.maxSteps && t <= tFar; step++ )
                 {
+                    const float3 x = make_float3( __fadd_rn( ef.x, __fmul_rn( t, df.x ) ), __fadd_rn( ef.y, __fmul_rn( t, df.y ) ),
+                                                  __fadd_rn( ef.z, __fmul_rn( t, df.z ) ) );
                     bool         ex;
-                    const SdfHit h = sdf_query<true>( b, ray_point( p.eye, d, t ), smem[ warp ], band, overflow, ex );
-                    bool         stop;
-                    const double adv = trace_step( h, rp, p.eps, stop );
-                    if ( stop )
+                    const SdfHit h      = sdf_query<true>( b, x, smem[ warp ], band, overflow, ex );
+                    const bool   inside = h.kind == kSdfSphere || h.kind == kSdfCircle || h.kind == kSdfProbe;
+                    if ( ( inside && h.value < eps ) || h.kind == kSdfClampInside )
                     {
                         hit = t;
                         break;
                     }
-                    t = __dadd_rn( t, adv );
+                    const float st = inside ? h.value : __fsub_rn( h.value, b.rp );
+                    t              = __fadd_rn( t, fmaxf( st, minStep ) );
                 }
                 float3 nrm = make_float3( 0.f, 0.f, 0.f );
-                if ( normals && hit < 1e300 )
+                if ( normals && hit < 3.4e38f )
                 {
-                    const d3 x = D3( __dadd_rn( p.eye[ 0 ], __dmul_rn( hit, d.x ) ), __dadd_rn( p.eye[ 1 ], __dmul_rn( hit, d.y ) ),
-                                     __dadd_rn( p.eye[ 2 ], __dmul_rn( hit, d.z ) ) );
+                    const double hd = (double)hit;
+                    const d3 x = D3( __dadd_rn( p.eye[ 0 ], __dmul_rn( hd, d.x ) ), __dadd_rn( p.eye[ 1 ], __dmul_rn( hd, d.y ) ),
+                                     __dadd_rn( p.eye[ 2 ], __dmul_rn( hd, d.z ) ) );
                     double g[ 3 ];
                     for ( int a = 0; a < 3; a++ )
                     {
@@ -3620,7 +3612,7 @@ namespace sesgb
                 }
                 if ( lane == 0 )
                 {
-                    depth[ px ] = (float)hit;
+                    depth[ px ] = hit;
                     if ( normals )
                     {
                         normals[ 3 * (size_t)px ]     = nrm.x;

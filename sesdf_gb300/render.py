@@ -49,30 +49,34 @@ def camera_rays(eye, target, up, fov_deg: float, width: int, height: int):
 
 def sphere_trace(sdf_fn, origin, dirs, probe_radius: float, t_near: float, t_far: float, eps: float = 1e-3,
                  max_steps: int = 256):
-    """Depth t (float64 [m], inf where the ray misses) of the first SES point along origin + t * dirs.
+    """Depth t (float32 [m], inf where the ray misses) of the first SES point along origin + t * dirs.
     sdf_fn(points float32 [k, 3]) -> (value [k], kind [k]) as numpy arrays."""
     m = dirs.shape[0]
-    probe_radius = float(np.float32(probe_radius))  # the build's float32 probe radius
-    t = np.full(m, float(t_near))
-    depth = np.full(m, np.inf)
+    # the march is in float32 (the build's probe radius, float32 points, steps and depths)
+    rp32, eps32 = np.float32(probe_radius), np.float32(eps)
+    min_step = np.float32(0.25) * eps32
+    t = np.full(m, np.float32(t_near), np.float32)
+    t_far32 = np.float32(t_far)
+    depth = np.full(m, np.inf, np.float32)
     live = np.arange(m)
-    o = np.asarray(origin, np.float64)
+    o = np.asarray(origin, np.float64).astype(np.float32)
+    d32 = np.asarray(dirs, np.float64).astype(np.float32)
     for _ in range(max_steps):
         if live.size == 0:
             break
-        p = (o[None, :] + t[live, None] * dirs[live]).astype(np.float32)
+        p = o[None, :] + t[live, None] * d32[live]
         v, k = sdf_fn(p)
-        v = np.asarray(v, np.float64)
+        v = np.asarray(v, np.float32)
         k = np.asarray(k)
         inside = np.isin(k, INSIDE_SAS)
-        hit = inside & (v < eps)
+        hit = inside & (v < eps32)
         depth[live[hit]] = t[live[hit]]
-        step = np.where(inside, v, v - probe_radius)
+        step = np.where(inside, v, v - rp32)
         # deeper than the band (kind 0) cannot be reached with these steps; such a ray stops as a hit
         hit |= k == 0
         depth[live[k == 0]] = t[live[k == 0]]
-        t[live] += np.where(hit, 0.0, np.maximum(step, 0.25 * eps))
-        live = live[~hit & (t[live] <= t_far)]
+        t[live] += np.where(hit, np.float32(0.0), np.maximum(step, min_step)).astype(np.float32)
+        live = live[~hit & (t[live] <= t_far32)]
     return depth
 
 
@@ -115,7 +119,7 @@ def depth_image(sdf_fn, atoms, probe_radius: float, width: int = 128, height: in
     nrm = np.zeros((width * height, 3))
     hit = np.isfinite(depth)
     if with_normals and hit.any():
-        nrm[hit] = normals(sdf_fn, eye[None, :] + depth[hit, None] * dirs[hit])
+        nrm[hit] = normals(sdf_fn, eye[None, :] + depth[hit, None].astype(np.float64) * dirs[hit])
     return depth.reshape(height, width).astype(np.float32), nrm.reshape(height, width, 3).astype(np.float32)
 
 
