@@ -2959,12 +2959,13 @@ namespace sesgb
         }
 
         // Float32 error bound of |q - c_k|^2 - R_k^2 for a point q computed in absolute float32
-        // coordinates: a few ulps of |q| on every coordinate, times 2 |q - c_k|, plus the rounding of
-        // the squares. Inside it the test is taken again in double precision.
-        __device__ __forceinline__ float hidden_band( float3 q, float d2, float Rk )
+        // coordinates: a few ulps of the coordinates (at most qQ / 4, the query's largest coordinate
+        // plus its reach) on every coordinate, times 2 |q - c_k| (taken as R_k: the bound matters only
+        // where |q - c_k| is close to R_k), plus the rounding of the squares. Inside it the test is
+        // taken again in double precision.
+        __device__ __forceinline__ float hidden_band( float qQ, float d2, float Rk )
         {
-            const float Q = fmaxf( fabsf( q.x ), fmaxf( fabsf( q.y ), fabsf( q.z ) ) );
-            return 3.8147e-6f * ( d2 + Rk * Rk + 4.f * Q * sqrtf( d2 ) + 1.f );
+            return 3.8147e-6f * ( d2 + Rk * ( Rk + qQ ) + 1.f );
         }
 
         // point q (double) strictly inside the SAS sphere of atom k, in double precision
@@ -3034,6 +3035,8 @@ namespace sesgb
             const uint32_t lane      = lane_id();
             bool           exactLane = false;
             exact                    = false;
+            // 4 x (largest coordinate of any point of dE this query examines)
+            const float qQ = 4.f * ( fmaxf( fabsf( x.x ), fmaxf( fabsf( x.y ), fabsf( x.z ) ) ) + 12.f );
             const float    T    = b.rp + band;
             const FineGrid g    = b.fine[ 0 ];
             Rows           rows;
@@ -3238,7 +3241,7 @@ namespace sesgb
                             const float  dx = q.x - nk.x, dy = q.y - nk.y, dz = q.z - nk.z;
                             const float  d2 = dx * dx + dy * dy + dz * dz;
                             const float  m  = d2 - nk.w * nk.w;
-                            const float  eb = hidden_band( q, d2, nk.w );
+                            const float  eb = hidden_band( qQ, d2, nk.w );
                             hidden          = hidden || m < -eb;
                             unsure          = unsure || !( fabsf( m ) > eb );
                         }
@@ -3305,7 +3308,7 @@ namespace sesgb
                             const float  dx = q.x - nk.x, dy = q.y - nk.y, dz = q.z - nk.z;
                             const float  d2 = dx * dx + dy * dy + dz * dz;
                             const float  m  = d2 - nk.w * nk.w;
-                            const float  eb = hidden_band( q, d2, nk.w );
+                            const float  eb = hidden_band( qQ, d2, nk.w );
                             hidden          = m < -eb;
                             unsure          = unsure || !( fabsf( m ) > eb );
                         }

@@ -489,6 +489,8 @@ def compare_sorted(ref: dict, gpu: dict, rp: float, mode: str) -> dict:
             dmin = min(np.linalg.norm(pg[a] - pg[b]) for a in range(len(on)) for b in range(a + 1, len(on)))
             return dmin < 4.0 * err
         unexp = 0
+        seg_cases = []
+        in_ref = set(rows_r.view(vt).ravel().tolist())
         for v in sdiff:
             r = np.frombuffer(v.tobytes(), np.int64)
             if circle_tainted(int(r[0]), int(r[1])) or int(r[2]) in bad_probe_keys or int(r[3]) in bad_probe_keys:
@@ -496,6 +498,13 @@ def compare_sorted(ref: dict, gpu: dict, rp: float, mode: str) -> dict:
             if order_in_band(int(r[0]), int(r[1])):
                 continue
             unexp += 1
+            if len(seg_cases) < 10:
+                on = np.flatnonzero(((g0 == r[0]) | (g1 == r[0]) | (g2 == r[0])) & ((g0 == r[1]) | (g1 == r[1]) | (g2 == r[1])))
+                seg_cases.append({"circle": [int(gpu["perm"][r[0]]), int(gpu["perm"][r[1]])], "side": "ref" if v in in_ref else "gpu",
+                                  "probes": [list(map(int, gpu["perm"][list(_decode_probe_key(int(k), n)[0])])) + [_decode_probe_key(int(k), n)[1]]
+                                             for k in (r[2], r[3])],
+                                  "circle_probes_gpu": int(len(on))})
+        rep["segment_cases"] = seg_cases
         rep["segments"] = int(len(rows_g))
         rep["segment_mismatch"] = int(len(sdiff))
         rep["segment_unexplained"] = unexp
