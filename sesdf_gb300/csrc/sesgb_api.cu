@@ -353,7 +353,9 @@ namespace
 
         // G: neighbours of singular probes
         mark( 8 );
-        launch_fine_params( b, 2.f * c->rp + 0.01f, 0, s, b.nbrSpan );
+        // singular probes are sparse in the atoms' box: their grid stays on cutoff cells (a half-cutoff
+        // grid hits the cell capacity and is coarsened; measured slower)
+        launch_fine_params( b, 2.f * c->rp + 0.01f, 0, s, 1 );
         launch_cells( b, 1, b.capProbes, &d->Q, sc, s );
         launch_probe_neighbors( b, s );
 
