@@ -17,11 +17,13 @@
 // the legacy default stream. Deviations, each needed to run it safely:
 //   * launches with zero elements are skipped (KernelConfig::From divides by
 //     zero for them, sesdf/include/bcs/cuda/setup.inl:21-25);
-//   * the temporary intersection buffer is sized N*128 instead of C1*2 and the
+//   * the temporary intersection buffer is sized N*(slots per atom) instead of C1*2 and the
 //     intersection buffer gets a tail of Q*16 bytes, so that the reference
 //     kernels' unchecked writes stay inside allocations;
 //   * the exterior status buffer is zeroed once at construction (the
 //     reference leaves its j < i slots as whatever cudaMalloc returned).
+// One harness serves both libraries the reference builds (128 and 288 neighbour
+// slots per atom, sesdf/CMakeLists.txt:96-117): the capacity is chosen per build.
 // The structs below mirror the reference's kernel parameter layouts
 // (sesdf/include/bcs/cuda/grid.cuh:9-16, sesdf/include/bcs/sesdf/data.cuh:27-115,
 // sesdf/include/bcs/ssesdf/data.cuh:27-92); their sizes are checked against the
@@ -105,7 +107,9 @@ namespace
         uint8_t *  visibilityStatus;
     };
 
-    constexpr uint32_t kMaxNbr       = 128; // BCS_SESDF_MAXNEIGHBORPERATOM
+    // BCS_SESDF_MAXNEIGHBORPERATOM of the two libraries the reference builds (sesdf/CMakeLists.txt:96-117)
+    constexpr uint32_t kMaxNbr       = 128;
+    constexpr uint32_t kMaxNbr288    = 288;
     constexpr uint32_t kMaxIntNbr    = 32;
     constexpr uint32_t kMeanIntPerC  = 2;
 
@@ -126,6 +130,9 @@ namespace
         kXFillIntersections,
         kXFillCircles,
         kXIntNeighbors,
+        kSectors288,
+        kFindIntersections288,
+        kXFindIntersections288,
         kCount
     };
 
@@ -146,6 +153,9 @@ namespace
         "bcs::ssesdf::fillIntersections(",
         "bcs::ssesdf::fillCircles(",
         "bcs::ssesdf::findIntersectionsNeighbors(",
+        "bcs::sesdf::buildConvexPatchesSectors<288u>(",
+        "bcs::sesdf::findIntersectionsBetweenCircles<288u>(",
+        "bcs::ssesdf::findIntersectionsBetweenCircles<288u>(",
     };
 
     CUlibrary  g_lib = nullptr;
@@ -299,6 +309,7 @@ namespace
     struct Ref
     {
         int            mode = 0; // 0 full, 1 exterior
+        uint32_t       maxNbr = kMaxNbr; // neighbour slots per atom: 128 or 288 (the library the kernels come from)
         const float *  hostAtoms = nullptr;
         uint32_t       n  = 0;
         float          rp = 1.4f;
@@ -356,10 +367,10 @@ namespace
             r->convexPatches = DBuf( sizeof( uint2 ) * N );
         r->atomIndices = DBuf( sizeof( uint32_t ) * N );
         r->nbrCount    = DBuf( sizeof( uint32_t ) * N );
-        r->nbrIds      = DBuf( sizeof( uint32_t ) * kMaxNbr * N );
-        r->status      = DBuf( kMaxNbr * N + 1, r->mode == 1 );
+        r->nbrIds      = DBuf( sizeof( uint32_t ) * r->maxNbr * N );
+        r->status      = DBuf( r->maxNbr * N + 1, r->mode == 1 );
         if ( r->mode == 0 )
-            r->globalToTrimmed = DBuf( sizeof( uint32_t ) * ( kMaxNbr * N + 1 ) );
+            r->globalToTrimmed = DBuf( sizeof( uint32_t ) * ( r->maxNbr * N + 1 ) );
 
         cudaMemPool_t pool;
         int           dev = 0;
@@ -380,7 +391,7 @@ namespace
         c.neighborNb                 = r->nbrCount.get<uint32_t>();
         c.neighborIds                = r->nbrIds.get<uint32_t>();
         c.visibilityStatus           = r->status.get<uint8_t>();
-        c.maxNeighborPerAtom         = kMaxNbr;
+        c.maxNeighborPerAtom         = r->maxNbr;
         c.maxIntersectionsPerCircles = kMeanIntPerC;
         c.maxIntersectionNeighbors   = kMaxIntNbr;
         c.globalToTrimmedId          = r->globalToTrimmed.get<uint32_t>();
@@ -410,7 +421,7 @@ namespace
         *ctx.hSegmentCount    = 0;
         *ctx.hVisibleCircleNb = 0;
         const uint32_t N      = r->n;
-        const uint64_t slots  = (uint64_t)N * kMaxNbr;
+        const uint64_t slots  = (uint64_t)N * r->maxNbr;
 
         // #1 H2D
         cudaMemcpy( ctx.atoms, r->hostAtoms, sizeof( float4 ) * N, cudaMemcpyHostToDevice );
@@ -424,14 +435,14 @@ namespace
             uint32_t         g, b;
             const uint32_t * cs = r->grid.start.get<uint32_t>();
             const uint32_t * ce = r->grid.end.get<uint32_t>();
-            kernelConfig( N, kMaxNbr, g, b );
+            kernelConfig( N, r->maxNbr, g, b );
             if ( N && !launch( kFindCircles, g, b, 0, r->gridInfo, cs, ce, ctx ) )
                 return false;
         }
         DBuf       temp( slots * sizeof( uint2 ) + ( slots + 1 ) * sizeof( uint32_t ), true );
         uint32_t * mask            = temp.get<uint32_t>( slots * sizeof( uint2 ) );
         uint2 *    tempFullCircles = temp.get<uint2>();
-        if ( N && !launch( kVisibility, N, kMaxNbr, kMaxNbr * sizeof( float4 ), ctx, tempFullCircles, mask ) )
+        if ( N && !launch( kVisibility, N, r->maxNbr, r->maxNbr * sizeof( float4 ), ctx, tempFullCircles, mask ) )
             return false;
 
         // prefixSumCount (memory.inl:26-49)
@@ -454,7 +465,7 @@ namespace
         {
             uint2 *  convex  = r->convexPatches.get<uint2>();
             float4 * sectors = r->fCircleAndSectors.get<float4>( *ctx.hFullCircleNb * sizeof( uint2 ) + alignment );
-            if ( !launch( kSectors, N, kMaxNbr, 0, ctx, mask, convex, sectors ) )
+            if ( !launch( r->maxNbr == kMaxNbr288 ? kSectors288 : kSectors, N, r->maxNbr, 0, ctx, mask, convex, sectors ) )
                 return false;
         }
         if ( *ctx.hFullCircleNb > 0 )
@@ -478,7 +489,7 @@ namespace
             {
                 DBuf   tempIds( sizeof( int4 ) * std::max<uint64_t>( (uint64_t)C1 * kMeanIntPerC, slots ) );
                 int4 * tids = tempIds.get<int4>();
-                if ( !launch( kFindIntersections, N, kMaxNbr, 0, ctx, tids ) )
+                if ( !launch( r->maxNbr == kMaxNbr288 ? kFindIntersections288 : kFindIntersections, N, r->maxNbr, 0, ctx, tids ) )
                     return false;
                 d2h( ctx.hIntersectionNb, ctx.dIntersectionNb, 1 );
                 const uint32_t I = *ctx.hIntersectionNb;
@@ -573,7 +584,7 @@ namespace
         ctx.neighborNb                 = r->nbrCount.get<uint32_t>();
         ctx.neighborIds                = r->nbrIds.get<uint32_t>();
         ctx.visibilityStatus           = r->status.get<uint8_t>();
-        ctx.maxNeighborPerAtom         = kMaxNbr;
+        ctx.maxNeighborPerAtom         = r->maxNbr;
         ctx.maxIntersectionsPerCircles = 2;
         ctx.maxIntersectionNeighbors   = kMaxIntNbr;
         ctx.dIntersectionNb            = r->dIntersectionNb;
@@ -583,7 +594,7 @@ namespace
         ctx.hVisibleCircleNb  = r->hVisibleCircleNb;
         *ctx.hVisibleCircleNb = 0;
         const uint32_t N      = r->n;
-        const uint64_t slots  = (uint64_t)N * kMaxNbr;
+        const uint64_t slots  = (uint64_t)N * r->maxNbr;
 
         cudaMemcpy( ctx.atoms, r->hostAtoms, sizeof( float4 ) * N, cudaMemcpyHostToDevice );
 
@@ -596,11 +607,11 @@ namespace
             uint32_t         g, b;
             const uint32_t * cs = r->grid.start.get<uint32_t>();
             const uint32_t * ce = r->grid.end.get<uint32_t>();
-            kernelConfig( N, kMaxNbr, g, b );
+            kernelConfig( N, r->maxNbr, g, b );
             if ( N && !launch( kXFindCircles, g, b, 0, r->gridInfo, cs, ce, ctx ) )
                 return false;
         }
-        if ( N && !launch( kXVisibility, N, kMaxNbr, kMaxNbr * sizeof( float4 ), ctx ) )
+        if ( N && !launch( kXVisibility, N, r->maxNbr, r->maxNbr * sizeof( float4 ), ctx ) )
             return false;
         *ctx.hVisibleCircleNb
             = (uint32_t)thrust::count_if( thrust::device, ctx.visibilityStatus, ctx.visibilityStatus + slots, NonZeroU8() );
@@ -616,7 +627,7 @@ namespace
             {
                 DBuf   tempIds( sizeof( int4 ) * std::max<uint64_t>( (uint64_t)ctx.intersectedCircleNb * 2, slots ) );
                 int4 * tids = tempIds.get<int4>();
-                if ( !launch( kXFindIntersections, N, kMaxNbr, 0, ctx, tids ) )
+                if ( !launch( r->maxNbr == kMaxNbr288 ? kXFindIntersections288 : kXFindIntersections, N, r->maxNbr, 0, ctx, tids ) )
                     return false;
                 d2h( ctx.hIntersectionNb, ctx.dIntersectionNb, 1 );
                 const uint32_t I = *ctx.hIntersectionNb;
@@ -753,9 +764,15 @@ extern "C"
 
     // Constructs the reference object (the host atoms are borrowed, as the
     // reference's ConstSpan is).
-    void * sesref_create( const float * atoms, uint32_t n, const float * aabb, float rp, int mode )
+    void * sesref_create_cap( const float * atoms, uint32_t n, const float * aabb, float rp, int mode, uint32_t maxNbr )
     {
+        if ( maxNbr != kMaxNbr && maxNbr != kMaxNbr288 )
+        {
+            g_err = "neighbour slots per atom: 128 or 288";
+            return nullptr;
+        }
         Ref * r       = new Ref();
+        r->maxNbr     = maxNbr;
         r->mode       = mode;
         r->hostAtoms  = atoms;
         r->n          = n;
@@ -763,6 +780,11 @@ extern "C"
         construct( r, aabb );
         cudaDeviceSynchronize();
         return r;
+    }
+
+    void * sesref_create( const float * atoms, uint32_t n, const float * aabb, float rp, int mode )
+    {
+        return sesref_create_cap( atoms, n, aabb, rp, mode, kMaxNbr );
     }
 
     int sesref_build( void * h )
@@ -824,11 +846,11 @@ extern "C"
         else if ( s == "nbr_count" )
             src = r->nbrCount.p, need = 4 * N;
         else if ( s == "nbr_ids" )
-            src = r->nbrIds.p, need = 4 * N * kMaxNbr;
+            src = r->nbrIds.p, need = 4 * N * r->maxNbr;
         else if ( s == "status" )
-            src = r->status.p, need = N * kMaxNbr;
+            src = r->status.p, need = N * r->maxNbr;
         else if ( s == "global_to_trimmed" && r->mode == 0 )
-            src = r->globalToTrimmed.p, need = 4 * ( N * kMaxNbr + 1 );
+            src = r->globalToTrimmed.p, need = 4 * ( N * r->maxNbr + 1 );
         else if ( s == "convex" && r->mode == 0 )
             src = r->convexPatches.p, need = 8 * N;
         else if ( s == "full_circles" && r->mode == 0 )

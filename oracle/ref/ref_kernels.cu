@@ -14,6 +14,8 @@
 //   bcs::sesdf::findIntersectionsBetweenCircles<128>      sesdf/include/bcs/sesdf/operations.inl:230-486
 //   bcs::sesdf::buildSegments<256,16>                     sesdf/include/bcs/sesdf/operations.inl:552-668
 //   bcs::ssesdf::* (exterior twins)                       sesdf/src/ssesdf/operations.cu, sesdf/include/bcs/ssesdf/operation.inl
+// The templates are instantiated for both capacities the reference builds (sesdf/CMakeLists.txt:96-117:
+// the default library with 128 neighbour slots per atom, sesdf288 with 288).
 #include "src/cuda/grid.cu"
 #include "src/sesdf/operations.cu"
 #include "src/ssesdf/operations.cu"
@@ -24,6 +26,8 @@ namespace bcs
     {
         template __global__ void findIntersectionsBetweenCircles<128u>( SesdfContext, int4 * );
         template __global__ void buildConvexPatchesSectors<128u>( SesdfContext, const uint32_t * const, uint2 *, float4 * );
+        template __global__ void findIntersectionsBetweenCircles<288u>( SesdfContext, int4 * );
+        template __global__ void buildConvexPatchesSectors<288u>( SesdfContext, const uint32_t * const, uint2 *, float4 * );
         template __global__ void buildSegments<256, 16>( const SesdfContext,
                                                          const uint32_t,
                                                          const uint32_t *,
@@ -35,5 +39,6 @@ namespace bcs
     namespace ssesdf
     {
         template __global__ void findIntersectionsBetweenCircles<128u>( SsesdfContext, int4 * );
+        template __global__ void findIntersectionsBetweenCircles<288u>( SsesdfContext, int4 * );
     } // namespace ssesdf
 } // namespace bcs

@@ -60,6 +60,9 @@ def _load():
         lib.sesref_error.restype = ctypes.c_char_p
         lib.sesref_create.restype = ctypes.c_void_p
         lib.sesref_create.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_float, ctypes.c_int]
+        lib.sesref_create_cap.restype = ctypes.c_void_p
+        lib.sesref_create_cap.argtypes = [ctypes.c_void_p, ctypes.c_uint32, ctypes.c_void_p, ctypes.c_float, ctypes.c_int,
+                                          ctypes.c_uint32]
         lib.sesref_build.argtypes = [ctypes.c_void_p]
         lib.sesref_time.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
         lib.sesref_counts.argtypes = [ctypes.c_void_p, ctypes.c_void_p]
@@ -81,8 +84,14 @@ MAX_NBR = 128
 class RefBuild:
     """One reference object (bcs::Sesdf or bcs::Ssesdf) on the reference kernels."""
 
-    def __init__(self, atoms: np.ndarray, probe_radius: float = 1.4, mode: str = "full", box=None):
+    def __init__(self, atoms: np.ndarray, probe_radius: float = 1.4, mode: str = "full", box=None,
+                 max_nbr: int = MAX_NBR):
+        """max_nbr: neighbour slots per atom, 128 (the reference's sesdf library) or 288 (its sesdf288
+        library, sesdf/CMakeLists.txt:96-117)."""
+        if max_nbr not in (128, 288):
+            raise ValueError("max_nbr: 128 or 288")
         self.lib = _load()
+        self.max_nbr = max_nbr
         self.atoms = np.ascontiguousarray(np.asarray(atoms, np.float32).reshape(-1, 4))
         self.mode = mode
         if box is None:
@@ -90,8 +99,10 @@ class RefBuild:
             hi = (self.atoms[:, :3] + self.atoms[:, 3:4]).max(0)
             box = np.concatenate([lo, hi])
         self.box = np.ascontiguousarray(box, np.float32)
-        self.h = self.lib.sesref_create(self.atoms.ctypes.data, self.atoms.shape[0], self.box.ctypes.data,
-                                        ctypes.c_float(probe_radius), 0 if mode == "full" else 1)
+        self.h = self.lib.sesref_create_cap(self.atoms.ctypes.data, self.atoms.shape[0], self.box.ctypes.data,
+                                            ctypes.c_float(probe_radius), 0 if mode == "full" else 1, max_nbr)
+        if not self.h:
+            raise RuntimeError("reference object: " + self.lib.sesref_error().decode())
 
     def build(self):
         if self.lib.sesref_build(self.h) != 0:
@@ -121,13 +132,13 @@ class RefBuild:
         out = {"counts": c, "atoms": self._get("atoms", n, np.float32, 4),
                "perm": self._get("atom_indices", n, np.uint32),
                "nbr_count": self._get("nbr_count", n, np.uint32),
-               "nbr_ids": self._get("nbr_ids", n * MAX_NBR, np.uint32).reshape(n, MAX_NBR),
-               "status": self._get("status", n * MAX_NBR, np.uint8).reshape(n, MAX_NBR),
+               "nbr_ids": self._get("nbr_ids", n * self.max_nbr, np.uint32).reshape(n, self.max_nbr),
+               "status": self._get("status", n * self.max_nbr, np.uint8).reshape(n, self.max_nbr),
                "probe_ids": self._get("int_ids", c["I"], np.int32, 4),
                "probe_pos": self._get("int_pos", c["I"], np.float32, 4),
                "probe_nbrs": self._get("int_nbrs", 32 * c["Q"], np.float32, 4)}
         if self.mode == "full":
-            out["global_to_trimmed"] = self._get("global_to_trimmed", n * MAX_NBR + 1, np.uint32)
+            out["global_to_trimmed"] = self._get("global_to_trimmed", n * self.max_nbr + 1, np.uint32)
             out["convex"] = self._get("convex", n, np.uint32, 2)
             out["full"] = self._get("full_circles", c["F"], np.uint32, 2)
             out["sectors"] = self._get("sectors", c["V"], np.float32, 4)

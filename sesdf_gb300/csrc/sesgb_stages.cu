@@ -1485,21 +1485,26 @@ namespace sesgb
             const float4    ai  = b.atoms[ i ];
             const float     Ri  = ai.w + b.rp;
             const size_t    row = (size_t)i * b.cap;
+            const uint32_t  po  = b.pairOff[ i ];
 
             const bool useMask = ni <= (uint32_t)kMaskSlots;
             uint32_t   p       = 0;
             uint64_t   partial = 0; // slots of the partial circles (i, j), i < j
             float      d2max = 0.f, bmax = 0.f;
-            for ( uint32_t base0 = 0; base0 < ni; base0 += 64 )
+            // two rows of 32 neighbours at a time. The rows (ids, statuses) are read up to the
+            // capacity without waiting for the count (slots past it are not used), so that they
+            // travel with the atom's own loads; the neighbours' atoms, counts and touch masks
+            // follow together: two round trips to memory for an atom of up to 64 neighbours
+            for ( uint32_t base0 = 0; base0 == 0 || base0 < ni; base0 += 64 )
             {
-                // two rows of 32 neighbours: the loads of both issued before their use
                 uint32_t jj[ 2 ] = { 0u, 0u }, st[ 2 ] = { 0u, 0u }, cn[ 2 ] = { 0u, 0u };
                 float4   aa[ 2 ];
+                uint64_t tm[ 2 ] = { ~0ull, ~0ull };
 #pragma unroll
                 for ( int h = 0; h < 2; h++ )
                 {
                     const uint32_t s = base0 + 32 * h + lane;
-                    if ( s < ni )
+                    if ( s < b.cap )
                     {
                         jj[ h ] = b.nbr[ row + s ];
                         st[ h ] = b.status[ row + s ];
@@ -1513,6 +1518,10 @@ namespace sesgb
                     {
                         aa[ h ] = b.atoms[ jj[ h ] ];
                         cn[ h ] = b.nbrCount[ jj[ h ] ];
+                        // past the touch buffer's capacity (a build that overflowed P and is built
+                        // again) every neighbour counts as touching
+                        if ( useMask && po + s < b.capPairs )
+                            tm[ h ] = b.touch[ po + s ];
                     }
                 }
 #pragma unroll
@@ -1536,12 +1545,7 @@ namespace sesgb
                         m.full[ s ]       = cn[ h ] >= b.cap;
                         isP               = st[ h ] == 1 && i < j;
                         if ( isP && useMask )
-                        {
-                            // past the touch buffer's capacity (a build that overflowed P and is built
-                            // again) every neighbour counts as touching
-                            const uint32_t at = b.pairOff[ i ] + s;
-                            m.touch[ s ]      = at < b.capPairs ? b.touch[ at ] : ~0ull;
-                        }
+                            m.touch[ s ] = tm[ h ];
                         d2max = fmaxf( d2max, dd );
                         bmax  = fmaxf( bmax, Ri * Ri + dd + Rl * Rl );
                     }

@@ -23,5 +23,5 @@ def test_launch_list_summary():
     text = open(os.path.join(ROOT, "profiles", "launches_assembly100k_full.md")).read()
     assert "--clock-control none" in text
     rows = [ln for ln in text.splitlines() if ln.startswith("| k_")]
-    names = {ln.split("|")[1].strip() for ln in rows}
+    names = {ln.split("|")[1].strip().split("<")[0] for ln in rows}
     assert {"k_probes", "k_visibility", "k_neighbors"} <= names

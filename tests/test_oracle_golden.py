@@ -24,7 +24,8 @@ def test_oracle_matches_reference_kernels(path):
     name = os.path.basename(path)[:-4]
     mode = "full" if name.endswith("_full") else "exterior"
     atoms, box, rp = g["atoms"], g["box"], float(g["probe_radius"])
-    o = oracle.run(atoms, rp, mode, box=box)
+    cap = int(g["max_nbr"]) if "max_nbr" in g else 128
+    o = oracle.run(atoms, rp, mode, box=box, max_nbr=cap)
     rep = refcompare.compare(atoms, rp, mode, g, o)
     print(name, rep)
     assert rep["nbr_unexplained"] == 0
