@@ -579,7 +579,7 @@ REF_D2H_BYTES_EXTERIOR = 4 + 5 * 8
 def run_profile_case(args):
     """One on-demand workload of the 20,000-atom globule, args.steps times after args.warmup, for
     profiler runs (no JSON line): sdf (forward and adjoint at 200,000 of the 1M queries), area
-    (SES area and its adjoint), render (512 x 512 image), cavities (0.5 A voxels)."""
+    (SES area and its adjoint), render (512 x 512 depth and normal image, as timed), cavities (0.5 A voxels)."""
     import torch
     from sesdf_gb300 import SesBuild, render, synth
     atoms, q = synth.sdf_workload()
@@ -593,6 +593,7 @@ def run_profile_case(args):
     gs = torch.ones(m, dtype=torch.float32, device="cuda")
     ga = torch.empty((atoms.shape[0], 4), dtype=torch.float32, device="cuda")
     depth = torch.empty(512 * 512, dtype=torch.float32, device="cuda")
+    nrm = torch.empty(3 * 512 * 512, dtype=torch.float32, device="cuda")
     eye, centre, up, t_near, t_far = render.framing(atoms, RP)
     f, r, u = render.camera_basis(eye, centre, up)
     cam = dict(eye=eye, forward=f, right=r, up=u, tan_half_fov=float(np.tan(np.radians(20.0))), t_near=float(t_near),
@@ -606,7 +607,7 @@ def run_profile_case(args):
             g.ses_area(None, stream.cuda_stream)
             g.ses_area_backward(ga.data_ptr(), (1.0, 1.0, 1.0), stream.cuda_stream)
         elif args.profile_case == "render":
-            g.render(cam, depth.data_ptr(), None, stream.cuda_stream)
+            g.render(cam, depth.data_ptr(), nrm.data_ptr(), stream.cuda_stream)
         elif args.profile_case == "cavities":
             g.cavities(0.5)
     for _ in range(args.warmup + args.steps):

@@ -302,7 +302,8 @@ int sesgb_sdf_backward( sesgb_ctx * ctx, const float * device_queries, uint32_t 
  * is below eps (or deeper than the band), at t_far, or after max_steps evaluations.
  * device_depth: float[width * height], t of the hit or +inf; device_normals (may be
  * NULL): float3 per pixel, the normalised central difference of the signed distance
- * (step normal_step) at the hit, 0 for a miss. Ray arithmetic is in double precision. */
+ * (step normal_step) at the hit, 0 for a miss. Ray setup, march and normals are in
+ * float32, every operation rounded on its own in the order written above. */
 typedef struct sesgb_camera
 {
     double   eye[ 3 ];

@@ -3538,11 +3538,11 @@ namespace sesgb
         // (every SES point lies at rp from E); outside (kinds 1, 2) value - rp bounds the distance
         // to the SAS, which holds the SES. A ray stops when an inside value falls below eps (a hit
         // at t), when it reaches a point deeper than the band (kind 0, taken as a hit), or when t
-        // passes tFar; it advances by at least eps / 4. The direction of a pixel is computed once
-        // in double precision and rounded to float32; the march (points eye + t d, steps, t) is in
-        // float32 with explicitly rounded operations, in the order a host tracer writes them, so
-        // that the image does not depend on contraction choices. The normal of a hit is the
-        // normalised central difference of the signed distance (step normalStep, double precision).
+        // passes tFar; it advances by at least eps / 4. The ray setup, the march (points eye + t d,
+        // steps, t) and the normals are in float32 with every operation rounded on its own, in the
+        // order the host tracer writes them, so that the image does not depend on contraction
+        // choices. The normal of a hit is the normalised central difference of the signed distance
+        // (step normalStep) at the hit point.
         __global__ void __launch_bounds__( 32 * kSdfWarps ) k_trace( Build b, TraceParams p, float band, float * depth,
                                                                        float * normals )
         {
@@ -3550,26 +3550,27 @@ namespace sesgb
             const uint32_t     warp = threadIdx.x >> 5, lane = lane_id();
             uint32_t           overflow = 0;
             const uint32_t     pixels   = p.width * p.height;
-            const d3           f        = D3( p.forward[ 0 ], p.forward[ 1 ], p.forward[ 2 ] );
-            const d3           r        = D3( p.right[ 0 ], p.right[ 1 ], p.right[ 2 ] );
-            const d3           u        = D3( p.up[ 0 ], p.up[ 1 ], p.up[ 2 ] );
+            const float3       f        = make_float3( (float)p.forward[ 0 ], (float)p.forward[ 1 ], (float)p.forward[ 2 ] );
+            const float3       r        = make_float3( (float)p.right[ 0 ], (float)p.right[ 1 ], (float)p.right[ 2 ] );
+            const float3       u        = make_float3( (float)p.up[ 0 ], (float)p.up[ 1 ], (float)p.up[ 2 ] );
             const float3       ef       = make_float3( (float)p.eye[ 0 ], (float)p.eye[ 1 ], (float)p.eye[ 2 ] );
-            const float        eps      = (float)p.eps, tFar = (float)p.tFar;
+            const float        th       = (float)p.tanHalfFov, W = (float)p.width, H = (float)p.height;
+            const float        eps      = (float)p.eps, tFar = (float)p.tFar, hn = (float)p.normalStep;
             const float        minStep  = __fmul_rn( 0.25f, eps );
             for ( uint32_t px = blockIdx.x * kSdfWarps + warp; px < pixels; px += gridDim.x * kSdfWarps )
             {
                 const uint32_t iy = px / p.width, ix = px - iy * p.width;
                 // pinhole ray through the pixel centre, row-major from the top left
-                const double xs = __dmul_rn( __dmul_rn( __dsub_rn( __ddiv_rn( __dmul_rn( 2.0, __dadd_rn( (double)ix, 0.5 ) ),
-                                                                              (double)p.width ), 1.0 ), p.tanHalfFov ),
-                                             (double)p.width );
-                const double xsw = __ddiv_rn( xs, (double)p.height );
-                const double ys  = __dmul_rn( __dsub_rn( 1.0, __ddiv_rn( __dmul_rn( 2.0, __dadd_rn( (double)iy, 0.5 ) ),
-                                                                         (double)p.height ) ), p.tanHalfFov );
-                d3           d   = dadd( dadd( f, dmul( r, xsw ) ), dmul( u, ys ) );
-                const double len = __dsqrt_rn( ddot( d, d ) );
-                d                = D3( __ddiv_rn( d.x, len ), __ddiv_rn( d.y, len ), __ddiv_rn( d.z, len ) );
-                const float3 df  = make_float3( (float)d.x, (float)d.y, (float)d.z );
+                const float xs  = __fdiv_rn( __fmul_rn( __fmul_rn( __fsub_rn( __fdiv_rn( __fmul_rn( 2.f, __fadd_rn( (float)ix, 0.5f ) ), W ), 1.f ),
+                                                                  th ),
+                                                        W ),
+                                             H );
+                const float ys  = __fmul_rn( __fsub_rn( 1.f, __fdiv_rn( __fmul_rn( 2.f, __fadd_rn( (float)iy, 0.5f ) ), H ) ), th );
+                const float dx  = __fadd_rn( __fadd_rn( f.x, __fmul_rn( r.x, xs ) ), __fmul_rn( u.x, ys ) );
+                const float dy  = __fadd_rn( __fadd_rn( f.y, __fmul_rn( r.y, xs ) ), __fmul_rn( u.y, ys ) );
+                const float dz  = __fadd_rn( __fadd_rn( f.z, __fmul_rn( r.z, xs ) ), __fmul_rn( u.z, ys ) );
+                const float len = __fsqrt_rn( __fadd_rn( __fadd_rn( __fmul_rn( dx, dx ), __fmul_rn( dy, dy ) ), __fmul_rn( dz, dz ) ) );
+                const float3 df = make_float3( __fdiv_rn( dx, len ), __fdiv_rn( dy, len ), __fdiv_rn( dz, len ) );
                 float        t   = (float)p.tNear;
                 float        hit = __int_as_float( 0x7f800000 ); // +inf: background
                 for ( uint32_t step = 0; step < p.maxSteps && t <= tFar; step++ )
@@ -3590,32 +3591,32 @@ namespace sesgb
                 float3 nrm = make_float3( 0.f, 0.f, 0.f );
                 if ( normals && hit < 3.4e38f )
                 {
-                    const double hd = (double)hit;
-                    const d3 x = D3( __dadd_rn( p.eye[ 0 ], __dmul_rn( hd, d.x ) ), __dadd_rn( p.eye[ 1 ], __dmul_rn( hd, d.y ) ),
-                                     __dadd_rn( p.eye[ 2 ], __dmul_rn( hd, d.z ) ) );
-                    double g[ 3 ];
+                    // the hit point as the march computed it, moved by +-hn along each axis
+                    const float3 x = make_float3( __fadd_rn( ef.x, __fmul_rn( hit, df.x ) ), __fadd_rn( ef.y, __fmul_rn( hit, df.y ) ),
+                                                  __fadd_rn( ef.z, __fmul_rn( hit, df.z ) ) );
+                    float g[ 3 ];
                     for ( int a = 0; a < 3; a++ )
                     {
-                        double v2[ 2 ];
+                        float v2[ 2 ];
                         for ( int sg = 0; sg < 2; sg++ )
                         {
-                            const double e = sg == 0 ? p.normalStep : -p.normalStep;
-                            float3       q = make_float3( (float)x.x, (float)x.y, (float)x.z );
+                            const float e = sg == 0 ? hn : -hn;
+                            float3      q = x;
                             if ( a == 0 )
-                                q.x = (float)__dadd_rn( x.x, e );
+                                q.x = __fadd_rn( x.x, e );
                             else if ( a == 1 )
-                                q.y = (float)__dadd_rn( x.y, e );
+                                q.y = __fadd_rn( x.y, e );
                             else
-                                q.z = (float)__dadd_rn( x.z, e );
+                                q.z = __fadd_rn( x.z, e );
                             bool ex;
-                            v2[ sg ] = (double)sdf_query<true>( b, q, smem[ warp ], band, overflow, ex ).value;
+                            v2[ sg ] = sdf_query<true>( b, q, smem[ warp ], band, overflow, ex ).value;
                         }
-                        g[ a ] = __ddiv_rn( __dsub_rn( v2[ 0 ], v2[ 1 ] ), __dmul_rn( 2.0, p.normalStep ) );
+                        g[ a ] = __fdiv_rn( __fsub_rn( v2[ 0 ], v2[ 1 ] ), __fmul_rn( 2.f, hn ) );
                     }
-                    const double gl = __dsqrt_rn( __dadd_rn( __dadd_rn( __dmul_rn( g[ 0 ], g[ 0 ] ), __dmul_rn( g[ 1 ], g[ 1 ] ) ),
-                                                             __dmul_rn( g[ 2 ], g[ 2 ] ) ) );
-                    const double inv = gl > 0.0 ? gl : 1.0;
-                    nrm = make_float3( (float)__ddiv_rn( g[ 0 ], inv ), (float)__ddiv_rn( g[ 1 ], inv ), (float)__ddiv_rn( g[ 2 ], inv ) );
+                    const float gl  = __fsqrt_rn( __fadd_rn( __fadd_rn( __fmul_rn( g[ 0 ], g[ 0 ] ), __fmul_rn( g[ 1 ], g[ 1 ] ) ),
+                                                             __fmul_rn( g[ 2 ], g[ 2 ] ) ) );
+                    const float inv = gl > 0.f ? gl : 1.f;
+                    nrm = make_float3( __fdiv_rn( g[ 0 ], inv ), __fdiv_rn( g[ 1 ], inv ), __fdiv_rn( g[ 2 ], inv ) );
                 }
                 if ( lane == 0 )
                 {

@@ -16,7 +16,8 @@ Normals are the normalised central differences of the signed distance at the hit
 The tracer takes the signed distance as a function of (m, 3) float32 points, so the same code runs on
 the GPU build (``gpu_sdf_fn``) and, in the tests, on the FP64 oracle. ``gpu_depth_image`` is the same
 image from one device launch (``sesgb_render``: a warp per ray, the signed distance evaluated in the
-kernel, no host round trip per step); its ray arithmetic follows this module's operation for operation.
+kernel, no host round trip per step); its ray arithmetic (float32, every operation rounded on its own)
+follows this module's operation for operation.
 """
 from __future__ import annotations
 
@@ -37,14 +38,20 @@ def camera_basis(eye, target, up):
 
 
 def camera_rays(eye, target, up, fov_deg: float, width: int, height: int):
-    """Unit ray directions (height*width, 3) float64 of a pinhole camera, row-major from the top left."""
-    f, r, u = camera_basis(eye, target, up)
-    h = np.tan(np.radians(fov_deg) / 2.0)
-    xs = (2.0 * (np.arange(width) + 0.5) / width - 1.0) * h * width / height
-    ys = (1.0 - 2.0 * (np.arange(height) + 0.5) / height) * h
-    d = f[None, None, :] + xs[None, :, None] * r[None, None, :] + ys[:, None, None] * u[None, None, :]
-    d /= np.linalg.norm(d, axis=2, keepdims=True)
-    return d.reshape(-1, 3)
+    """Unit ray directions (height*width, 3) float32 of a pinhole camera, row-major from the top left.
+    float32 arithmetic, every operation rounded on its own in the order written (the device tracer's)."""
+    f, r, u = (v.astype(np.float32) for v in camera_basis(eye, target, up))
+    th = np.float32(np.tan(np.radians(fov_deg) / 2.0))
+    W, H = np.float32(width), np.float32(height)
+    one, two, half = np.float32(1.0), np.float32(2.0), np.float32(0.5)
+    ix = np.arange(width, dtype=np.float32)
+    iy = np.arange(height, dtype=np.float32)
+    xs = ((((two * (ix + half)) / W - one) * th) * W) / H
+    ys = (one - (two * (iy + half)) / H) * th
+    d = (f[None, None, :] + xs[None, :, None] * r[None, None, :]) + ys[:, None, None] * u[None, None, :]
+    ln = np.sqrt((d[..., 0] * d[..., 0] + d[..., 1] * d[..., 1]) + d[..., 2] * d[..., 2])
+    d = d / ln[..., None]
+    return d.reshape(-1, 3).astype(np.float32)
 
 
 def sphere_trace(sdf_fn, origin, dirs, probe_radius: float, t_near: float, t_far: float, eps: float = 1e-3,
@@ -81,17 +88,20 @@ def sphere_trace(sdf_fn, origin, dirs, probe_radius: float, t_near: float, t_far
 
 
 def normals(sdf_fn, points, h: float = 1e-2):
-    """Unit gradients (float64 [k, 3]) of the signed distance at points by central differences."""
-    p = np.asarray(points, np.float64)
+    """Unit gradients (float32 [k, 3]) of the signed distance at float32 points by central differences
+    (float32 arithmetic, every operation rounded on its own, as the device tracer computes them)."""
+    p = np.asarray(points, np.float32)
+    h32 = np.float32(h)
     g = np.zeros_like(p)
     for a in range(3):
-        e = np.zeros(3)
-        e[a] = h
-        vp, _ = sdf_fn((p + e).astype(np.float32))
-        vm, _ = sdf_fn((p - e).astype(np.float32))
-        g[:, a] = (np.asarray(vp, np.float64) - np.asarray(vm, np.float64)) / (2 * h)
-    n = np.linalg.norm(g, axis=1, keepdims=True)
-    return g / np.where(n > 0, n, 1.0)
+        qp, qm = p.copy(), p.copy()
+        qp[:, a] = p[:, a] + h32
+        qm[:, a] = p[:, a] - h32
+        vp, _ = sdf_fn(qp)
+        vm, _ = sdf_fn(qm)
+        g[:, a] = (np.asarray(vp, np.float32) - np.asarray(vm, np.float32)) / (np.float32(2.0) * h32)
+    n = np.sqrt((g[:, 0] * g[:, 0] + g[:, 1] * g[:, 1]) + g[:, 2] * g[:, 2])
+    return g / np.where(n > 0, n, np.float32(1.0))[:, None]
 
 
 def framing(atoms, probe_radius: float, view=(0.3, -1.0, 0.5), fov_deg: float = 40.0):
@@ -116,10 +126,12 @@ def depth_image(sdf_fn, atoms, probe_radius: float, width: int = 128, height: in
     eye, centre, up, t_near, t_far = framing(atoms, probe_radius, view, fov_deg)
     dirs = camera_rays(eye, centre, up, fov_deg, width, height)
     depth = sphere_trace(sdf_fn, eye, dirs, probe_radius, t_near, t_far, eps)
-    nrm = np.zeros((width * height, 3))
+    nrm = np.zeros((width * height, 3), np.float32)
     hit = np.isfinite(depth)
     if with_normals and hit.any():
-        nrm[hit] = normals(sdf_fn, eye[None, :] + depth[hit, None].astype(np.float64) * dirs[hit])
+        # the hit points as the march computed them (float32)
+        o32 = np.asarray(eye, np.float64).astype(np.float32)
+        nrm[hit] = normals(sdf_fn, o32[None, :] + depth[hit, None] * dirs[hit])
     return depth.reshape(height, width).astype(np.float32), nrm.reshape(height, width, 3).astype(np.float32)
 
 

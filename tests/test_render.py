@@ -64,11 +64,15 @@ def test_surface_between_vdw_union_and_sas():
         dc = np.linalg.norm(p[:, None, :] - a[None, :, :3], axis=2)
         assert np.all((dc - a[None, :, 3]).min(axis=1) >= -1e-4)       # outside the vdW union
         assert np.all((dc - a[None, :, 3] - RP).min(axis=1) <= 1e-4)   # inside the SAS
-        # a ray that meets a vdW sphere meets the SES no later
+        # a ray that meets a vdW sphere (passing at least eps inside it) meets the SES no later; the
+        # float32 ray directions are unit vectors only to a few ulps, so the entry solves the quadratic
+        # with |d|^2 as it is
+        d64 = dirs.astype(np.float64)
+        dd = np.einsum("ij,ij->i", d64, d64)
         for i in range(a.shape[0]):
             oc = eye - a[i, :3]
-            b = dirs @ oc
-            disc = b * b - (oc @ oc - a[i, 3] ** 2)
-            tv = np.where(disc > 0, -b - np.sqrt(np.maximum(disc, 0.0)), np.inf)
+            b = d64 @ oc
+            disc = b * b - dd * (oc @ oc - a[i, 3] ** 2)
+            tv = np.where(disc > 2 * a[i, 3] * EPS, (-b - np.sqrt(np.maximum(disc, 0.0))) / dd, np.inf)
             meets = np.isfinite(tv)
             assert np.all(hit[meets]) and np.all(d[meets] <= tv[meets] + 1e-4)
