@@ -42,6 +42,9 @@ namespace sesgb
         constexpr int      kAreaIv    = 64 + 2;          // cuts of one constraint circle (a lane's own, local memory)
         constexpr int      kLuneIv    = kAreaNbr + 2;    // cuts of one lune-plane circle (the warp's, shared memory)
         constexpr int      kProbeCons = 3 + (int)kMaxProbeNbr;
+        // |tw| below which a torus arc end's angle terms are taken in double precision: its float32
+        // position carries rounding ~1e-7 / |tw|, and the terms go as 1 / tw
+        constexpr float kShallowCrossing = 0.1f;
         static_assert( kMaxProbeNbr <= 32, "one neighbour cap per lane" );
 
         struct Circ
@@ -444,6 +447,56 @@ namespace sesgb
                 atomicAdd( g + 4 * (size_t)a + 3, r );
         }
 
+        // Pair constraint (w, c) of atom i and neighbour atom j in double precision, from the float32 atoms.
+        __device__ __forceinline__ void pair_cons_d( float4 ai, float4 aj, double rp, d3 & w, double & c )
+        {
+            const d3     D  = D3( (double)aj.x - (double)ai.x, (double)aj.y - (double)ai.y, (double)aj.z - (double)ai.z );
+            const double d  = sqrt( ddot( D, D ) );
+            const double Ri = (double)ai.w + rp, Rj = (double)aj.w + rp;
+            w               = dmul( D, 1.0 / d );
+            c               = ( Ri * Ri - Rj * Rj + d * d ) / ( 2.0 * d * Ri );
+        }
+
+        // Angle part of the torus of circle m at one arc end where circle m crosses the plane of
+        // constraint nn at a small angle (|tw| small): there the end's float32 position, and so tw
+        // and 1 / tw, carry rounding magnified by the shallow crossing. The end is taken again in
+        // double precision as the point of circle m on that plane (the one on the side of the
+        // float32 end), with both constraints recomputed from the atoms, and its terms are formed
+        // in double precision (coef = Gs / tw; Gs = -G or G by the end): out = gc[nn], gw[nn],
+        // gc[m], gw[m].
+        __device__ __noinline__ void arc_end_terms_d( const Build & b, uint32_t i, uint32_t jm, uint32_t jn, f3 yf, float Gs,
+                                                      double out[ 8 ] )
+        {
+            const float4 ai = b.atoms[ i ];
+            d3           wm, wn;
+            double       cm, cn;
+            pair_cons_d( ai, b.atoms[ jm ], (double)b.rp, wm, cm );
+            pair_cons_d( ai, b.atoms[ jn ], (double)b.rp, wn, cn );
+            const double g   = ddot( wm, wn );
+            const double den = 1.0 - g * g;
+            for ( int k = 0; k < 8; k++ )
+                out[ k ] = 0.0;
+            if ( !( den > 0.0 ) )
+                return;
+            const double al = ( cm - g * cn ) / den, be = ( cn - g * cm ) / den;
+            const d3     nv = dcross( wm, wn );
+            double       g2 = ( 1.0 - ( al * al + be * be + 2.0 * al * be * g ) ) / den;
+            g2              = g2 > 0.0 ? g2 : 0.0;
+            const double ga = ( (double)yf.x * nv.x + (double)yf.y * nv.y + (double)yf.z * nv.z ) < 0.0 ? -sqrt( g2 ) : sqrt( g2 );
+            const d3     y  = dadd( dadd( dmul( wm, al ), dmul( wn, be ) ), dmul( nv, ga ) );
+            const d3     yc = dsub( y, dmul( wm, cm ) );
+            const double tw = ddot( dcross( wm, yc ), wn );
+            if ( !( fabs( tw ) > 0.0 ) )
+                return;
+            const double coef = (double)Gs / tw;
+            const double sm2  = 1.0 - cm * cm;
+            out[ 0 ]          = coef;
+            out[ 1 ] = -coef * y.x, out[ 2 ] = -coef * y.y, out[ 3 ] = -coef * y.z;
+            out[ 4 ]          = -coef * ( g - ( cm / sm2 ) * ddot( yc, wn ) );
+            const d3 gwm      = dmul( dsub( dmul( wn, cm ), dmul( yc, g ) ), -coef );
+            out[ 5 ] = gwm.x, out[ 6 ] = gwm.y, out[ 7 ] = gwm.z;
+        }
+
         struct AreaSmem
         {
             float4 cons[ kAreaNbr ];
@@ -528,8 +581,20 @@ namespace sesgb
                         const float4 kn  = S.cons[ nn ];
                         const f3     wn  = F3( kn.x, kn.y, kn.z );
                         const float  tw  = dot( cross( C.w, yc ), wn );
-                        if ( !( fabsf( tw ) > 0.f ) )
+                        if ( fabsf( tw ) < kShallowCrossing )
+                        {
+                            double t[ 8 ];
+                            arc_end_terms_d( b, i, j, b.nbr[ row + nn ], y, e == 0 ? -G : G, t );
+                            atomicAdd( &S.gc[ nn ], (float)t[ 0 ] );
+                            atomicAdd( &S.gw[ nn ].x, (float)t[ 1 ] );
+                            atomicAdd( &S.gw[ nn ].y, (float)t[ 2 ] );
+                            atomicAdd( &S.gw[ nn ].z, (float)t[ 3 ] );
+                            atomicAdd( &S.gc[ m ], (float)t[ 4 ] );
+                            atomicAdd( &S.gw[ m ].x, (float)t[ 5 ] );
+                            atomicAdd( &S.gw[ m ].y, (float)t[ 6 ] );
+                            atomicAdd( &S.gw[ m ].z, (float)t[ 7 ] );
                             continue;
+                        }
                         const float coef = ( e == 0 ? -G : G ) / tw;
                         const float wwn  = dot( C.w, wn );
                         atomicAdd( &S.gc[ nn ], coef );
@@ -622,8 +687,235 @@ namespace sesgb
                 atomicOr( &b.counts->overflow, (uint32_t)kOverflowArea );
         }
 
+        // ---- double-precision twin of a probe region's adjoint ------------------------------
+        // A neighbour probe closer than kCloseProbe makes a cap of nearly a hemisphere whose terms
+        // go as 1 / L (L the distance of the two probes): the float32 arc integrals' rounding shows
+        // there. Such a region's adjoint is taken again in double precision: the same constraints
+        // from the float32 probe positions and atoms, every constraint's allowed arcs (the gaps
+        // between its cuts by the others; the lune split of the area does not change their sums),
+        // and the same terms as the float32 path.
+        constexpr float kCloseProbe = 0.5f;
+
+        struct dcons
+        {
+            double x, y, z, w;
+        };
+        __device__ __forceinline__ dcons dcons_of( double x, double y, double z, double w ) { return { x, y, z, w }; }
+
+        __device__ __forceinline__ double wrap2pi_d( double a )
+        {
+            a = fmod( a, 2.0 * 3.14159265358979323846 );
+            return a < 0.0 ? a + 2.0 * 3.14159265358979323846 : a;
+        }
+
+        // allowed-arc length and integral of y over constraint m of the region kd[0, M)
+        __device__ void constraint_arcs_d( const dcons * kd, int M, int m, double & dphi, d3 & iy )
+        {
+            const double k2Pi = 2.0 * 3.14159265358979323846;
+            dphi              = 0.0;
+            iy                = D3( 0.0, 0.0, 0.0 );
+            const double cm   = kd[ m ].w;
+            if ( !( cm < 1.0 ) )
+                return;
+            const d3     wm = D3( kd[ m ].x, kd[ m ].y, kd[ m ].z );
+            const double sm = sqrt( ( 1.0 - cm ) * ( 1.0 + cm ) );
+            const double ax = fabs( wm.x ), ay = fabs( wm.y ), az = fabs( wm.z );
+            const d3     t  = ( ax <= ay && ax <= az ) ? D3( 1.0, 0.0, 0.0 ) : ( ay <= az ? D3( 0.0, 1.0, 0.0 ) : D3( 0.0, 0.0, 1.0 ) );
+            d3           e1 = dcross( wm, t );
+            e1              = dmul( e1, 1.0 / sqrt( ddot( e1, e1 ) ) );
+            const d3 e2     = dcross( wm, e1 );
+            double   ivS[ kProbeCons ], ivL[ kProbeCons ], enV[ kProbeCons ], enL[ kProbeCons ];
+            bool     unc[ kProbeCons ];
+            int      nIv = 0;
+            for ( int n = 0; n < M; n++ )
+            {
+                if ( n == m )
+                    continue;
+                const double cn = kd[ n ].w;
+                if ( !( cn < 1.0 ) )
+                    continue;
+                const d3 wn = D3( kd[ n ].x, kd[ n ].y, kd[ n ].z );
+                if ( wn.x == wm.x && wn.y == wm.y && wn.z == wm.z && cn == cm )
+                {
+                    if ( n < m )
+                        return; // the same constraint twice: the first one keeps the circle
+                    continue;
+                }
+                const double p1 = ddot( e1, wn ), p2 = ddot( e2, wn );
+                const double B = sm * sqrt( p1 * p1 + p2 * p2 ), rhs = cn - cm * ddot( wm, wn );
+                if ( !( B > fabs( rhs ) ) )
+                {
+                    if ( rhs < 0.0 )
+                        return; // the whole circle lies inside cap n
+                    continue;
+                }
+                const double delta = atan2( sqrt( ( B - rhs ) * ( B + rhs ) ), rhs );
+                ivS[ nIv ]         = wrap2pi_d( atan2( p2, p1 ) - delta );
+                ivL[ nIv ]         = 2.0 * delta;
+                nIv++;
+            }
+            if ( nIv == 0 )
+            {
+                dphi = k2Pi;
+                iy   = dmul( wm, cm * k2Pi );
+                return;
+            }
+            for ( int q = 0; q < nIv; q++ )
+            {
+                enV[ q ]          = wrap2pi_d( ivS[ q ] + ivL[ q ] );
+                const double len2 = wrap2pi_d( enV[ q ] - ivS[ q ] );
+                enL[ q ]          = len2 >= 0.5 * ivL[ q ] ? len2 : ivL[ q ];
+            }
+            for ( int a = 0; a < nIv; a++ )
+            {
+                unc[ a ] = true;
+                for ( int c = 0; c < nIv && unc[ a ]; c++ )
+                    if ( c != a && wrap2pi_d( enV[ a ] - ivS[ c ] ) < enL[ c ] )
+                        unc[ a ] = false;
+            }
+            for ( int a = 0; a < nIv; a++ )
+            {
+                if ( !unc[ a ] )
+                    continue;
+                const double end = enV[ a ];
+                bool         dup = false;
+                for ( int c = 0; c < a && !dup; c++ )
+                    dup = unc[ c ] && enV[ c ] == end;
+                if ( dup )
+                    continue;
+                double gap = k2Pi;
+                bool   any = false;
+                for ( int c = 0; c < nIv; c++ )
+                {
+                    const double g = wrap2pi_d( ivS[ c ] - end );
+                    if ( g > 0.0 && ( !any || g < gap ) )
+                    {
+                        gap = g;
+                        any = true;
+                    }
+                }
+                if ( !any )
+                    continue;
+                dphi += gap;
+                const double c0 = cos( end ), s0 = sin( end ), c1 = cos( end + gap ), s1 = sin( end + gap );
+                iy = dadd( iy, dadd( dmul( wm, cm * gap ), dmul( dsub( dmul( e1, s1 - s0 ), dmul( e2, c1 - c0 ) ), sm ) ) );
+            }
+        }
+
+        // The warp's probe p (a region with a nearly coincident neighbour): its adjoint terms in
+        // double precision into gradSorted (contact directions) and probeGrad (probe positions).
+        // kd, sums: shared memory of kProbeCons entries each.
+        __device__ __noinline__ void probe_region_grad_d( const Build & b, uint32_t p, float gConcave, float * gradSorted,
+                                                          float4 * probeGrad, dcons * kd, dcons * sums )
+        {
+            const uint32_t lane = lane_id();
+            const double   rp   = (double)b.rp;
+            const int4     id   = b.probeIds[ p ];
+            const float4   pf   = b.probePos[ p ];
+            const d3       P    = D3( (double)pf.x, (double)pf.y, (double)pf.z );
+            const int      ia[ 3 ] = { id.x, id.y, id.z };
+            d3             v[ 3 ];
+            double         Lv[ 3 ];
+            for ( int a = 0; a < 3; a++ )
+            {
+                const float4 c = b.atoms[ ia[ a ] ];
+                const d3     D = D3( (double)c.x - P.x, (double)c.y - P.y, (double)c.z - P.z );
+                Lv[ a ]        = sqrt( ddot( D, D ) );
+                v[ a ]         = dmul( D, 1.0 / Lv[ a ] );
+            }
+            d3     u[ 3 ];
+            double ul[ 3 ], sg[ 3 ];
+            bool   flat = false;
+            for ( int e = 0; e < 3; e++ )
+            {
+                u[ e ]            = dcross( v[ e ], v[ ( e + 1 ) % 3 ] );
+                ul[ e ]           = sqrt( ddot( u[ e ], u[ e ] ) );
+                const double side = ddot( u[ e ], v[ ( e + 2 ) % 3 ] );
+                flat |= !( ul[ e ] > 0.0 ) || side == 0.0;
+                sg[ e ] = side > 0.0 ? 1.0 : -1.0;
+            }
+            if ( flat )
+                return; // a flat triangle has no area
+            const uint32_t Q   = min( b.counts->Q, b.capProbes );
+            const uint32_t cnt = p < Q ? min( (uint32_t)id.w, kMaxProbeNbr ) : 0u;
+            const int      M   = 3 + (int)cnt;
+            if ( lane < 3 )
+            {
+                const d3 w  = dmul( u[ lane ], -sg[ lane ] / ul[ lane ] );
+                kd[ lane ] = dcons_of( w.x, w.y, w.z, 0.0 );
+            }
+            uint32_t q = 0;
+            double   L = 0.0;
+            if ( lane < cnt )
+            {
+                q               = b.probeNbrIdx[ (size_t)p * kMaxProbeNbr + lane ];
+                const float4 pq = b.probePos[ q ];
+                const d3     D  = D3( (double)pq.x - P.x, (double)pq.y - P.y, (double)pq.z - P.z );
+                L               = sqrt( ddot( D, D ) );
+                kd[ 3 + lane ]  = L > 0.0 && L < 2.0 * rp ? dcons_of( D.x / L, D.y / L, D.z / L, L / ( 2.0 * rp ) )
+                                                          : dcons_of( 0.0, 0.0, 1.0, 2.0 ); // vacuous
+            }
+            __syncwarp();
+            for ( int m = (int)lane; m < M; m += 32 )
+            {
+                double dphi;
+                d3     iy;
+                constraint_arcs_d( kd, M, m, dphi, iy );
+                sums[ m ] = dcons_of( iy.x, iy.y, iy.z, dphi );
+            }
+            __syncwarp();
+            const double k2 = (double)gConcave * rp * rp;
+            d3           gP = D3( 0.0, 0.0, 0.0 );
+            if ( lane == 0 )
+            {
+                d3 gv[ 3 ] = { D3( 0.0, 0.0, 0.0 ), D3( 0.0, 0.0, 0.0 ), D3( 0.0, 0.0, 0.0 ) };
+                for ( int e = 0; e < 3; e++ )
+                {
+                    const d3  gw = dmul( D3( sums[ e ].x, sums[ e ].y, sums[ e ].z ), -k2 );
+                    const d3  wh = dmul( u[ e ], 1.0 / ul[ e ] );
+                    const d3  gu = dmul( dsub( gw, dmul( wh, ddot( gw, wh ) ) ), -sg[ e ] / ul[ e ] );
+                    const int a = e, c2 = ( e + 1 ) % 3;
+                    gv[ a ]     = dadd( gv[ a ], dcross( v[ c2 ], gu ) );
+                    gv[ c2 ]    = dadd( gv[ c2 ], dcross( gu, v[ a ] ) );
+                }
+                for ( int a = 0; a < 3; a++ )
+                {
+                    const d3 gD = dmul( dsub( gv[ a ], dmul( v[ a ], ddot( gv[ a ], v[ a ] ) ) ), 1.0 / Lv[ a ] );
+                    add4( gradSorted, (uint32_t)ia[ a ], F3( (float)gD.x, (float)gD.y, (float)gD.z ), 0.f );
+                    gP = dsub( gP, gD );
+                }
+            }
+            if ( lane < cnt && L > 0.0 && L < 2.0 * rp )
+            {
+                const int    m  = 3 + (int)lane;
+                const d3     w  = D3( kd[ m ].x, kd[ m ].y, kd[ m ].z );
+                const d3     gw = dmul( D3( sums[ m ].x, sums[ m ].y, sums[ m ].z ), -k2 );
+                const double gc = k2 * sums[ m ].w;
+                const d3     gD = dadd( dmul( dsub( gw, dmul( w, ddot( gw, w ) ) ), 1.0 / L ), dmul( w, gc / ( 2.0 * rp ) ) );
+                gP              = dsub( gP, gD );
+                atomicAdd( &probeGrad[ q ].x, (float)gD.x );
+                atomicAdd( &probeGrad[ q ].y, (float)gD.y );
+                atomicAdd( &probeGrad[ q ].z, (float)gD.z );
+            }
+            for ( int o = 16; o > 0; o >>= 1 )
+            {
+                gP.x += __shfl_xor_sync( 0xffffffffu, gP.x, o );
+                gP.y += __shfl_xor_sync( 0xffffffffu, gP.y, o );
+                gP.z += __shfl_xor_sync( 0xffffffffu, gP.z, o );
+            }
+            if ( lane == 0 )
+            {
+                atomicAdd( &probeGrad[ p ].x, (float)gP.x );
+                atomicAdd( &probeGrad[ p ].y, (float)gP.y );
+                atomicAdd( &probeGrad[ p ].z, (float)gP.z );
+            }
+            __syncwarp();
+        }
+
         struct ProbeAreaSmem
         {
+            dcons kd[ kProbeCons ];   // constraints of a region taken in double precision
+            dcons sums[ kProbeCons ]; // and their allowed-arc integrals and lengths
             float4 cons[ kProbeCons ];
             float  dphi[ kProbeCons ];
             float4 iy[ kProbeCons ];
@@ -722,7 +1014,11 @@ namespace sesgb
                         for ( int a = 0; a < 3; a++ )
                             atomicAdd( atomArea + b.perm[ ia[ a ] ], cA * ( 1.f / 3.f ) );
                 }
-                if ( kGrad )
+                // a nearly coincident neighbour probe: the region's adjoint in double precision
+                const bool close = kGrad && __any_sync( 0xffffffffu, lane < cnt && S.dist[ 3 + lane ] < kCloseProbe );
+                if ( close )
+                    probe_region_grad_d( b, p, gConcave, gradSorted, probeGrad, S.kd, S.sums );
+                if ( kGrad && !close )
                 {
                     const float k2 = gConcave * rp * rp;
                     f3          gP = F3( 0.f, 0.f, 0.f );

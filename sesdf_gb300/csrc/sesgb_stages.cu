@@ -3573,50 +3573,76 @@ namespace sesgb
                 const float3 df = make_float3( __fdiv_rn( dx, len ), __fdiv_rn( dy, len ), __fdiv_rn( dz, len ) );
                 float        t   = (float)p.tNear;
                 float        hit = __int_as_float( 0x7f800000 ); // +inf: background
-                for ( uint32_t step = 0; step < p.maxSteps && t <= tFar; step++ )
+                // One query call site for the march and the six evaluations of the normal (the
+                // query is inlined once). Evaluation k of the normal moves the hit point by +hn
+                // (k even) or -hn (k odd) along axis k / 2.
+                float3   xh = make_float3( 0.f, 0.f, 0.f ), g = make_float3( 0.f, 0.f, 0.f );
+                float    vp = 0.f;
+                uint32_t step = 0;
+                int      k    = -1; // -1: marching
+                while ( true )
                 {
-                    const float3 x = make_float3( __fadd_rn( ef.x, __fmul_rn( t, df.x ) ), __fadd_rn( ef.y, __fmul_rn( t, df.y ) ),
-                                                  __fadd_rn( ef.z, __fmul_rn( t, df.z ) ) );
-                    bool         ex;
-                    const SdfHit h      = sdf_query<true>( b, x, smem[ warp ], band, overflow, ex );
-                    const bool   inside = h.kind == kSdfSphere || h.kind == kSdfCircle || h.kind == kSdfProbe;
-                    if ( ( inside && h.value < eps ) || h.kind == kSdfClampInside )
+                    float3 q;
+                    if ( k < 0 )
                     {
-                        hit = t;
-                        break;
+                        if ( !( step < p.maxSteps && t <= tFar ) )
+                            break;
+                        q = make_float3( __fadd_rn( ef.x, __fmul_rn( t, df.x ) ), __fadd_rn( ef.y, __fmul_rn( t, df.y ) ),
+                                         __fadd_rn( ef.z, __fmul_rn( t, df.z ) ) );
                     }
-                    const float st = inside ? h.value : __fsub_rn( h.value, b.rp );
-                    t              = __fadd_rn( t, fmaxf( st, minStep ) );
+                    else
+                    {
+                        if ( k == 6 )
+                            break;
+                        const float e = ( k & 1 ) ? -hn : hn;
+                        q             = xh;
+                        if ( k < 2 )
+                            q.x = __fadd_rn( xh.x, e );
+                        else if ( k < 4 )
+                            q.y = __fadd_rn( xh.y, e );
+                        else
+                            q.z = __fadd_rn( xh.z, e );
+                    }
+                    bool         ex;
+                    const SdfHit h = sdf_query<true>( b, q, smem[ warp ], band, overflow, ex );
+                    if ( k < 0 )
+                    {
+                        step++;
+                        const bool inside = h.kind == kSdfSphere || h.kind == kSdfCircle || h.kind == kSdfProbe;
+                        if ( ( inside && h.value < eps ) || h.kind == kSdfClampInside )
+                        {
+                            hit = t;
+                            if ( !normals )
+                                break;
+                            // the hit point as the march computed it
+                            xh = q;
+                            k  = 0;
+                            continue;
+                        }
+                        const float st = inside ? h.value : __fsub_rn( h.value, b.rp );
+                        t              = __fadd_rn( t, fmaxf( st, minStep ) );
+                        continue;
+                    }
+                    if ( ( k & 1 ) == 0 )
+                        vp = h.value;
+                    else
+                    {
+                        const float ga = __fdiv_rn( __fsub_rn( vp, h.value ), __fmul_rn( 2.f, hn ) );
+                        if ( k == 1 )
+                            g.x = ga;
+                        else if ( k == 3 )
+                            g.y = ga;
+                        else
+                            g.z = ga;
+                    }
+                    k++;
                 }
                 float3 nrm = make_float3( 0.f, 0.f, 0.f );
                 if ( normals && hit < 3.4e38f )
                 {
-                    // the hit point as the march computed it, moved by +-hn along each axis
-                    const float3 x = make_float3( __fadd_rn( ef.x, __fmul_rn( hit, df.x ) ), __fadd_rn( ef.y, __fmul_rn( hit, df.y ) ),
-                                                  __fadd_rn( ef.z, __fmul_rn( hit, df.z ) ) );
-                    float g[ 3 ];
-                    for ( int a = 0; a < 3; a++ )
-                    {
-                        float v2[ 2 ];
-                        for ( int sg = 0; sg < 2; sg++ )
-                        {
-                            const float e = sg == 0 ? hn : -hn;
-                            float3      q = x;
-                            if ( a == 0 )
-                                q.x = __fadd_rn( x.x, e );
-                            else if ( a == 1 )
-                                q.y = __fadd_rn( x.y, e );
-                            else
-                                q.z = __fadd_rn( x.z, e );
-                            bool ex;
-                            v2[ sg ] = sdf_query<true>( b, q, smem[ warp ], band, overflow, ex ).value;
-                        }
-                        g[ a ] = __fdiv_rn( __fsub_rn( v2[ 0 ], v2[ 1 ] ), __fmul_rn( 2.f, hn ) );
-                    }
-                    const float gl  = __fsqrt_rn( __fadd_rn( __fadd_rn( __fmul_rn( g[ 0 ], g[ 0 ] ), __fmul_rn( g[ 1 ], g[ 1 ] ) ),
-                                                             __fmul_rn( g[ 2 ], g[ 2 ] ) ) );
+                    const float gl  = __fsqrt_rn( __fadd_rn( __fadd_rn( __fmul_rn( g.x, g.x ), __fmul_rn( g.y, g.y ) ), __fmul_rn( g.z, g.z ) ) );
                     const float inv = gl > 0.f ? gl : 1.f;
-                    nrm = make_float3( __fdiv_rn( g[ 0 ], inv ), __fdiv_rn( g[ 1 ], inv ), __fdiv_rn( g[ 2 ], inv ) );
+                    nrm = make_float3( __fdiv_rn( g.x, inv ), __fdiv_rn( g.y, inv ), __fdiv_rn( g.z, inv ) );
                 }
                 if ( lane == 0 )
                 {

@@ -44,3 +44,5 @@ def test_oracle_matches_reference_kernels(path):
 def test_golden_fixtures_present():
     names = {os.path.basename(p)[:-4] for p in GOLDEN}
     assert "globule2k_full" in names and "globule2k_exterior" in names
+    # probe 2.4 A on the reference's 288-slot library
+    assert {"globule2k_rp24_full", "globule2k_rp24_exterior", "1AGA_rp24_full", "101M_rp24_full"} <= names
