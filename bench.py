@@ -532,6 +532,9 @@ def run_ours(args, rank, world, local):
             "k_sdf": issue_roofline("k_sdf", sx["forward_ms"], clocks.get("sm_mhz"), 16.0 * m + 16.0 * n20,
                                     "globule20k_1m"),
         }
+        # the image: 16 bytes (depth + normal) per pixel out; the build it traces is L2-resident
+        extra["rooflines"]["k_trace"] = issue_roofline("k_trace", sx["render_512x512_ms"], clocks.get("sm_mhz"),
+                                                       16.0 * 512 * 512, "globule20k_512")
         prof_a, prof_p = profiled("k_area_atoms", "globule20k"), profiled("k_area_probes", "globule20k")
         if prof_a.get("duration_us") and prof_p.get("duration_us"):
             share = prof_a["duration_us"] / (prof_a["duration_us"] + prof_p["duration_us"])

@@ -81,10 +81,11 @@ def test_globules(n, seed):
 
 
 def test_gradient_matches_oracle():
-    """A probe near the plane of its three centres (h -> 0, its mirror probe about to
-    merge with it) moves with its atoms as 1/h: there float32 rounding shows in a
-    handful of components (FP64 positions perturbed by 1e-7 A move the oracle's own
-    gradient as much). The bulk agrees to 1e-3 of the largest component."""
+    """The adjoint against the oracle's FP64 adjoint on the same float32 probe positions: within
+    1e-3 relative (Frobenius) and every component within 1e-3 of the largest. Where the adjoint
+    is ill-conditioned (torus arc ends at shallow crossings, probe regions with a nearly
+    coincident neighbour probe, probes near the plane of their centres) the GPU takes those
+    terms in double precision."""
     atoms = synth.globule(2000, 1000)
     _, _, g = gpu_area(atoms, grad=True)
     _, _, go = oracle_area(atoms, grad=True)
@@ -94,7 +95,7 @@ def test_gradient_matches_oracle():
     frac = np.mean(err <= 1e-3 * scale)
     print(f"area adjoint, 2,000 atoms: GPU vs oracle {rel:.2e} relative (Frobenius), {frac:.4f} of components within "
           f"1e-3 of the largest, worst {err.max() / scale:.2e}")
-    assert rel <= 5e-3 and frac >= 0.995, (rel, frac, err.max(), scale, np.unravel_index(np.argmax(err), err.shape))
+    assert rel <= 1e-3 and frac == 1.0, (rel, frac, err.max(), scale, np.unravel_index(np.argmax(err), err.shape))
 
 
 def test_torch_autograd():
@@ -107,7 +108,7 @@ def test_torch_autograd():
     want, _, go = oracle_area(atoms, grad=True)
     assert float(area.detach()) == pytest.approx(want.sum(), rel=1e-4)
     g = a.grad.cpu().numpy().astype(np.float64)
-    assert np.linalg.norm(g - 2.0 * go) <= 5e-3 * np.linalg.norm(2.0 * go)
+    assert np.linalg.norm(g - 2.0 * go) <= 1e-3 * np.linalg.norm(2.0 * go)
 
 
 def test_sdf_workload_globule():
@@ -120,4 +121,4 @@ def test_sdf_workload_globule():
     assert np.mean(np.abs(per - wper) <= 1e-3 + 1e-4 * np.abs(wper)) >= 0.999
     rel = np.linalg.norm(g - go) / np.linalg.norm(go)
     print(f"area adjoint, 20,000 atoms: GPU vs oracle {rel:.2e} relative (Frobenius)")
-    assert rel <= 5e-3
+    assert rel <= 1e-3
