@@ -509,6 +509,23 @@ static uint8_t circle_status( const ora_t * o, uint32_t i, uint32_t s, uint64_t 
     return (uint8_t)( isVisible * ( 1 + isComplete ) );
 }
 
+static int32_t find_slot( const ora_t * o, uint32_t atom, uint32_t target );
+
+/* Full build: circles (i, j) and (j, i) are one circle (the intersection of the
+ * SAS spheres of i and j), so that, where neither neighbour list is cut at the
+ * capacity, the circle is evaluated once, from its lower atom (i < j), and the
+ * slot of (j, i) takes that status. Every atom that can touch the circle is a
+ * neighbour of both i and j (its SAS sphere reaches a point of both spheres), so
+ * the two evaluations of the reference differ only where a test lies within
+ * float32 rounding, or the 1e-4 margin, of its threshold. A list cut at the
+ * capacity misses neighbours the other side may hold: such circles are
+ * evaluated from both sides, as the reference does. */
+static int mirrored_circle( const ora_t * o, uint32_t i, uint32_t j )
+{
+    return o->mode == ORA_MODE_FULL && j < i && o->noff[ i + 1 ] - o->noff[ i ] < o->maxNbr &&
+           o->noff[ j + 1 ] - o->noff[ j ] < o->maxNbr;
+}
+
 static void stage_visibility( ora_t * o )
 {
     o->status  = (uint8_t *)calloc( o->P ? o->P : 1, 1 );
@@ -523,10 +540,26 @@ static void stage_visibility( ora_t * o )
             const uint32_t j = o->nbr[ base + s ];
             if ( o->mode == ORA_MODE_EXTERIOR && !( (uint32_t)i < j ) )
                 continue;
+            if ( mirrored_circle( o, (uint32_t)i, j ) )
+                continue;
             uint64_t b = 0, c = 0;
             o->status[ base + s ] = circle_status( o, (uint32_t)i, s, &b, &c );
             bandB += b;
             bandC += c;
+        }
+    }
+#pragma omp parallel for schedule( dynamic, 256 )
+    for ( int64_t i = 0; i < (int64_t)o->n; i++ )
+    {
+        const uint32_t base = o->noff[ i ], ni = o->noff[ i + 1 ] - base;
+        for ( uint32_t s = 0; s < ni; s++ )
+        {
+            const uint32_t j = o->nbr[ base + s ];
+            if ( !mirrored_circle( o, (uint32_t)i, j ) )
+                continue;
+            /* both lists are complete and the neighbour predicate is symmetric: i is in N(j) */
+            const int32_t t       = find_slot( o, j, (uint32_t)i );
+            o->status[ base + s ] = t >= 0 ? o->status[ o->noff[ j ] + (uint32_t)t ] : 0;
         }
     }
     o->counters[ BAND_BURIED ] += bandB;

@@ -275,6 +275,10 @@ namespace sesgb
                 p                 = b.probePos[ pi ];
                 if ( b.nMol > 1 )
                     m = mol_of( b, (uint32_t)b.probeIds[ pi ].x );
+                // singular probes: w holds the reference-grid hash of the position, the
+                // sort key of the probe in its neighbours' lists (k_probe_neighbors)
+                const GridRef gr = grid_of( b, m );
+                p.w              = __uint_as_float( ref_grid_hash( gr, ref_grid_position( gr, p.x, p.y, p.z ) ) );
             }
             const FineGrid g = b.fine[ m ];
             key              = cell_base( b, m ) + fine_key( g, fine_cell( g, p.x, p.y, p.z ) );
@@ -493,6 +497,21 @@ namespace sesgb
             }
         }
 
+        // slot of target in an ascending neighbour row, or -1
+        __device__ __forceinline__ int find_in_row( const uint32_t * row, uint32_t len, uint32_t target )
+        {
+            uint32_t lo = 0, hi = len;
+            while ( lo < hi )
+            {
+                const uint32_t mid = ( lo + hi ) >> 1;
+                if ( row[ mid ] < target )
+                    lo = mid + 1;
+                else
+                    hi = mid;
+            }
+            return ( lo < len && row[ lo ] == target ) ? (int)lo : -1;
+        }
+
         // ---- circle visibility ----------------------------------------------
         // Warp per atom i, lane per circle (i, s): every lane tests its circle
         // against the same k in turn. The neighbourhood is staged in shared memory
@@ -516,7 +535,8 @@ namespace sesgb
             kVisBuried    = 1,
             kVisTouched   = 2,
             kVisEvaluated = 4,
-            kVisUpper     = 8, // circle (i, j) with i < j: its touch mask is kept
+            kVisUpper     = 8,  // circle (i, j) with i < j: its touch mask is kept
+            kVisMirror    = 16, // circle (i, j), j < i, of two complete lists: takes the status of (j, i)
         };
 
         __host__ __device__ inline uint32_t staged_rows( uint32_t cap ) { return cap < (uint32_t)kNbrBuf ? cap : (uint32_t)kNbrBuf; }
@@ -681,8 +701,12 @@ namespace sesgb
             const size_t   row = (size_t)i * b.cap;
 
             // stage the neighbourhood (padded by 32 far slots) and the list of
-            // circles to evaluate (the exterior build evaluates circles (i, j) with
-            // i < j only)
+            // circles to evaluate: circles (i, j) with i < j, and in the full build
+            // also the circles (i, j), j < i, of a list cut at the capacity on either
+            // side. Circles (i, j) and (j, i) are one circle, and every atom that can
+            // touch it is in both complete lists, so that the other lower circles take
+            // the status of (j, i) in k_visibility_final (the reference evaluates both,
+            // operations.cu:126-204; the two differ only inside its float32 band)
             float    d2max = 0.f, r2max = 0.f;
             uint32_t nc    = 0;
             for ( uint32_t base = 0; base < ni + 32; base += 32 )
@@ -693,13 +717,18 @@ namespace sesgb
                 {
                     const uint32_t j  = b.nbr[ row + s ];
                     const float4   aj = b.atoms[ j ];
+                    const bool     mirror = b.mode == 0 && j < i && ni < b.cap && b.nbrCount[ j ] < b.cap;
                     const f3       d  = F3( aj.x - ai.x, aj.y - ai.y, aj.z - ai.z );
                     const float    dd = dot( d, d );
                     const float    Rk = aj.w + b.rp;
                     m.rel[ s ]        = make_float4( d.x, d.y, d.z, ( ( Ri * Ri + dd ) - Rk * Rk ) - 1e-4f );
                     m.dd[ s ]         = dd;
-                    eval              = b.mode == 0 || i < j;
-                    m.res[ s ]        = ( eval ? kVisEvaluated : 0 ) | ( i < j ? kVisUpper : 0 );
+                    eval              = b.mode == 0 ? !mirror : i < j;
+                    m.res[ s ]        = ( eval ? kVisEvaluated : 0 ) | ( i < j ? kVisUpper : 0 ) | ( mirror ? kVisMirror : 0 );
+                    // the slot of i in the list of j (both complete; the neighbour predicate is
+                    // symmetric), kept for k_visibility_final in slotTrim, which k_emit fills later
+                    if ( mirror )
+                        b.slotTrim[ row + s ] = (uint32_t)find_in_row( b.nbr + (size_t)j * b.cap, b.nbrCount[ j ], i );
                     d2max             = fmaxf( d2max, dd );
                     r2max             = fmaxf( r2max, Rk * Rk );
                 }
@@ -726,8 +755,9 @@ namespace sesgb
             uint32_t nq = 0;
             // Circles go 32 at a time, one per lane, each lane looping over all k
             // (the same k in every lane: shared-memory broadcasts). A last step with
-            // fewer circles spreads the k of each circle over a group of G lanes
-            // (k = lane in group + G u).
+            // at most 16 circles spreads the k of each circle over a group of G lanes
+            // (k = lane in group + G u). (Steps of 8 or 16 circles with every lane
+            // busy, instead of one step with idle lanes, measured slower on GB300.)
             for ( uint32_t c0 = 0; c0 < nc; )
             {
                 const uint32_t rem = nc - c0;
@@ -929,10 +959,13 @@ namespace sesgb
         }
 
         // statuses (0 buried, 1 partial, 2 complete; circles not evaluated 0) and
-        // the per-atom counts; four atoms per warp, eight lanes per atom
+        // the per-atom counts; four atoms per warp, eight lanes per atom. A lane holds
+        // up to eight slots of its atom in registers, so that their loads (and those
+        // of the mirrored circles' statuses) are in flight together.
         __global__ void __launch_bounds__( 32 * kWarpsPerBlock ) k_visibility_final( Build b )
         {
             pdl_begin();
+            constexpr uint32_t kHeld = 8;
             const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
             const uint32_t grp = lane / 8, gl = lane % 8;
             const uint32_t i    = ( blockIdx.x * kWarpsPerBlock + warp ) * 4 + grp;
@@ -940,15 +973,49 @@ namespace sesgb
             const uint32_t ni   = live ? b.nbrCount[ i ] : 0u;
             const size_t   row  = (size_t)i * b.cap;
             uint32_t       vis = 0, part = 0, full = 0;
-            for ( uint32_t s = gl; s < ni; s += 8 )
+            for ( uint32_t s0 = 0; s0 < ni; s0 += 8 * kHeld )
             {
-                const uint32_t j  = b.nbr[ row + s ];
-                const uint32_t r  = b.status[ row + s ];
-                const uint8_t  st = ( r & kVisEvaluated ) ? ( ( r & kVisBuried ) ? 0 : ( ( r & kVisTouched ) ? 1 : 2 ) ) : 0;
-                b.status[ row + s ] = st;
-                vis += st != 0;
-                part += ( st == 1 && i < j );
-                full += ( st == 2 && i < j );
+                uint32_t j[ kHeld ], r[ kHeld ], t[ kHeld ];
+#pragma unroll
+                for ( uint32_t h = 0; h < kHeld; h++ )
+                {
+                    const uint32_t s = s0 + gl + 8 * h;
+                    j[ h ] = r[ h ] = 0;
+                    t[ h ]          = 0xffffffffu;
+                    if ( s < ni )
+                    {
+                        j[ h ] = b.nbr[ row + s ];
+                        r[ h ] = b.status[ row + s ];
+                        // the slot of i in the list of j, left in slotTrim by k_visibility
+                        // for the mirrored circles (k_emit fills slotTrim later)
+                        if ( b.mode == 0 )
+                            t[ h ] = b.slotTrim[ row + s ];
+                    }
+                }
+#pragma unroll
+                for ( uint32_t h = 0; h < kHeld; h++ )
+                    if ( ( r[ h ] & kVisMirror ) )
+                    {
+                        // the status of (j, i): its flags, or the status another warp already
+                        // made of them (which has no kVisEvaluated bit)
+                        const uint32_t q = t[ h ] < b.cap ? b.status[ (size_t)j[ h ] * b.cap + t[ h ] ] : 0u;
+                        r[ h ] = ( q & kVisEvaluated ) ? q
+                                                       : ( q == 0 ? kVisEvaluated | kVisBuried
+                                                                  : q == 1 ? kVisEvaluated | kVisTouched : kVisEvaluated );
+                    }
+#pragma unroll
+                for ( uint32_t h = 0; h < kHeld; h++ )
+                {
+                    const uint32_t s = s0 + gl + 8 * h;
+                    if ( s < ni )
+                    {
+                        const uint8_t st = ( r[ h ] & kVisEvaluated ) ? ( ( r[ h ] & kVisBuried ) ? 0 : ( ( r[ h ] & kVisTouched ) ? 1 : 2 ) ) : 0;
+                        b.status[ row + s ] = st;
+                        vis += st != 0;
+                        part += ( st == 1 && i < j[ h ] );
+                        full += ( st == 2 && i < j[ h ] );
+                    }
+                }
             }
             for ( int o = 4; o > 0; o >>= 1 )
             {
@@ -1065,19 +1132,6 @@ namespace sesgb
         }
 
         // ---- probes: enumeration, float32 screen, double-precision solve -------
-        __device__ __forceinline__ int find_in_row( const uint32_t * row, uint32_t len, uint32_t target )
-        {
-            uint32_t lo = 0, hi = len;
-            while ( lo < hi )
-            {
-                const uint32_t mid = ( lo + hi ) >> 1;
-                if ( row[ mid ] < target )
-                    lo = mid + 1;
-                else
-                    hi = mid;
-            }
-            return ( lo < len && row[ lo ] == target ) ? (int)lo : -1;
-        }
 
         // ---- probe solve -----------------------------------------------------
         // Double-precision triplet point in closed form. With a = c_j - c_i,
@@ -2355,7 +2409,6 @@ namespace sesgb
                 const float4   pq = b.probePos[ pi ];
                 const uint32_t m  = b.nMol > 1 ? mol_of( b, (uint32_t)b.probeIds[ pi ].x ) : 0u;
                 const FineGrid g  = b.fine[ m ];
-                const GridRef  gr = grid_of( b, m );
                 const uint32_t * cells = b.cellStart + cell_base( b, m );
                 const bool       span2 = g.span == 2;
                 Rows             rows;
@@ -2393,7 +2446,7 @@ namespace sesgb
                                 fp64++;
                             }
                             if ( pass )
-                                key = ( (unsigned long long)ref_grid_hash( gr, ref_grid_position( gr, pp.x, pp.y, pp.z ) ) << 32 ) | p;
+                                key = ( (unsigned long long)__float_as_uint( pp.w ) << 32 ) | p;
                         }
                     }
                     const uint32_t mask = __ballot_sync( 0xffffffffu, pass );

@@ -151,7 +151,9 @@ def compare(atoms_in: np.ndarray, rp: float, mode: str, ref: dict, o: dict) -> d
             continue
         st_bad += 1
         tainted.add(frozenset(key))
-        if status_margin(pos, rad, a, b, sorted(on[a]), rpd) >= WIDE:
+        # the oracle evaluates a circle of two complete lists from its lower atom only: any
+        # atom of either list can decide it
+        if status_margin(pos, rad, a, b, sorted(set(on[a]) | set(on[b])), rpd) >= WIDE:
             st_unexp += 1
     rep["status_mismatch"] = st_bad
     rep["status_unexplained"] = st_unexp
@@ -372,7 +374,10 @@ def compare_sorted(ref: dict, gpu: dict, rp: float, mode: str) -> dict:
     for q in bad.tolist():
         i, j = int(ci_[q]), int(cj_[q])
         c = (min(i, j), max(i, j))
-        margin = 0.0 if i in bad_atoms else status_margin(pos, rad, i, j, nbrs_of(i), rpd)
+        # the full build evaluates a circle of two complete lists from its lower atom only, so the
+        # neighbours of both atoms can decide it
+        margin = 0.0 if i in bad_atoms or (not ext and j in bad_atoms) else \
+            status_margin(pos, rad, i, j, sorted(set(nbrs_of(i)) | set(nbrs_of(j))), rpd)
         inband = margin < WIDE
         if inband or not ext:
             tainted.add(c)
