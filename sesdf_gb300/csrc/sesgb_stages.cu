@@ -2602,95 +2602,161 @@ namespace sesgb
         }
 
         // ---- exterior tori ---------------------------------------------------
+        // squared radius of circle (i, j) in double precision from the float32 atoms (out of
+        // line: its conversions run only for the nearly tangent circles that need it)
+        __device__ __noinline__ float torus_r2_d( float4 ai, float4 aj, float rp )
+        {
+            const double Rid = (double)ai.w + (double)rp, Rjd = (double)aj.w + (double)rp;
+            const double ex = (double)aj.x - (double)ai.x, ey = (double)aj.y - (double)ai.y, ez = (double)aj.z - (double)ai.z;
+            const double dd = ex * ex + ey * ey + ez * ez;
+            const double td = ( Rid * Rid - Rjd * Rjd + dd ) / ( 2.0 * dd );
+            return (float)( Rid * Rid - td * td * dd );
+        }
+
+        // status-2 circles per atom: four atoms per warp, eight lanes per atom
         __global__ void __launch_bounds__( 32 * kWarpsPerBlock ) k_tori_count( Build b )
         {
             pdl_begin();
             const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
-            const uint32_t i    = blockIdx.x * kWarpsPerBlock + warp;
-            if ( i >= b.n )
-                return;
-            const uint32_t ni = b.nbrCount[ i ];
+            const uint32_t grp = lane / 8, gl = lane % 8;
+            const uint32_t i  = ( blockIdx.x * kWarpsPerBlock + warp ) * 4 + grp;
+            const uint32_t ni = i < b.n ? b.nbrCount[ i ] : 0u;
             uint32_t       c  = 0;
-            for ( uint32_t s = lane; s < ni; s += 32 )
+#pragma unroll 4
+            for ( uint32_t s = gl; s < ni; s += 8 )
                 c += b.status[ (size_t)i * b.cap + s ] == 2;
-            for ( int o = 16; o > 0; o >>= 1 )
+            for ( int o = 4; o > 0; o >>= 1 )
                 c += __shfl_xor_sync( 0xffffffffu, c, o );
-            if ( lane == 0 )
+            if ( i < b.n && gl == 0 )
                 b.torCnt[ i ] = c;
         }
 
+        // Torus of circle (i, s) of status 2 (fillCircles, ssesdf/operations.cu:246-285), in
+        // coordinates relative to atom i; writes its three records at idx
+        __device__ __forceinline__ void torus_of( const Build & b, uint32_t i, uint32_t s, uint32_t idx, uint32_t & ovf,
+                                                  uint32_t & degenerate )
+        {
+            const float4 ai = b.atoms[ i ];
+            const float4 aj = b.atoms[ b.nbr[ (size_t)i * b.cap + s ] ];
+            const float  Ri = ai.w + b.rp;
+            const float  Rj = aj.w + b.rp;
+            const f3     dj = F3( aj.x - ai.x, aj.y - ai.y, aj.z - ai.z );
+            const float  d  = dot( dj, dj );
+            const float  t  = ( Ri * Ri - Rj * Rj + d ) / ( 2.f * d );
+            const f3     c  = dj * t; // circle centre relative to atom i
+            float        r2 = Ri * Ri - dot( c, c );
+            if ( r2 < 0.004f * Ri * Ri )
+                // nearly tangent SAS spheres: the radius is the root of a difference of nearly
+                // equal numbers; taken in double precision from the float32 atoms
+                r2 = torus_r2_d( ai, aj, b.rp );
+            const float r  = sqrtf( fmaxf( r2, 0.f ) );
+            const f3    ta = normalize( c );
+            f3          cz = cross( ta, F3( 0.f, 0.f, 1.f ) );
+            if ( dot( cz, cz ) < 1e-12f )
+            {
+                // the reference normalises a zero vector here (NaN); use the x axis instead
+                cz = cross( ta, F3( 1.f, 0.f, 0.f ) );
+                degenerate++;
+            }
+            const f3    ortho = normalize( cz );
+            const f3    P     = c + ortho * r;
+            const f3    X     = normalize( P ) * ai.w;
+            const float lpi   = sqrtf( dot( P, P ) );
+            const f3    Pj    = P - dj;
+            const float lpj   = sqrtf( dot( Pj, Pj ) );
+            const f3    C     = dj * ( lpi / ( lpj + lpi ) );
+            const f3    XC    = X - C;
+            const float dist  = sqrtf( dot( XC, XC ) );
+            const f3    Cout  = C - c;
+            if ( idx < b.capTori )
+            {
+                b.torPos[ idx ]  = make_float4( ai.x + c.x, ai.y + c.y, ai.z + c.z, r );
+                b.torAxis[ idx ] = make_float4( ta.x, ta.y, ta.z, b.rp );
+                b.torVs[ idx ]   = make_float4( Cout.x, Cout.y, Cout.z, dist );
+            }
+            else
+                ovf |= kOverflowTori;
+        }
+
+        // A warp gathers the status-2 circles of kToriAtoms consecutive atoms into a shared
+        // queue (atom, slot, output index) and evaluates them 32 at a time, one per lane (an
+        // atom has a few tori among ~40 slots: a lane per slot left most lanes idle)
+        constexpr uint32_t kToriAtoms = 8;
         __global__ void __launch_bounds__( 32 * kWarpsPerBlock ) k_tori( Build b )
         {
             pdl_begin();
-            const uint32_t warp = threadIdx.x >> 5, lane = lane_id();
-            const uint32_t i    = blockIdx.x * kWarpsPerBlock + warp;
-            if ( i >= b.n )
-                return;
-            const uint32_t ni   = b.nbrCount[ i ];
-            const float4   ai   = b.atoms[ i ];
-            uint32_t       base = b.torOff[ i ], ovf = 0, degenerate = 0;
-            for ( uint32_t s0 = 0; s0 < ni; s0 += 32 )
-            {
-                const uint32_t s     = s0 + lane;
-                const bool     valid = s < ni && b.status[ (size_t)i * b.cap + s ] == 2;
-                const uint32_t m     = __ballot_sync( 0xffffffffu, valid );
-                if ( valid )
+            __shared__ uint4   queue[ kWarpsPerBlock ][ 64 ];
+            __shared__ uint8_t stat[ kWarpsPerBlock ][ 64 * kToriAtoms ];
+            const uint32_t     warp = threadIdx.x >> 5, lane = lane_id();
+            const uint32_t     i0   = ( blockIdx.x * kWarpsPerBlock + warp ) * kToriAtoms;
+            uint4 *          q    = queue[ warp ];
+            uint32_t         nq = 0, ovf = 0, degenerate = 0;
+            auto             drain = [ & ]( bool all ) {
+                while ( nq >= 32 || ( all && nq > 0 ) )
                 {
-                    const uint32_t idx = base + __popc( m & lanemask_lt() );
-                    const float4   aj  = b.atoms[ b.nbr[ (size_t)i * b.cap + s ] ];
-                    const float    Ri  = ai.w + b.rp;
-                    const float    Rj  = aj.w + b.rp;
-                    const f3       dj  = F3( aj.x - ai.x, aj.y - ai.y, aj.z - ai.z );
-                    const float    d   = dot( dj, dj );
-                    const float    t   = ( Ri * Ri - Rj * Rj + d ) / ( 2.f * d );
-                    const f3       c   = dj * t; // circle centre relative to atom i
-                    float          r2  = Ri * Ri - dot( c, c );
-                    if ( r2 < 0.004f * Ri * Ri )
+                    const uint32_t take = nq < 32 ? nq : 32;
+                    if ( lane < take )
                     {
-                        // nearly tangent SAS spheres: the radius is the root of a difference of nearly
-                        // equal numbers; taken in double precision from the float32 atoms
-                        const double Rid = (double)ai.w + (double)b.rp, Rjd = (double)aj.w + (double)b.rp;
-                        const double ex = (double)aj.x - (double)ai.x, ey = (double)aj.y - (double)ai.y,
-                                     ez = (double)aj.z - (double)ai.z;
-                        const double dd = ex * ex + ey * ey + ez * ez;
-                        const double td = ( Rid * Rid - Rjd * Rjd + dd ) / ( 2.0 * dd );
-                        r2              = (float)( Rid * Rid - td * td * dd );
+                        const uint4 e = q[ lane ];
+                        torus_of( b, e.x, e.y, e.z, ovf, degenerate );
                     }
-                    const float r  = sqrtf( fmaxf( r2, 0.f ) );
-                    const f3    ta = normalize( c );
-                    f3             cz  = cross( ta, F3( 0.f, 0.f, 1.f ) );
-                    if ( dot( cz, cz ) < 1e-12f )
-                    {
-                        // the reference normalises a zero vector here (NaN); use the x axis instead
-                        cz = cross( ta, F3( 1.f, 0.f, 0.f ) );
-                        degenerate++;
-                    }
-                    const f3    ortho = normalize( cz );
-                    const f3    P     = c + ortho * r;
-                    const f3    X     = normalize( P ) * ai.w;
-                    const float lpi   = sqrtf( dot( P, P ) );
-                    const f3    Pj    = P - dj;
-                    const float lpj   = sqrtf( dot( Pj, Pj ) );
-                    const f3    C     = dj * ( lpi / ( lpj + lpi ) );
-                    const f3    XC    = X - C;
-                    const float dist  = sqrtf( dot( XC, XC ) );
-                    const f3    Cout  = C - c;
-                    if ( idx < b.capTori )
-                    {
-                        b.torPos[ idx ]  = make_float4( ai.x + c.x, ai.y + c.y, ai.z + c.z, r );
-                        b.torAxis[ idx ] = make_float4( ta.x, ta.y, ta.z, b.rp );
-                        b.torVs[ idx ]   = make_float4( Cout.x, Cout.y, Cout.z, dist );
-                    }
-                    else
-                        ovf |= kOverflowTori;
+                    const uint32_t rest = nq - take; // at most 31
+                    uint4          keep = make_uint4( 0u, 0u, 0u, 0u );
+                    if ( lane < rest )
+                        keep = q[ take + lane ];
+                    __syncwarp();
+                    if ( lane < rest )
+                        q[ lane ] = keep;
+                    __syncwarp();
+                    nq = rest;
                 }
-                base += __popc( m );
+            };
+            // the atoms' counts, output offsets and first 64 statuses, all loads in flight together
+            // (statuses past the count are read within the row's capacity and not used), the
+            // statuses into shared memory
+            uint32_t myNi = 0, myBase = 0;
+            if ( lane < kToriAtoms && i0 + lane < b.n )
+            {
+                myNi   = b.nbrCount[ i0 + lane ];
+                myBase = b.torOff[ i0 + lane ];
             }
+            uint8_t * st = stat[ warp ];
+#pragma unroll
+            for ( uint32_t a = 0; a < kToriAtoms; a++ )
+#pragma unroll
+                for ( uint32_t h = 0; h < 2; h++ )
+                    st[ 64 * a + 32 * h + lane ] =
+                        i0 + a < b.n && lane + 32 * h < b.cap ? b.status[ (size_t)( i0 + a ) * b.cap + lane + 32 * h ] : (uint8_t)0;
+            __syncwarp();
+            for ( uint32_t a = 0; a < kToriAtoms; a++ )
+            {
+                const uint32_t i    = i0 + a;
+                const uint32_t ni   = __shfl_sync( 0xffffffffu, myNi, a );
+                uint32_t       base = __shfl_sync( 0xffffffffu, myBase, a );
+                for ( uint32_t s0 = 0; s0 < ni; s0 += 32 )
+                {
+                    const uint32_t s     = s0 + lane;
+                    const uint32_t code  = s0 < 64 ? st[ 64 * a + s ] : ( s < ni ? b.status[ (size_t)i * b.cap + s ] : 0u );
+                    const bool     valid = s < ni && code == 2;
+                    const uint32_t m     = __ballot_sync( 0xffffffffu, valid );
+                    const uint32_t r     = __popc( m & lanemask_lt() );
+                    if ( valid ) // nq <= 31 here: the queue holds up to 63 entries
+                        q[ nq + r ] = make_uint4( i, s, base + r, 0u );
+                    nq += __popc( m );
+                    base += __popc( m );
+                    __syncwarp();
+                    drain( false );
+                }
+            }
+            drain( true );
             for ( int o = 16; o > 0; o >>= 1 )
+            {
                 degenerate += __shfl_xor_sync( 0xffffffffu, degenerate, o );
+                ovf |= __shfl_xor_sync( 0xffffffffu, ovf, o );
+            }
             if ( lane == 0 && degenerate )
                 atomicAdd( &b.counts->torusDegenerate, degenerate );
-            if ( ovf )
+            if ( lane == 0 && ovf )
                 atomicOr( &b.counts->overflow, ovf );
         }
 
@@ -2888,14 +2954,14 @@ namespace sesgb
     {
         if ( !b.n )
             return;
-        pdl_launch( k_tori_count, blocks_for( b.n, kWarpsPerBlock ), 32 * kWarpsPerBlock, 0, s, b );
+        pdl_launch( k_tori_count, blocks_for( b.n, kWarpsPerBlock * 4 ), 32 * kWarpsPerBlock, 0, s, b );
         counted();
     }
     void launch_tori_emit( const Build & b, cudaStream_t s )
     {
         if ( !b.n )
             return;
-        pdl_launch( k_tori, blocks_for( b.n, kWarpsPerBlock ), 32 * kWarpsPerBlock, 0, s, b );
+        pdl_launch( k_tori, blocks_for( b.n, kWarpsPerBlock * kToriAtoms ), 32 * kWarpsPerBlock, 0, s, b );
         counted();
     }
     uint64_t launch_count() { return g_launches.load(); }
