@@ -487,7 +487,10 @@ namespace sesgb
             if ( lane == 0 )
             {
                 b.nbrCount[ i ] = kept;
-                atomicMax( &b.counts->maxNbr, count );
+                // every warp updating one counter serialised the kernel's ends on its L2 atomics:
+                // a warp whose count is not above the maximum already seen skips the update
+                if ( count > *(volatile uint32_t *)&b.counts->maxNbr )
+                    atomicMax( &b.counts->maxNbr, count );
                 if ( count > b.cap )
                     atomicAdd( &b.counts->nbrTruncated, 1u );
                 if ( count > kNbrBuf )
