@@ -1,5 +1,6 @@
 // sesgb_internal.h -- host-side declarations shared by the CUDA translation units.
 #pragma once
+#include <cstddef>
 #include <cstdint>
 #include <cuda_runtime.h>
 
@@ -51,13 +52,16 @@ namespace sesgb
         uint32_t fineCells;  // cells of the neighbour grid in use
         float    fineCell;   // edge of a neighbour-grid cell (A)
         float    rmax;       // largest vdW radius
-        uint32_t staged;     // probes written to the staging chunks
         uint32_t regTotal;   // regular (non-singular) probes
+        // staged and jobs form one 8-byte word: k_probes advances both with one 64-bit atomic
+        uint32_t staged;     // probes written to the staging chunks
         uint32_t jobs;       // double-precision probe jobs
         uint32_t segCircles; // circles carrying at least two probes
         uint32_t visBand;    // visibility tests queued for double precision
         uint32_t probeCursor; // work counter of the persistent probe screen
     };
+    static_assert( offsetof( DeviceCounts, staged ) % 8 == 0 && offsetof( DeviceCounts, jobs ) == offsetof( DeviceCounts, staged ) + 4,
+                   "staged and jobs form one 8-byte word" );
 
     enum Overflow : uint32_t
     {

@@ -1767,32 +1767,17 @@ namespace sesgb
                 fp64 += __shfl_xor_sync( 0xffffffffu, fp64, o );
             }
             __syncwarp();
-            // one chunk per atom; one double-precision job per kept side or band candidate
-            const uint32_t kept  = nEnt < (uint32_t)kProbeBuf ? nEnt : (uint32_t)kProbeBuf;
-            uint32_t       chunk = 0;
-            if ( lane == 0 )
-            {
-                if ( nEnt > (uint32_t)kProbeBuf )
-                    atomicOr( &b.counts->overflow, (uint32_t)kOverflowAtomProbes );
-                chunk = kept ? atomicAdd( &b.counts->staged, kept ) : 0u;
-                if ( cands )
-                    atomicAdd( &b.counts->cand, cands );
-                if ( fp64 )
-                    atomicAdd( &b.counts->fp64[ kFp64Neighbor ], fp64 );
-            }
-            chunk = __shfl_sync( 0xffffffffu, chunk, 0 );
-            // an atom with more entries than the warp holds (an error of the build) places none, so
-            // that the probe offsets stay within the staged ones
-            const bool fits = chunk + kept <= b.capProbes && nEnt <= (uint32_t)kProbeBuf;
-            // jobs: a fill entry is one job (counted up from the bottom of the job array); a
-            // band candidate's two entries are one job on its first entry (counted down
-            // from the top), so that each kind runs with full warps
-            uint32_t fillHere = 0, bandHere = 0;
+            // one chunk per atom; one double-precision job per kept side or band candidate.
+            // Jobs: a fill entry is one job (counted up from the bottom of the job array); a
+            // band candidate's two entries are one job on its first entry (counted down from the
+            // top), so that each kind runs with full warps
+            const uint32_t kept     = nEnt < (uint32_t)kProbeBuf ? nEnt : (uint32_t)kProbeBuf;
+            uint32_t       fillHere = 0, bandHere = 0;
             for ( uint32_t q0 = 0; q0 < kept; q0 += 32 )
             {
                 const uint32_t q    = q0 + lane;
                 bool           fill = false, band = false;
-                if ( q < kept && fits )
+                if ( q < kept )
                 {
                     const uint32_t info = m.ent[ q ].y;
                     fill                = ( ( info >> 1 ) & 1u ) == kJobFill;
@@ -1800,6 +1785,37 @@ namespace sesgb
                 }
                 fillHere += __popc( __ballot_sync( 0xffffffffu, fill ) );
                 bandHere += __popc( __ballot_sync( 0xffffffffu, band ) );
+            }
+            // the staging chunk and the fill-job slots in one 64-bit atomic: every atom's warp adds
+            // to these counters, and a contended atomic whose result a warp waits for is costly
+            uint32_t chunk = 0, jbase = 0;
+            if ( lane == 0 )
+            {
+                if ( nEnt > (uint32_t)kProbeBuf )
+                    atomicOr( &b.counts->overflow, (uint32_t)kOverflowAtomProbes );
+                if ( kept )
+                {
+                    const unsigned long long old = atomicAdd( reinterpret_cast<unsigned long long *>( &b.counts->staged ),
+                                                              (unsigned long long)kept | ( (unsigned long long)fillHere << 32 ) );
+                    chunk = (uint32_t)old;
+                    jbase = (uint32_t)( old >> 32 );
+                }
+                if ( cands )
+                    atomicAdd( &b.counts->cand, cands );
+                if ( fp64 )
+                    atomicAdd( &b.counts->fp64[ kFp64Neighbor ], fp64 );
+            }
+            chunk = __shfl_sync( 0xffffffffu, chunk, 0 );
+            jbase = __shfl_sync( 0xffffffffu, jbase, 0 );
+            // an atom with more entries than the warp holds (an error of the build) places none, so
+            // that the probe offsets stay within the staged ones; its fill-job slots get empty jobs
+            const bool fits = chunk + kept <= b.capProbes && nEnt <= (uint32_t)kProbeBuf;
+            if ( !fits )
+            {
+                for ( uint32_t t = lane; t < fillHere; t += 32 )
+                    if ( jbase + t < b.capProbes )
+                        b.jobs[ jbase + t ] = make_uint4( 0u, 0xffffffffu, 0u, 0u );
+                bandHere = 0;
             }
             // slot of k in N(j) for every kept entry, found by the whole warp: coalesced
             // passes over the rows of four entries at a time, their loads in flight together
@@ -1851,12 +1867,9 @@ namespace sesgb
                 }
             }
             __syncwarp();
-            uint32_t jbase = 0, gbase = 0;
-            if ( lane == 0 && fillHere )
-                jbase = atomicAdd( &b.counts->jobs, fillHere );
+            uint32_t gbase = 0;
             if ( lane == 0 && bandHere )
                 gbase = atomicAdd( &b.counts->bandJobs, bandHere );
-            jbase = __shfl_sync( 0xffffffffu, jbase, 0 );
             gbase = __shfl_sync( 0xffffffffu, gbase, 0 );
             for ( uint32_t q0 = 0; q0 < kept; q0 += 32 )
             {
@@ -1971,6 +1984,9 @@ namespace sesgb
                 const uint32_t ent  = jb.x, i = jb.y;
                 const uint32_t sj   = jb.z & 0xffffu, sk = jb.z >> 16;
                 const uint32_t side = ( jb.w >> 16 ) & 0xffu;
+                // the empty jobs of an atom whose entries did not fit (a build that is redone larger)
+                if ( i >= b.n || ent >= b.capProbes || sj >= b.cap || sk >= b.cap )
+                    continue;
                 const size_t   row  = (size_t)i * b.cap;
                 const float4   ai = b.atoms[ i ], aj = b.atoms[ b.nbr[ row + sj ] ], ak = b.atoms[ b.nbr[ row + sk ] ];
                 int4           cid  = b.stageCid[ ent ];
@@ -1998,6 +2014,8 @@ namespace sesgb
                 const uint4    jb  = b.jobs[ b.capProbes - 1u - g ];
                 const uint32_t ent = jb.x, i = jb.y;
                 const uint32_t sj  = jb.z & 0xffffu, sk = jb.z >> 16;
+                if ( i >= b.n || ent + 1u >= b.capProbes || sj >= b.cap || sk >= b.cap )
+                    continue; // an empty job
                 const size_t   row = (size_t)i * b.cap;
                 const float4   ai = b.atoms[ i ], aj = b.atoms[ b.nbr[ row + sj ] ], ak = b.atoms[ b.nbr[ row + sk ] ];
                 d3             x[ 2 ];
