@@ -1920,9 +1920,11 @@ namespace sesgb
             }
         }
 
-        // W warps per block; with kQueue the grid is persistent and its warps take atoms from a
-        // work counter (in sorted order: molecule by molecule, reference-grid cell by cell), else
-        // warp w of block k takes atom k W + w
+        // W warps per block; with kQueue the grid is persistent and its warps take tiles of atoms
+        // from a work counter (in sorted order: molecule by molecule, reference-grid cell by cell),
+        // else warp w of block k takes atom k W + w (the default: the block scheduler hands out the
+        // atoms with no counter atomic, measured 50 us faster at 100k atoms)
+        constexpr uint32_t kProbeTile = 4;
         template<int W, bool kQueue>
         __global__ void __launch_bounds__( 32 * W, 32 / W ) k_probes( Build b )
         {
@@ -1937,16 +1939,21 @@ namespace sesgb
                     probes_of_atom( b, i, mine );
                 return;
             }
-            for ( uint32_t it = 0; it < b.n; it++ ) // bounded: every turn takes a new atom
+            // work items: tiles of kProbeTile consecutive atoms of the sorted order (molecule by
+            // molecule, reference-grid cell by cell), one counter atomic per tile
+            for ( uint32_t it = 0; it < b.n; it++ ) // bounded: every turn takes a new tile
             {
-                uint32_t i = 0;
+                uint32_t t = 0;
                 if ( lane == 0 )
-                    i = atomicAdd( &b.counts->probeCursor, 1u );
-                i = __shfl_sync( 0xffffffffu, i, 0 );
-                if ( i >= b.n )
+                    t = atomicAdd( &b.counts->probeCursor, kProbeTile );
+                t = __shfl_sync( 0xffffffffu, t, 0 );
+                if ( t >= b.n )
                     break;
-                probes_of_atom( b, i, mine );
-                __syncwarp();
+                for ( uint32_t i = t; i < t + kProbeTile && i < b.n; i++ )
+                {
+                    probes_of_atom( b, i, mine );
+                    __syncwarp();
+                }
             }
         }
 
