@@ -2323,10 +2323,15 @@ namespace sesgb
                 const bool     isSecondary = (int)i == sids.x && (int)j == sids.z;
                 const bool     reverse     = ( spos.w < 0.f ) != isSecondary; // direction < 0
 
-                // float32 keys, coordinates relative to atom i
+                // float32 keys, coordinates relative to atom i. Two probes need none: the first
+                // probe's key is 0 and every other key is >= 0, so the stable order is (0, 1)
+                // whatever the keys (the circles of two probes are most of them)
                 float   key[ kSegBuf ];
                 uint8_t ord[ kSegBuf ];
-                bool    exact = true;
+                ord[ 0 ]   = 0;
+                ord[ 1 ]   = 1;
+                bool exact = true;
+                if ( nb > 2 )
                 {
                     const float Ri = ai.w + b.rp, Rj = aj.w + b.rp;
                     const f3    dj = F3( aj.x - ai.x, aj.y - ai.y, aj.z - ai.z );
@@ -2368,7 +2373,7 @@ namespace sesgb
                         if ( key[ m ] - key[ m - 1 ] < kKeyTol )
                             exact = false;
                 }
-                if ( !exact && !segment_order_ff( b, ai, aj, spos, lst, nb, reverse, ord ) )
+                if ( nb > 2 && !exact && !segment_order_ff( b, ai, aj, spos, lst, nb, reverse, ord ) )
                 {
                     // double-precision keys (the oracle's), same stable ordering
                     fp64++;
