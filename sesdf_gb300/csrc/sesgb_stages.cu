@@ -1787,7 +1787,9 @@ namespace sesgb
                 bandHere += __popc( __ballot_sync( 0xffffffffu, band ) );
             }
             // the staging chunk and the fill-job slots in one 64-bit atomic: every atom's warp adds
-            // to these counters, and a contended atomic whose result a warp waits for is costly
+            // to these counters, and a contended atomic whose result a warp waits for is costly. The
+            // low word (staged entries, at most kProbeBuf per atom) cannot carry into the high word
+            // below 2^25 atoms; far below that the build's 32-bit capacities overflow and regrow first
             uint32_t chunk = 0, jbase = 0;
             if ( lane == 0 )
             {
