@@ -127,35 +127,49 @@ namespace sesgb
         }
 
         // Bitonic sort of up to 64 keys held in registers, two per lane: key
-        // index lane + 32 r is held in v[r]; ascending on return.
-        template<class T> __device__ __forceinline__ void warp_sort64( T & v0, T & v1, bool two )
+        // index lane + 32 r is held in v[r]; ascending on return. The network is
+        // unrolled at compile time for 32 and for 64 keys (the partner distance and
+        // direction of every step are constants): the loop form with a run-time size
+        // cost the neighbour search ~54 us per 100k atoms, most of it loop control.
+        template<class T, bool kTwo> __device__ __forceinline__ void warp_sort_net( T & v0, T & v1 )
         {
-            const uint32_t lane = lane_id();
-            const uint32_t top  = two ? 64u : 32u;
+            const uint32_t     lane = lane_id();
+            constexpr uint32_t top  = kTwo ? 64u : 32u;
+#pragma unroll
             for ( uint32_t k = 2; k <= top; k <<= 1 )
+            {
+#pragma unroll
                 for ( uint32_t j = k >> 1; j > 0; j >>= 1 )
                 {
                     if ( j == 32 )
                     {
                         // partner in the lane's other register; k == 64: ascending
                         const T lo = min( v0, v1 ), hi = max( v0, v1 );
-                        v0 = lo;
-                        v1 = hi;
+                        v0         = lo;
+                        v1         = hi;
                         continue;
                     }
                     const bool lower = ( lane & j ) == 0;
                     {
-                        const T        p   = __shfl_xor_sync( 0xffffffffu, v0, j );
-                        const bool     asc = ( lane & k ) == 0;
-                        v0                 = ( lower == asc ) ? min( v0, p ) : max( v0, p );
+                        const T    p   = __shfl_xor_sync( 0xffffffffu, v0, j );
+                        const bool asc = ( lane & k ) == 0;
+                        v0             = ( lower == asc ) ? min( v0, p ) : max( v0, p );
                     }
-                    if ( two )
+                    if ( kTwo )
                     {
-                        const T        p   = __shfl_xor_sync( 0xffffffffu, v1, j );
-                        const bool     asc = ( ( lane + 32u ) & k ) == 0;
-                        v1                 = ( lower == asc ) ? min( v1, p ) : max( v1, p );
+                        const T    p   = __shfl_xor_sync( 0xffffffffu, v1, j );
+                        const bool asc = ( ( lane + 32u ) & k ) == 0;
+                        v1             = ( lower == asc ) ? min( v1, p ) : max( v1, p );
                     }
                 }
+            }
+        }
+        template<class T> __device__ __forceinline__ void warp_sort64( T & v0, T & v1, bool two )
+        {
+            if ( two )
+                warp_sort_net<T, true>( v0, v1 );
+            else
+                warp_sort_net<T, false>( v0, v1 );
         }
 
         // ---- molecules of a batch ---------------------------------------------
