@@ -1723,20 +1723,32 @@ namespace sesgb
                     uint32_t       sj = 0, sk = 0;
                     if ( c < total )
                     {
-                        uint32_t lo = 0, hi = p; // last circle whose first candidate is <= c
-                        while ( hi - lo > 1 )
+                        // last circle whose first candidate is <= c (at most 64 circles here)
+                        uint32_t lo = 0;
+#pragma unroll
+                        for ( uint32_t step = 32; step > 0; step >>= 1 )
+                            if ( lo + step < p && m.coff[ lo + step ] <= c )
+                                lo += step;
+                        // its r-th candidate: the r-th set bit of the mask (r from 0), found by halving
+                        const uint64_t w  = later( lo );
+                        uint32_t       r  = c - m.coff[ lo ];
+                        const uint32_t wl = (uint32_t)w, nl = __popc( wl );
+                        uint32_t       word = r < nl ? wl : (uint32_t)( w >> 32 );
+                        uint32_t       pos  = r < nl ? 0u : 32u;
+                        r                   = r < nl ? r : r - nl;
+#pragma unroll
+                        for ( uint32_t h = 16; h > 0; h >>= 1 )
                         {
-                            const uint32_t mid = ( lo + hi ) >> 1;
-                            if ( m.coff[ mid ] <= c )
-                                lo = mid;
-                            else
-                                hi = mid;
+                            const uint32_t cnt = __popc( word & ( ( 1u << h ) - 1u ) );
+                            if ( r >= cnt )
+                            {
+                                r -= cnt;
+                                word >>= h;
+                                pos += h;
+                            }
                         }
-                        uint64_t w = later( lo );
-                        for ( uint32_t r = c - m.coff[ lo ]; r; r-- )
-                            w &= w - 1;
-                        sj  = m.plist[ lo ];
-                        sk  = (uint32_t)( __ffsll( (long long)w ) - 1 );
+                        sj = m.plist[ lo ];
+                        sk = pos;
                         isC = pair_is_neighbor( b, m, pb, sj, sk, fp64 );
                     }
                     enqueue( isC, sj, sk );
