@@ -1508,15 +1508,19 @@ namespace sesgb
             if ( useMask )
             {
                 // only an atom that touches both circles (i, j) and (i, k) can hold a point of both
-                for ( uint64_t occ = m.touch[ sj ] & m.touch[ sk ] & ~( ( 1ull << sj ) | ( 1ull << sk ) ); occ; occ &= occ - 1 )
-                {
-                    const int r = occlude( (uint32_t)( __ffsll( (long long)occ ) - 1 ) );
-                    if ( r )
+                // in ascending slot order, one 32-bit half of the mask at a time
+                const uint64_t occ = m.touch[ sj ] & m.touch[ sk ] & ~( ( 1ull << sj ) | ( 1ull << sk ) );
+#pragma unroll
+                for ( uint32_t h = 0; h < 2; h++ )
+                    for ( uint32_t w = (uint32_t)( occ >> ( 32 * h ) ); w; w &= w - 1 )
                     {
-                        band = r == 1;
-                        return;
+                        const int r = occlude( 32u * h + (uint32_t)( __ffs( (int)w ) - 1 ) );
+                        if ( r )
+                        {
+                            band = r == 1;
+                            return;
+                        }
                     }
-                }
             }
             else
             {
