@@ -2467,6 +2467,11 @@ namespace sesgb
             const uint32_t                warp = threadIdx.x >> 5, lane = lane_id();
             const uint32_t                Q    = min( b.counts->Q, b.capProbes );
             const float                   t2   = 2.f * b.rp;
+            // one molecule: the reference-grid hash has 3 log2(size) bits and the index of a singular
+            // probe pBits; when they fit in 31 bits the keys are sorted as 32-bit values
+            const uint32_t pBits  = Q > 1 ? 32u - (uint32_t)__clz( (int)( Q - 1u ) ) : 1u;
+            const uint32_t hBits  = 3u * ( 31u - (uint32_t)__clz( b.grid.size > 0 ? b.grid.size : 1 ) );
+            const bool     narrow = b.nMol <= 1 && hBits + pBits <= 31u;
             uint32_t                      fp64 = 0, trunc = 0;
             for ( uint32_t q = blockIdx.x * kWarpsPerBlock + warp; q < Q; q += gridDim.x * kWarpsPerBlock )
             {
@@ -2529,7 +2534,20 @@ namespace sesgb
                     // in registers (the common case)
                     key0                    = lane < held ? buf[ warp ][ lane ] : ~0ull;
                     unsigned long long key1 = lane + 32 < held ? buf[ warp ][ lane + 32 ] : ~0ull;
-                    warp_sort64( key0, key1, held > 32 );
+                    if ( narrow )
+                    {
+                        // (hash, index) packed into 32 bits where both fit below the padding value:
+                        // the same order with half the shuffles and compares
+                        const auto pack = [ & ]( unsigned long long k ) {
+                            return k == ~0ull ? 0xffffffffu : ( (uint32_t)( k >> 32 ) << pBits ) | (uint32_t)k;
+                        };
+                        uint32_t n0 = pack( key0 ), n1 = pack( key1 );
+                        warp_sort64( n0, n1, held > 32 );
+                        key0 = n0 == 0xffffffffu ? ~0ull
+                                                 : ( (unsigned long long)( n0 >> pBits ) << 32 ) | ( n0 & ( ( 1u << pBits ) - 1u ) );
+                    }
+                    else
+                        warp_sort64( key0, key1, held > 32 );
                 }
                 else
                 {
